@@ -1,0 +1,508 @@
+// extern "C" entry points of libchgpu.so (declared in include/chgpu.h).
+//
+// One handle = one channel run on the current device: the field V in a
+// plane-major layout [component][y-plane][mode] (mode = ix*(2nz+1)+iz+nz,
+// contiguous), the RK history, the spectra of the six products of every
+// plane, the x/z work buffers of the transforms, the y-discretisation tables
+// and the module scalars (time, deltat, flow rates, pressure-gradient
+// corrections, CFL), all resident on the device.  A whole time step
+// (channel.f90:118-167) is a fixed sequence of launches reading every
+// dynamic value (deltat, lambda) from device memory, captured once into a
+// CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/chgpu.h"
+#include "chgpu_internal.h"
+#include "kernels.cuh"
+
+using namespace chgpu;
+
+namespace {
+
+constexpr double RK[3][3] = {
+    {120.0 / 32.0, 2.0, 0.0},
+    {120.0 / 8.0, 50.0 / 8.0, 34.0 / 8.0},
+    {120.0 / 20.0, 90.0 / 20.0, 50.0 / 20.0}};  // dnsdata.f90:70-72
+
+thread_local std::string g_create_error;
+
+}  // namespace
+
+struct chgpu_handle {
+  chgpu_params p{};
+  Dims d{};
+  BcRows bc{};
+  Tables tab;
+  RadixDev rz{}, rx{};
+  int mixed = 0;
+  int zcols = 1, xrows = 1;
+  cudaStream_t stream = nullptr;
+  // device buffers
+  double2* V = nullptr;
+  void* old = nullptr;
+  void* VV = nullptr;
+  void* Zb = nullptr;
+  void* Pb = nullptr;
+  double2* rhs = nullptr;
+  double* fac = nullptr;
+  double* der = nullptr;
+  double* d0lu = nullptr;
+  double* yint = nullptr;
+  double* dy = nullptr;
+  void* twz = nullptr;
+  void* twx = nullptr;
+  void* twh = nullptr;
+  DevScalars* sc = nullptr;
+  DevScalars* sc_host = nullptr;  // pinned
+  cudaGraphExec_t graph = nullptr;
+  bool field_set = false;
+  long long launches = 0;
+  std::string err;
+};
+
+namespace {
+
+int fail(chgpu_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  else g_create_error = msg;
+  return code;
+}
+
+int cuda_fail(chgpu_handle* h, cudaError_t e, const char* where) {
+  return fail(h, e == cudaErrorMemoryAllocation ? CHGPU_E_NOMEM : CHGPU_E_CUDA,
+              std::string(where) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+}
+
+#define CK(h, call)                                         \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return cuda_fail((h), e_, #call); \
+  } while (0)
+
+size_t tsize(const chgpu_handle* h) { return h->mixed ? sizeof(float2) : sizeof(double2); }
+
+template <typename V2>
+std::vector<V2> roots(int n) {  // forward roots exp(-2 pi i m/n), from the mathematics in extended precision
+  std::vector<V2> w(n);
+  for (int m = 0; m < n; ++m) {
+    long double ang = 2.0L * 3.14159265358979323846264338327950288L * (long double)m / (long double)n;
+    w[m].x = (decltype(w[m].x))cosl(ang);
+    w[m].y = (decltype(w[m].x))(-sinl(ang));
+  }
+  return w;
+}
+
+template <typename V2>
+int upload_roots(chgpu_handle* h, void** dst, int n) {
+  std::vector<V2> w = roots<V2>(n);
+  CK(h, cudaMalloc(dst, sizeof(V2) * n));
+  CK(h, cudaMemcpy(*dst, w.data(), sizeof(V2) * n, cudaMemcpyHostToDevice));
+  return 0;
+}
+
+ConvLaunch conv_launch(chgpu_handle* h, int compute_cfl, int products, int plane0, int nplanes) {
+  ConvLaunch L{};
+  L.d = h->d;
+  L.rz = h->rz;
+  L.rx = h->rx;
+  L.V = h->V;
+  L.Zb = h->Zb;
+  L.Pb = h->Pb;
+  L.VV = h->VV;
+  L.twz = h->twz;
+  L.twx = h->twx;
+  L.twh = h->twh;
+  L.dy = h->dy;
+  L.sc = h->sc;
+  L.zcols = h->zcols;
+  L.xrows = h->xrows;
+  L.plane0 = plane0;
+  L.nplanes = nplanes;
+  L.compute_cfl = compute_cfl;
+  L.products = products;
+  return L;
+}
+
+SolveLaunch solve_launch(chgpu_handle* h, const double* ode) {
+  SolveLaunch L{};
+  L.d = h->d;
+  L.bc = h->bc;
+  L.V = h->V;
+  L.VV = h->VV;
+  L.old = h->old;
+  L.rhs = h->rhs;
+  L.fac = h->fac;
+  L.der = h->der;
+  L.d0lu = h->d0lu;
+  L.yint = h->yint;
+  L.sc = h->sc;
+  if (ode) {
+    L.ode[0] = ode[0];
+    L.ode[1] = ode[1];
+    L.ode[2] = ode[2];
+  }
+  return L;
+}
+
+void run_convolutions(chgpu_handle* h, int compute_cfl, int products, int plane0, int nplanes) {
+  ConvLaunch L = conv_launch(h, compute_cfl, products, plane0, nplanes);
+  if (h->mixed) launch_convolutions<float>(L, h->stream);
+  else launch_convolutions<double>(L, h->stream);
+  h->launches += products ? 3 : 2;
+}
+
+void run_rhs(chgpu_handle* h, const double* ode) {
+  SolveLaunch L = solve_launch(h, ode);
+  if (h->mixed) launch_rhs<float>(L, h->stream);
+  else launch_rhs<double>(L, h->stream);
+  h->launches += 1;
+}
+
+// rhs_in_field: read the right-hand sides from V (the reference's in-place
+// convention) instead of the separate buffer k_rhs writes.
+void run_linsolve(chgpu_handle* h, double ode1, double lambda, int from_dt, bool rhs_in_field) {
+  SolveLaunch L = solve_launch(h, nullptr);
+  L.ode[0] = ode1;
+  L.lambda = lambda;
+  L.lambda_from_dt = from_dt;
+  if (rhs_in_field) {
+    L.rhs_src = h->V;
+    L.rhs_cstride = (size_t)h->d.nplanes * h->d.nmodes;
+    L.rhs_plane_off = 1;
+  } else {
+    L.rhs_src = h->rhs;
+    L.rhs_cstride = (size_t)(h->d.ny - 1) * h->d.nmodes;
+    L.rhs_plane_off = -1;
+  }
+  launch_linsolve(L, h->stream);
+  h->launches += 1;
+}
+
+void run_outstats(chgpu_handle* h) {
+  SolveLaunch L = solve_launch(h, nullptr);
+  launch_outstats(L, h->stream);
+  h->launches += 1;
+}
+
+// One time-loop iteration (channel.f90:118-167) on the stream.
+void enqueue_step(chgpu_handle* h) {
+  for (int k = 0; k < 3; ++k) {
+    launch_advance_time(h->sc, 2.0 / RK[k][0], k == 0, h->stream);
+    h->launches += 1;
+    run_convolutions(h, k == 2, 1, 0, h->d.nplanes);
+    run_rhs(h, RK[k]);
+    run_linsolve(h, RK[k][0], 0.0, 1, false);
+  }
+  run_outstats(h);
+}
+
+void fill_stats(const chgpu_handle* h, chgpu_stats* st) {
+  const DevScalars& s = *h->sc_host;
+  std::memcpy(st->line, s.line, sizeof st->line);
+  std::memcpy(st->fr, s.fr, sizeof st->fr);
+  st->corrpx = s.corrpx;
+  st->corrpz = s.corrpz;
+  st->meanpx = s.meanpx;
+  st->meanpz = s.meanpz;
+  st->cfl = s.runtime_global;
+  st->deltat = s.deltat;
+  st->time = s.time;
+  st->istep = s.istep;
+}
+
+int pull_scalars(chgpu_handle* h) {
+  CK(h, cudaMemcpyAsync(h->sc_host, h->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  if (h->sc_host->error & 1) return fail(h, CHGPU_E_NONFINITE, "non-finite CFL or statistics (flow field blew up)");
+  return 0;
+}
+
+void release(chgpu_handle* h) {
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  void* bufs[] = {h->V, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->d0lu, h->yint, h->dy,
+                  h->twz, h->twx, h->twh, h->sc};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  if (h->sc_host) cudaFreeHost(h->sc_host);
+  if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* chgpu_last_error(const chgpu_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
+  if (!p || !out) return fail(nullptr, CHGPU_E_PARAM, "chgpu_create: null argument");
+  *out = nullptr;
+  if (p->nx < 1 || p->nz < 1 || p->ny < 8)
+    return fail(nullptr, CHGPU_E_PARAM, "chgpu_create: need nx>=1, nz>=1, ny>=8");
+  if (!(p->ymax > p->ymin) || !(p->a > 0) || !(p->alfa0 > 0) || !(p->beta0 > 0) || !(p->ni > 0))
+    return fail(nullptr, CHGPU_E_PARAM, "chgpu_create: need ymax>ymin, a>0, alfa0>0, beta0>0, ni>0");
+  if (p->precision != CHGPU_FP64 && p->precision != CHGPU_MIXED)
+    return fail(nullptr, CHGPU_E_PARAM, "chgpu_create: precision must be CHGPU_FP64 or CHGPU_MIXED");
+  if (p->cpi && p->cpi_type != 0 && p->cpi_type != 1)
+    return fail(nullptr, CHGPU_E_PARAM, "Wrong selection of CPI_Type");  // linsolve_blocking.inc:93-95
+  chgpu_handle* h = new (std::nothrow) chgpu_handle();
+  if (!h) return fail(nullptr, CHGPU_E_NOMEM, "chgpu_create: host allocation failed");
+  h->p = *p;
+  h->mixed = p->precision == CHGPU_MIXED;
+  int nxd, nzd;
+  padded_sizes(p->nx, p->nz, &nxd, &nzd);
+  Dims& d = h->d;
+  d.nx = p->nx; d.ny = p->ny; d.nz = p->nz;
+  d.nzt = 2 * p->nz + 1;
+  d.nxd = nxd; d.nzd = nzd;
+  d.nplanes = p->ny + 3;
+  d.nmodes = (p->nx + 1) * d.nzt;
+  d.npairs = (p->nx + 1) * (p->nz + 1);
+  d.alfa0 = p->alfa0; d.beta0 = p->beta0; d.ni = p->ni;
+  const double PI = 3.1415926535897932384626433832795028841971;
+  const double dx = PI / (p->alfa0 * nxd), dz = 2.0 * PI / (p->beta0 * nzd);
+  d.factor = 1.0 / (2.0 * nxd * nzd);  // dnsdata.f90:124
+  d.rdx = 1.0 / dx;
+  d.rdz = 1.0 / dz;
+  d.meanflowx = p->meanflowx; d.meanflowz = p->meanflowz;
+  d.cflmax = p->cflmax; d.gamma = p->gamma;
+  d.cpi = p->cpi; d.cpi_type = p->cpi_type;
+  compute_tables(*p, h->tab);
+  const Tables& t = h->tab;
+  std::memcpy(h->bc.v0bc, t.v0bc, 40); std::memcpy(h->bc.v0m1bc, t.v0m1bc, 40);
+  std::memcpy(h->bc.eta0bc, t.eta0bc, 40); std::memcpy(h->bc.eta0m1bc, t.eta0m1bc, 40);
+  std::memcpy(h->bc.vnbc, t.vnbc, 40); std::memcpy(h->bc.vnp1bc, t.vnp1bc, 40);
+  std::memcpy(h->bc.etanbc, t.etanbc, 40); std::memcpy(h->bc.etanp1bc, t.etanp1bc, 40);
+  std::memcpy(h->bc.d140, t.d140, 40); std::memcpy(h->bc.d14m1, t.d14m1, 40);
+  std::memcpy(h->bc.d14n, t.d14n, 40); std::memcpy(h->bc.d14np1, t.d14np1, 40);
+  Radix rz = make_radix(nzd), rx = make_radix(nxd);
+  if (rz.nst < 0 || rx.nst < 0) { delete h; return fail(nullptr, CHGPU_E_PARAM, "unsupported FFT length"); }
+  h->rz.n = rz.n; h->rz.nst = rz.nst; std::memcpy(h->rz.r, rz.r, sizeof rz.r);
+  h->rx.n = rx.n; h->rx.nst = rx.nst; std::memcpy(h->rx.r, rx.r, sizeof rx.r);
+  // tiles: columns per z-transform block and rows per x block, from the
+  // shared-memory budget (two ping-pong buffers; nine row buffers)
+  const size_t ts = tsize(h);
+  h->zcols = (int)std::max<size_t>(1, std::min<size_t>(8, (100 * 1024) / (2 * (size_t)nzd * ts)));
+  h->xrows = 1;
+  while (h->xrows < 4 && 9 * (size_t)(2 * h->xrows) * nxd * ts <= 200 * 1024 && nzd % (2 * h->xrows) == 0)
+    h->xrows *= 2;
+  if (9 * (size_t)h->xrows * nxd * ts > 227 * 1024 || 2 * (size_t)nzd * ts > 227 * 1024) {
+    delete h;
+    return fail(nullptr, CHGPU_E_PARAM, "transform length too large for one thread block");
+  }
+  int rc = 0;
+  auto dev_alloc = [&](void** ptr, size_t bytes, const char* what) -> int {
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e != cudaSuccess) return cuda_fail(h, e, what);
+    return 0;
+  };
+  const size_t nplanes = d.nplanes, nmodes = d.nmodes, nxp = p->nx + 1;
+  do {
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { rc = cuda_fail(h, e, "cudaStreamCreate"); break; }
+    e = conv_set_smem_limits();
+    if (e != cudaSuccess) { rc = cuda_fail(h, e, "cudaFuncSetAttribute"); break; }
+    if ((rc = dev_alloc((void**)&h->V, sizeof(double2) * 3 * nplanes * nmodes, "field"))) break;
+    if ((rc = dev_alloc(&h->old, ts * 2 * (p->ny - 1) * nmodes, "RK history"))) break;
+    if ((rc = dev_alloc(&h->VV, ts * 6 * nplanes * nmodes, "product spectra"))) break;
+    if ((rc = dev_alloc(&h->Zb, ts * 3 * nplanes * nxp * nzd, "z work buffer"))) break;
+    if ((rc = dev_alloc(&h->Pb, std::max(ts * 6 * nplanes * nxp * nzd, sizeof(double2) * 3 * nplanes * nmodes),
+                        "x work buffer"))) break;
+    if ((rc = dev_alloc((void**)&h->rhs, sizeof(double2) * 2 * (p->ny - 1) * nmodes, "rhs"))) break;
+    if ((rc = dev_alloc((void**)&h->fac, sizeof(double) * 4 * (p->ny - 1) * (size_t)d.npairs, "factors"))) break;
+    if ((rc = dev_alloc((void**)&h->der, sizeof(double) * t.der.size(), "der"))) break;
+    if ((rc = dev_alloc((void**)&h->d0lu, sizeof(double) * t.d0lu.size(), "D0mat"))) break;
+    if ((rc = dev_alloc((void**)&h->yint, sizeof(double) * std::max<size_t>(3, t.yint.size()), "yint"))) break;
+    if ((rc = dev_alloc((void**)&h->dy, sizeof(double) * t.dy.size(), "dy"))) break;
+    if ((rc = dev_alloc((void**)&h->sc, sizeof(DevScalars), "scalars"))) break;
+    e = cudaMallocHost((void**)&h->sc_host, sizeof(DevScalars));
+    if (e != cudaSuccess) { rc = cuda_fail(h, e, "cudaMallocHost"); break; }
+    if (h->mixed) {
+      if ((rc = upload_roots<float2>(h, &h->twz, nzd))) break;
+      if ((rc = upload_roots<float2>(h, &h->twx, nxd))) break;
+      if ((rc = upload_roots<float2>(h, &h->twh, 2 * nxd))) break;
+    } else {
+      if ((rc = upload_roots<double2>(h, &h->twz, nzd))) break;
+      if ((rc = upload_roots<double2>(h, &h->twx, nxd))) break;
+      if ((rc = upload_roots<double2>(h, &h->twh, 2 * nxd))) break;
+    }
+    cudaMemcpy(h->der, t.der.data(), sizeof(double) * t.der.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(h->d0lu, t.d0lu.data(), sizeof(double) * t.d0lu.size(), cudaMemcpyHostToDevice);
+    if (!t.yint.empty()) cudaMemcpy(h->yint, t.yint.data(), sizeof(double) * t.yint.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(h->dy, t.dy.data(), sizeof(double) * t.dy.size(), cudaMemcpyHostToDevice);
+    cudaMemset(h->V, 0, sizeof(double2) * 3 * nplanes * nmodes);
+    cudaMemset(h->old, 0, ts * 2 * (p->ny - 1) * nmodes);  // oldrhs starts at zero (RK1 has ODE(3)=0)
+    DevScalars s{};
+    s.deltat = p->deltat;
+    s.time = p->time;
+    s.meanpx = p->meanpx;
+    s.meanpz = p->meanpz;
+    s.u0 = p->u0;
+    s.uN = p->uN;
+    *h->sc_host = s;
+    e = cudaMemcpy(h->sc, &s, sizeof s, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { rc = cuda_fail(h, e, "upload scalars"); break; }
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) { rc = cuda_fail(h, e, "set-up"); break; }
+  } while (0);
+  if (rc) {
+    g_create_error = h->err;
+    release(h);
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return 0;
+}
+
+int chgpu_destroy(chgpu_handle* h) {
+  if (!h) return 0;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  release(h);
+  delete h;
+  return 0;
+}
+
+size_t chgpu_field_doubles(const chgpu_handle* h) { return h ? (size_t)2 * 3 * h->d.nplanes * h->d.nmodes : 0; }
+
+int chgpu_upload_field(chgpu_handle* h, const double* V) {
+  if (!h || !V) return fail(h, CHGPU_E_PARAM, "chgpu_upload_field: null argument");
+  const size_t n = (size_t)3 * h->d.nplanes * h->d.nmodes;
+  double2* stage = reinterpret_cast<double2*>(h->Pb);
+  CK(h, cudaMemcpyAsync(stage, V, sizeof(double2) * n, cudaMemcpyHostToDevice, h->stream));
+  // restart order per component: [mode][iy] -> device [iy][mode]
+  launch_transpose(stage, h->V, h->d.nmodes, h->d.nplanes, 3, h->stream);
+  h->launches += 1;
+  CK(h, cudaGetLastError());
+  CK(h, cudaStreamSynchronize(h->stream));
+  h->field_set = true;
+  return 0;
+}
+
+int chgpu_download_field(chgpu_handle* h, double* V) {
+  if (!h || !V) return fail(h, CHGPU_E_PARAM, "chgpu_download_field: null argument");
+  const size_t n = (size_t)3 * h->d.nplanes * h->d.nmodes;
+  double2* stage = reinterpret_cast<double2*>(h->Pb);
+  launch_transpose(h->V, stage, h->d.nplanes, h->d.nmodes, 3, h->stream);
+  h->launches += 1;
+  CK(h, cudaGetLastError());
+  CK(h, cudaMemcpyAsync(V, stage, sizeof(double2) * n, cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int chgpu_start(chgpu_handle* h, double time, double deltat, chgpu_stats* st) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "chgpu_start: null handle");
+  if (!h->field_set) return fail(h, CHGPU_E_STATE, "chgpu_start: upload the field first");
+  if (deltat == 0) deltat = 1.0;  // channel.f90:97
+  DevScalars s = *h->sc_host;
+  CK(h, cudaMemcpyAsync(h->sc_host, h->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  s = *h->sc_host;
+  s.time = time;
+  s.deltat = deltat;
+  s.cfl = 0.0;
+  s.istep = 0;
+  *h->sc_host = s;
+  CK(h, cudaMemcpyAsync(h->sc, h->sc_host, sizeof(DevScalars), cudaMemcpyHostToDevice, h->stream));
+  run_convolutions(h, 1, 0, 2, h->d.ny - 1);  // planes iy=1..ny-1 (channel.f90:96-99)
+  SolveLaunch L = solve_launch(h, nullptr);
+  launch_flowrate(L, h->stream);
+  h->launches += 1;
+  run_outstats(h);
+  CK(h, cudaGetLastError());
+  int rc = pull_scalars(h);
+  if (st) fill_stats(h, st);
+  return rc;
+}
+
+int chgpu_set_wall_velocity(chgpu_handle* h, double u0, double uN) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "null handle");
+  double v[2] = {u0, uN};
+  CK(h, cudaMemcpyAsync(&h->sc->u0, v, sizeof v, cudaMemcpyHostToDevice, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int chgpu_buildrhs(chgpu_handle* h, const double ode[3], int compute_cfl) {
+  if (!h || !ode) return fail(h, CHGPU_E_PARAM, "chgpu_buildrhs: null argument");
+  if (!h->field_set) return fail(h, CHGPU_E_STATE, "chgpu_buildrhs: upload the field first");
+  run_convolutions(h, compute_cfl ? 1 : 0, 1, 0, h->d.nplanes);
+  run_rhs(h, ode);
+  // write-back of the new right-hand sides into V(1:ny-1, :, :, 1:2) (dnsdata.f90:667-670)
+  const size_t rows = (size_t)(h->d.ny - 1) * h->d.nmodes;
+  for (int c = 0; c < 2; ++c)
+    CK(h, cudaMemcpyAsync(h->V + ((size_t)c * h->d.nplanes + 2) * h->d.nmodes, h->rhs + c * rows,
+                          sizeof(double2) * rows, cudaMemcpyDeviceToDevice, h->stream));
+  CK(h, cudaGetLastError());
+  return 0;
+}
+
+int chgpu_linsolve(chgpu_handle* h, double lambda) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "chgpu_linsolve: null handle");
+  run_linsolve(h, 0.0, lambda, 0, true);
+  CK(h, cudaGetLastError());
+  return 0;
+}
+
+int chgpu_outstats(chgpu_handle* h, chgpu_stats* st) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "chgpu_outstats: null handle");
+  run_outstats(h);
+  CK(h, cudaGetLastError());
+  int rc = pull_scalars(h);
+  if (st) fill_stats(h, st);
+  return rc;
+}
+
+int chgpu_step(chgpu_handle* h, chgpu_stats* st) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "chgpu_step: null handle");
+  if (!h->field_set) return fail(h, CHGPU_E_STATE, "chgpu_step: upload the field first");
+  if (!h->graph) {
+    cudaGraph_t g = nullptr;
+    CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const long long before = h->launches;
+    enqueue_step(h);
+    h->launches = before;
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      h->graph = nullptr;
+      return cuda_fail(h, e, "cudaGraphInstantiate");
+    }
+  }
+  CK(h, cudaGraphLaunch(h->graph, h->stream));
+  h->launches += 19;  // 3 x (time advance, 3 transform kernels, rhs, linsolve) + outstats
+  if (st) {
+    int rc = pull_scalars(h);
+    fill_stats(h, st);
+    return rc;
+  }
+  return 0;
+}
+
+int chgpu_get_stats(chgpu_handle* h, chgpu_stats* st) {
+  if (!h || !st) return fail(h, CHGPU_E_PARAM, "chgpu_get_stats: null argument");
+  int rc = pull_scalars(h);
+  fill_stats(h, st);
+  return rc;
+}
+
+int chgpu_synchronize(chgpu_handle* h) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "null handle");
+  return pull_scalars(h);
+}
+
+void* chgpu_stream(chgpu_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+long long chgpu_launch_count(const chgpu_handle* h) { return h ? h->launches : 0; }
+
+}  // extern "C"

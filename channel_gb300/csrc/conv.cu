@@ -1,0 +1,259 @@
+// The nonlinear terms of every y-plane: `convolutions` of the reference
+// (dnsdata.f90:487-602) as three batched shared-memory FFT kernels.
+//
+//   k_zinv : z-backward transform of u,v,w per (plane, column kx), with the
+//            3/2 zero band inserted while loading (dnsdata.f90:504-510).
+//            Writes Zb[c][plane][ix][jz] (physical z, spectral x).
+//   k_xrow : per (plane, rows jz): c2r in x of u,v,w (dnsdata.f90:533-535,
+//            real-to-complex packing into half-length transforms), the CFL
+//            maximum (:552-556), the six products times `factor`
+//            (:581-584), r2c of the products keeping kx<=nx (:586) -- the
+//            z<->x pencil transposes (mpi_transpose.f90:50-117) are the
+//            strided loads/stores of this kernel.  Writes Pb[p][plane][ix][jz].
+//   k_zfwd : z-forward transform of the six products per (plane, column),
+//            keeping |kz|<=nz (:590, truncation read by buildrhs :609).
+//            Writes VV[p][plane][mode].
+//
+// T is the arithmetic type: double (plain FP64 step) or float (mixed step).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "chgpu_internal.h"
+#include "cplx.cuh"
+#include "kernels.cuh"
+
+namespace chgpu {
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_zinv(const double2* __restrict__ V, typename C2<T>::t* __restrict__ Zb,
+                                              const typename C2<T>::t* __restrict__ twz, Dims d, RadixDev rz,
+                                              int nb_cols, int plane0) {
+  using V2 = typename C2<T>::t;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nzd = d.nzd, nz = d.nz, nxp = d.nx + 1;
+  V2* bufA = reinterpret_cast<V2*>(smem_raw);
+  V2* bufB = bufA + (size_t)nb_cols * nzd;
+  const int c = blockIdx.z;
+  const int plane = plane0 + blockIdx.y;
+  const int ix0 = blockIdx.x * nb_cols;
+  const int nb = min(nb_cols, nxp - ix0);
+  const size_t colbase = ((size_t)c * d.nplanes + plane) * nxp;
+  for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) {
+    const int b = idx / nzd;
+    const int jz = idx - b * nzd;
+    V2 val = mk<V2>((T)0, (T)0);
+    int izp = -1;
+    if (jz <= nz) izp = nz + jz;
+    else if (jz >= nzd - nz) izp = jz - nzd + nz;
+    if (izp >= 0) {
+      double2 x = V[(colbase + ix0 + b) * d.nzt + izp];
+      val = mk<V2>((T)x.x, (T)x.y);
+    }
+    bufA[idx] = val;
+  }
+  __syncthreads();
+  V2* res = fft_block<V2>(bufA, bufB, nb, rz, +1, twz);
+  for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) {
+    const int b = idx / nzd;
+    const int jz = idx - b * nzd;
+    Zb[(colbase + ix0 + b) * nzd + jz] = res[idx];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void block_max_atomic(T v, double* target) {
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __shared__ double wmax[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) wmax[wid] = (double)v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) m = wmax[i] > m ? wmax[i] : m;
+    // non-negative doubles order like their bit patterns
+    atomicMax(reinterpret_cast<unsigned long long*>(target), (unsigned long long)__double_as_longlong(m));
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_xrow(const typename C2<T>::t* __restrict__ Zb, typename C2<T>::t* __restrict__ Pb,
+                                              const typename C2<T>::t* __restrict__ twx,
+                                              const typename C2<T>::t* __restrict__ twh, const double* __restrict__ dy,
+                                              Dims d, RadixDev rx, int nrows, int plane0, int compute_cfl,
+                                              DevScalars* sc) {
+  using V2 = typename C2<T>::t;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int M = d.nxd, nx = d.nx, nxp = nx + 1, nzd = d.nzd;
+  const int plane = plane0 + blockIdx.y;
+  const int jz0 = blockIdx.x * nrows;
+  const int S = 3 * nrows * M;  // one buffer group: [3][nrows][M]
+  V2* A = reinterpret_cast<V2*>(smem_raw);
+  V2* B = A + S;
+  V2* Cb = B + S;
+  // load the three spectra rows (zTOx, x zero band; dnsdata.f90:533-535)
+  for (int idx = threadIdx.x; idx < 3 * M * nrows; idx += blockDim.x) {
+    const int r = idx % nrows;
+    const int ck = idx / nrows;
+    const int k = ck % M;
+    const int c = ck / M;
+    V2 val = mk<V2>((T)0, (T)0);
+    if (k <= nx) val = Zb[(((size_t)c * d.nplanes + plane) * nxp + k) * nzd + jz0 + r];
+    Cb[((size_t)c * nrows + r) * M + k] = val;
+  }
+  __syncthreads();
+  // c2r packing: Z[k] = (X[k]+conj(X[M-k])) + i (X[k]-conj(X[M-k])) e^{+i pi k/M}
+  for (int idx = threadIdx.x; idx < S; idx += blockDim.x) {
+    const int k = idx % M;
+    const int cr = idx / M;
+    const V2* X = Cb + (size_t)cr * M;
+    V2 xk = X[k];
+    V2 xm = mk<V2>((T)0, (T)0);
+    if (k == 0) xk.y = (T)0;  // the c2r reads only Re of the kx=0 entry
+    else xm = conjg(X[M - k]);
+    V2 e = xk + xm, o = cmul(xk - xm, conjg(twh[k]));
+    A[idx] = e + mul_i(o, +1);
+  }
+  __syncthreads();
+  V2* U = fft_block<V2>(A, B, 3 * nrows, rx, +1, twx);
+  V2* freeb = (U == A) ? B : A;
+  // CFL (dnsdata.f90:552-556) and products uu,vv,ww (:584)
+  const T f = (T)d.factor;
+  T cfl = (T)0;
+  bool bad = false;
+  const bool do_cfl = compute_cfl && plane >= 2 && plane <= d.ny;
+  const T rdx = (T)d.rdx, rdz = (T)d.rdz;
+  const T rdy = do_cfl ? (T)(1.0 / dy[plane - 1]) : (T)0;
+  for (int idx = threadIdx.x; idx < nrows * M; idx += blockDim.x) {
+    const int m = idx % M, r = idx / M;
+    V2 u = U[((size_t)0 * nrows + r) * M + m];
+    V2 v = U[((size_t)1 * nrows + r) * M + m];
+    V2 w = U[((size_t)2 * nrows + r) * M + m];
+    if (do_cfl) {
+      T c0 = fabs(u.x) * rdx + fabs(v.x) * rdy + fabs(w.x) * rdz;
+      T c1 = fabs(u.y) * rdx + fabs(v.y) * rdy + fabs(w.y) * rdz;
+      cfl = max(cfl, max(c0, c1));
+      bad = bad || !isfinite(c0) || !isfinite(c1);
+    }
+    Cb[((size_t)0 * nrows + r) * M + m] = mk<V2>(u.x * u.x * f, u.y * u.y * f);
+    Cb[((size_t)1 * nrows + r) * M + m] = mk<V2>(v.x * v.x * f, v.y * v.y * f);
+    Cb[((size_t)2 * nrows + r) * M + m] = mk<V2>(w.x * w.x * f, w.y * w.y * f);
+  }
+  if (bad) cfl = (T)INFINITY;  // a non-finite velocity shows up as an infinite CFL
+  if (compute_cfl) block_max_atomic<T>(cfl, &sc->cfl);
+  __syncthreads();
+  for (int half = 0; half < 2; ++half) {
+    if (half == 1) {  // products uv, vw, uw (dnsdata.f90:581-583)
+      for (int idx = threadIdx.x; idx < nrows * M; idx += blockDim.x) {
+        const int m = idx % M, r = idx / M;
+        V2 u = U[((size_t)0 * nrows + r) * M + m];
+        V2 v = U[((size_t)1 * nrows + r) * M + m];
+        V2 w = U[((size_t)2 * nrows + r) * M + m];
+        Cb[((size_t)0 * nrows + r) * M + m] = mk<V2>(u.x * v.x * f, u.y * v.y * f);
+        Cb[((size_t)1 * nrows + r) * M + m] = mk<V2>(v.x * w.x * f, v.y * w.y * f);
+        Cb[((size_t)2 * nrows + r) * M + m] = mk<V2>(u.x * w.x * f, u.y * w.y * f);
+      }
+      __syncthreads();
+    }
+    V2* P = fft_block<V2>(Cb, freeb, 3 * nrows, rx, -1, twx);
+    // r2c unpacking, kx = 0..nx (HFT + xTOz, dnsdata.f90:586-588)
+    for (int idx = threadIdx.x; idx < 3 * nxp * nrows; idx += blockDim.x) {
+      const int r = idx % nrows;
+      const int pk = idx / nrows;
+      const int k = pk % nxp;
+      const int p = pk / nxp;
+      const V2* Z = P + ((size_t)p * nrows + r) * M;
+      V2 zk = Z[k];
+      V2 zm = conjg(Z[k == 0 ? 0 : M - k]);
+      V2 e = scale(zk + zm, (T)0.5);
+      V2 dd = zk - zm;
+      V2 o = mk<V2>(dd.y * (T)0.5, -dd.x * (T)0.5);
+      V2 X = e + cmul(twh[k], o);
+      Pb[(((size_t)(3 * half + p) * d.nplanes + plane) * nxp + k) * nzd + jz0 + r] = X;
+    }
+    __syncthreads();
+    if (P != Cb) {  // keep Cb as the product buffer of the second half
+      V2* t = Cb;
+      Cb = P;
+      freeb = t;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_zfwd(const typename C2<T>::t* __restrict__ Pb, typename C2<T>::t* __restrict__ VV,
+                                              const typename C2<T>::t* __restrict__ twz, Dims d, RadixDev rz,
+                                              int nb_cols, int plane0) {
+  using V2 = typename C2<T>::t;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nzd = d.nzd, nz = d.nz, nxp = d.nx + 1, nzt = d.nzt;
+  V2* bufA = reinterpret_cast<V2*>(smem_raw);
+  V2* bufB = bufA + (size_t)nb_cols * nzd;
+  const int p = blockIdx.z;
+  const int plane = plane0 + blockIdx.y;
+  const int ix0 = blockIdx.x * nb_cols;
+  const int nb = min(nb_cols, nxp - ix0);
+  const size_t colbase = ((size_t)p * d.nplanes + plane) * nxp;
+  for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) bufA[idx] = Pb[(colbase + ix0) * nzd + idx];
+  __syncthreads();
+  V2* res = fft_block<V2>(bufA, bufB, nb, rz, -1, twz);
+  for (int idx = threadIdx.x; idx < nb * nzt; idx += blockDim.x) {
+    const int b = idx / nzt;
+    const int izp = idx - b * nzt;
+    const int iz = izp - nz;
+    const int jz = iz >= 0 ? iz : nzd + iz;
+    VV[(colbase + ix0 + b) * nzt + izp] = res[(size_t)b * nzd + jz];
+  }
+}
+
+template <typename T>
+void launch_convolutions(const ConvLaunch& L, cudaStream_t s) {
+  using V2 = typename C2<T>::t;
+  const Dims& d = L.d;
+  const int nxp = d.nx + 1;
+  {
+    dim3 grid((nxp + L.zcols - 1) / L.zcols, L.nplanes, 3);
+    size_t sm = 2 * (size_t)L.zcols * d.nzd * sizeof(V2);
+    k_zinv<T><<<grid, 256, sm, s>>>(L.V, (V2*)L.Zb, (const V2*)L.twz, d, L.rz, L.zcols, L.plane0);
+  }
+  {
+    dim3 grid(d.nzd / L.xrows, L.nplanes);
+    size_t sm = 9 * (size_t)L.xrows * d.nxd * sizeof(V2);
+    k_xrow<T><<<grid, 256, sm, s>>>((const V2*)L.Zb, (V2*)L.Pb, (const V2*)L.twx, (const V2*)L.twh, L.dy, d, L.rx,
+                                    L.xrows, L.plane0, L.compute_cfl, L.sc);
+  }
+  if (L.products) {
+    dim3 grid((nxp + L.zcols - 1) / L.zcols, L.nplanes, 6);
+    size_t sm = 2 * (size_t)L.zcols * d.nzd * sizeof(V2);
+    k_zfwd<T><<<grid, 256, sm, s>>>((const V2*)L.Pb, (V2*)L.VV, (const V2*)L.twz, d, L.rz, L.zcols, L.plane0);
+  }
+}
+
+template void launch_convolutions<double>(const ConvLaunch&, cudaStream_t);
+template void launch_convolutions<float>(const ConvLaunch&, cudaStream_t);
+
+namespace {
+template <typename K>
+cudaError_t allow_max_smem(K* kernel, int optin) {
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+}
+}  // namespace
+
+cudaError_t conv_set_smem_limits() {
+  int dev = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  if ((e = allow_max_smem(k_zinv<double>, optin))) return e;
+  if ((e = allow_max_smem(k_zinv<float>, optin))) return e;
+  if ((e = allow_max_smem(k_xrow<double>, optin))) return e;
+  if ((e = allow_max_smem(k_xrow<float>, optin))) return e;
+  if ((e = allow_max_smem(k_zfwd<double>, optin))) return e;
+  return allow_max_smem(k_zfwd<float>, optin);
+}
+
+}  // namespace chgpu

@@ -1,0 +1,78 @@
+// Launch descriptors shared by the kernel files and the C ABI layer.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "chgpu_internal.h"
+#include "cplx.cuh"
+
+namespace chgpu {
+
+// Sizes and physics constants passed by value to every kernel.
+struct Dims {
+  int nx, ny, nz, nzt, nxd, nzd;
+  int nplanes;  // ny+3 (iy=-1..ny+1 -> plane iy+1)
+  int nmodes;   // (nx+1)(2nz+1): mode m = ix*(2nz+1) + iz+nz
+  int npairs;   // (nx+1)(nz+1): pair (ix, |iz|)
+  double alfa0, beta0, ni, factor, rdx, rdz;
+  double meanflowx, meanflowz, cflmax, gamma;
+  int cpi, cpi_type;
+};
+
+// Boundary rows of setup_boundary_conditions and the one-sided wall
+// stencils (dnsdata.f90:259-308), by value.
+struct BcRows {
+  double v0bc[5], v0m1bc[5], eta0bc[5], eta0m1bc[5];
+  double vnbc[5], vnp1bc[5], etanbc[5], etanp1bc[5];
+  double d140[5], d14m1[5], d14n[5], d14np1[5];
+};
+
+struct ConvLaunch {
+  Dims d;
+  RadixDev rz, rx;
+  const double2* V;
+  void* Zb;
+  void* Pb;
+  void* VV;
+  const void* twz;
+  const void* twx;
+  const void* twh;
+  const double* dy;
+  DevScalars* sc;
+  int zcols, xrows;
+  int plane0, nplanes;
+  int compute_cfl;
+  int products;  // 0: stop after the x pass (the start-up CFL pass)
+};
+
+template <typename T> void launch_convolutions(const ConvLaunch& L, cudaStream_t s);
+cudaError_t conv_set_smem_limits();
+
+struct SolveLaunch {
+  Dims d;
+  BcRows bc;
+  double2* V;
+  const void* VV;
+  void* old;
+  double2* rhs;
+  const double2* rhs_src;  // where k_linsolve reads its right-hand sides
+  size_t rhs_cstride;      // component stride of rhs_src
+  int rhs_plane_off;       // row iy lives at plane iy+rhs_plane_off
+  double* fac;
+  const double* der;
+  const double* d0lu;
+  const double* yint;
+  DevScalars* sc;
+  double ode[3];
+  double lambda;  // used when lambda_from_dt == 0
+  int lambda_from_dt;
+};
+
+template <typename T> void launch_rhs(const SolveLaunch& L, cudaStream_t s);
+void launch_linsolve(const SolveLaunch& L, cudaStream_t s);
+void launch_advance_time(DevScalars* sc, double coef, int new_step, cudaStream_t s);
+void launch_outstats(const SolveLaunch& L, cudaStream_t s);
+void launch_flowrate(const SolveLaunch& L, cudaStream_t s);
+void launch_transpose(const double2* in, double2* out, int rows, int cols, int batch, cudaStream_t s);
+
+}  // namespace chgpu

@@ -1,0 +1,638 @@
+// The wall-normal half of the step: buildrhs rows and linsolve.
+//
+// k_rhs      : one thread per (mode, y-row): the five-point stencils of the
+//              six product spectra and of the field, the RK3/CN combination
+//              `timescheme` and the RK history update (dnsdata.f90:609-661).
+//              Results go to a separate buffer, which is what the reference's
+//              newrhs ring and write-back achieve (dnsdata.f90:667-670).
+// k_linsolve : one thread per pair of modes (kx, +kz) and (kx, -kz), whose
+//              matrices are equal because k^2 is: the pentadiagonal matrices
+//              are assembled, boundary-folded and factored once per row and
+//              applied to both modes (linsolve_blocking.inc:11-49), fused as
+//   pass A (iy=ny-1..1): assemble, applybc_n/applybc_0 (dnsdata.f90:458-472),
+//            LU5decompStep row, LeftLU5divStep1 row (rbparmat_blocking.f90:35-43,70-72)
+//   pass B (iy=1..ny-1): LeftLU5divStep2 (rbparmat_blocking.f90:93-95), then
+//            wall/ghost values (linsolve_blocking.inc:50-61)
+//   mean mode: U/W split, unit-forcing response, flow rates and the
+//            constant-flow-rate / CPI correction (linsolve_blocking.inc:62-97)
+//   pass C (iy=ny-1..1): COMPLEXderiv of v with LeftLU5divStep1(D0mat) (dnsdata.f90:339-373)
+//   pass D (iy=-1..ny+1): LeftLU5divStep2(D0mat) and u,w recovery (linsolve_blocking.inc:99-103)
+// The recurrences of each mode are sequential in y; parallelism is across modes.
+#include <cuda_runtime.h>
+
+#include "chgpu_internal.h"
+#include "cplx.cuh"
+#include "kernels.cuh"
+
+namespace chgpu {
+
+namespace {
+
+__device__ __forceinline__ double2 cz() { return make_double2(0.0, 0.0); }
+__device__ __forceinline__ double2 rmul(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+__device__ __forceinline__ float2 rmulf(float s, float2 a) { return make_float2(s * a.x, s * a.y); }
+__device__ __forceinline__ double2 cdivr(double2 a, double s) { return make_double2(a.x / s, a.y / s); }
+// (0 + i a) * z, the product with ialfa/ibeta of the reference (the zero real
+// part contributes exact zeros)
+template <typename V> __device__ __forceinline__ V mul_ia(decltype(V::x) a, V z) { return mk<V>(-(a * z.y), a * z.x); }
+
+__device__ __forceinline__ size_t vidx(const Dims& d, int c, int iy, int m) {
+  return ((size_t)c * d.nplanes + (iy + 1)) * d.nmodes + m;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// buildrhs rows
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, const typename C2<T>::t* __restrict__ VV,
+                                             typename C2<T>::t* __restrict__ old, double2* __restrict__ rhs,
+                                             const double* __restrict__ der, Dims d, double ode1, double ode2,
+                                             double ode3, const DevScalars* __restrict__ sc) {
+  using V2 = typename C2<T>::t;
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int iy = blockIdx.y + 1;
+  if (m >= d.nmodes) return;
+  const int ix = m / d.nzt;
+  const int iz = m - ix * d.nzt - d.nz;
+  const double* dr = der + (size_t)iy * 20;
+  double c0[5], c1[5], c2[5], c4[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    c0[j] = __ldg(dr + j);
+    c1[j] = __ldg(dr + 5 + j);
+    c2[j] = __ldg(dr + 10 + j);
+    c4[j] = __ldg(dr + 15 + j);
+  }
+  const T ta = (T)(ix * d.alfa0), tb = (T)(iz * d.beta0);
+  // DD(f,k) (dnsdata.f90:609-610) on product k (0-based) at rows iy-2..iy+2
+  V2 vv[6][5];
+#pragma unroll
+  for (int k = 0; k < 6; ++k)
+#pragma unroll
+    for (int j = 0; j < 5; ++j) vv[k][j] = VV[((size_t)k * d.nplanes + (iy - 1 + j)) * d.nmodes + m];
+  auto DD = [&](const double* c, int k) -> V2 {
+    V2 s = mk<V2>((T)c[0] * vv[k][0].x, (T)c[0] * vv[k][0].y);
+#pragma unroll
+    for (int j = 1; j < 5; ++j) s = s + mk<V2>((T)c[j] * vv[k][j].x, (T)c[j] * vv[k][j].y);
+    return s;
+  };
+  const V2 DD0_6 = DD(c0, 5), DD1_6 = DD(c1, 5);
+  const V2 rhsu = mk<V2>((T)0, (T)0) - mul_ia<V2>(ta, DD(c0, 0)) - DD(c1, 3) - mul_ia<V2>(tb, DD0_6);
+  const V2 rhsv = mk<V2>((T)0, (T)0) - mul_ia<V2>(ta, DD(c0, 3)) - DD(c1, 1) - mul_ia<V2>(tb, DD(c0, 4));
+  const V2 rhsw = mk<V2>((T)0, (T)0) - mul_ia<V2>(ta, DD0_6) - DD(c1, 4) - mul_ia<V2>(tb, DD(c0, 2));
+  const double a = ix * d.alfa0, b = iz * d.beta0;
+  const double k2 = a * a + b * b;
+  const T tk2 = (T)k2;
+  V2 explv = mul_ia<V2>(ta, mul_ia<V2>(ta, DD(c1, 0)) + DD(c2, 3) + mul_ia<V2>(tb, DD1_6)) +
+             mul_ia<V2>(tb, mul_ia<V2>(ta, DD1_6) + DD(c2, 4) + mul_ia<V2>(tb, DD(c1, 2)));
+  explv = explv - mk<V2>(tk2 * rhsv.x, tk2 * rhsv.y);
+  double2 v1[5], v2[5], v3[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    v1[j] = V[vidx(d, 0, iy - 2 + j, m)];
+    v2[j] = V[vidx(d, 1, iy - 2 + j, m)];
+    v3[j] = V[vidx(d, 2, iy - 2 + j, m)];
+  }
+  const double dt = sc->deltat;
+  const double ni = d.ni;
+  const size_t r0 = ((size_t)0 * (d.ny - 1) + (iy - 1)) * d.nmodes + m;  // eta
+  const size_t r1 = ((size_t)1 * (d.ny - 1) + (iy - 1)) * d.nmodes + m;  // d2v
+  // timescheme (dnsdata.f90:486) for D2v (:647)
+  {
+    double2 s2 = rmul(c2[0], v2[0]), s0 = rmul(c0[0], v2[0]);
+    double os = ni * (c4[0] - 2.0 * k2 * c2[0] + k2 * k2 * c0[0]);
+    double2 impl = rmul(os, v2[0]);
+#pragma unroll
+    for (int j = 1; j < 5; ++j) {
+      s2 = s2 + rmul(c2[j], v2[j]);
+      s0 = s0 + rmul(c0[j], v2[j]);
+      os = ni * (c4[j] - 2.0 * k2 * c2[j] + k2 * k2 * c0[j]);
+      impl = impl + rmul(os, v2[j]);
+    }
+    const double2 unkn = s2 - rmul(k2, s0);
+    const V2 o = old[r1];
+    const double2 e = make_double2((double)explv.x, (double)explv.y);
+    double2 r = cdivr(rmul(ode1, unkn), dt) + impl;
+    r = r + rmul(ode2, e);
+    r = r - rmul(ode3, make_double2((double)o.x, (double)o.y));
+    old[r1] = explv;
+    rhs[r1] = r;
+  }
+  if (ix == 0 && iz == 0) {  // mean flow U + iW (:648-654)
+    const double2 e = make_double2((double)rhsu.x + sc->meanpx, (double)rhsw.x + sc->meanpz);
+    double su = c0[0] * v1[0].x, sw = c0[0] * v3[0].x, tu = c2[0] * v1[0].x, tw = c2[0] * v3[0].x;
+#pragma unroll
+    for (int j = 1; j < 5; ++j) {
+      su = su + c0[j] * v1[j].x;
+      sw = sw + c0[j] * v3[j].x;
+      tu = tu + c2[j] * v1[j].x;
+      tw = tw + c2[j] * v3[j].x;
+    }
+    const double2 unkn = make_double2(su, sw);
+    const double2 impl = make_double2(ni * tu, ni * tw);
+    const V2 o = old[r0];
+    double2 r = cdivr(rmul(ode1, unkn), dt) + impl;
+    r = r + rmul(ode2, e);
+    r = r - rmul(ode3, make_double2((double)o.x, (double)o.y));
+    old[r0] = mk<V2>((T)e.x, (T)e.y);
+    rhs[r0] = r;
+  } else {  // eta (:656-661)
+    const V2 ee = mul_ia<V2>(tb, rhsu) - mul_ia<V2>(ta, rhsw);
+    double2 s1 = rmul(c0[0], v1[0]), s3 = rmul(c0[0], v3[0]);
+    double sq = ni * (c2[0] - k2 * c0[0]);
+    double2 impl = rmul(sq, mul_ia<double2>(b, v1[0]) - mul_ia<double2>(a, v3[0]));
+#pragma unroll
+    for (int j = 1; j < 5; ++j) {
+      s1 = s1 + rmul(c0[j], v1[j]);
+      s3 = s3 + rmul(c0[j], v3[j]);
+      sq = ni * (c2[j] - k2 * c0[j]);
+      impl = impl + rmul(sq, mul_ia<double2>(b, v1[j]) - mul_ia<double2>(a, v3[j]));
+    }
+    const double2 unkn = mul_ia<double2>(b, s1) - mul_ia<double2>(a, s3);
+    const V2 o = old[r0];
+    const double2 e = make_double2((double)ee.x, (double)ee.y);
+    double2 r = cdivr(rmul(ode1, unkn), dt) + impl;
+    r = r + rmul(ode2, e);
+    r = r - rmul(ode3, make_double2((double)o.x, (double)o.y));
+    old[r0] = ee;
+    rhs[r0] = r;
+  }
+}
+
+template <typename T>
+void launch_rhs(const SolveLaunch& L, cudaStream_t s) {
+  using V2 = typename C2<T>::t;
+  dim3 grid((L.d.nmodes + 127) / 128, L.d.ny - 1);
+  k_rhs<T><<<grid, 128, 0, s>>>(L.V, (const V2*)L.VV, (V2*)L.old, L.rhs, L.der, L.d, L.ode[0], L.ode[1], L.ode[2],
+                                L.sc);
+}
+template void launch_rhs<double>(const SolveLaunch&, cudaStream_t);
+template void launch_rhs<float>(const SolveLaunch&, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// linsolve
+// ---------------------------------------------------------------------------
+namespace {
+
+// one row of the two pentadiagonal matrices (linsolve_blocking.inc:12-13)
+__device__ __forceinline__ void assemble(const double* __restrict__ dr, double lambda, double k2, double ni,
+                                         double Dv[5], double De[5]) {
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    const double d0 = __ldg(dr + j), d2 = __ldg(dr + 10 + j), d4 = __ldg(dr + 15 + j);
+    const double os = ni * (d4 - 2.0 * k2 * d2 + k2 * k2 * d0);
+    const double sq = ni * (d2 - k2 * d0);
+    Dv[j] = lambda * (d2 - k2 * d0) - os;
+    De[j] = lambda * d0 - sq;
+  }
+}
+
+// applybc_n rows ny-1 / ny-2 and applybc_0 rows 1 / 2 (dnsdata.f90:458-472)
+__device__ __forceinline__ void bc_top1(double A[5], const double* bcn, const double* bcnp1) {
+  double e = A[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) A[j] = A[j] - e * bcnp1[j] / bcnp1[4];
+  e = A[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) A[j] = A[j] - e * bcn[j] / bcn[3];
+}
+__device__ __forceinline__ void bc_top2(double A[5], const double* bcn) {
+  const double e = A[4];
+#pragma unroll
+  for (int j = 1; j < 4; ++j) A[j] = A[j] - e * bcn[j - 1] / bcn[3];
+}
+__device__ __forceinline__ void bc_bot1(double A[5], const double* bc0, const double* bc0m1) {
+  double e = A[0];
+#pragma unroll
+  for (int j = 1; j < 5; ++j) A[j] = A[j] - e * bc0m1[j] / bc0m1[0];
+  e = A[1];
+#pragma unroll
+  for (int j = 2; j < 5; ++j) A[j] = A[j] - e * bc0[j] / bc0[1];
+}
+__device__ __forceinline__ void bc_bot2(double A[5], const double* bc0) {
+  const double e = A[0];
+#pragma unroll
+  for (int j = 1; j < 4; ++j) A[j] = A[j] - e * bc0[j + 1] / bc0[1];
+}
+
+// LU5decompStep for one row given the (scaled) lower entries of the two rows
+// below: L1 = row+1 (j=-2,-1), L2 = row+2.
+__device__ __forceinline__ void lu_row(double A[5], const double L1[2], const double L2[2]) {
+  double piv = A[4];
+  A[3] = A[3] - piv * L2[1];
+  A[2] = A[2] - piv * L2[0];
+  piv = A[3];
+  A[2] = A[2] - piv * L1[1];
+  A[1] = A[1] - piv * L1[0];
+  piv = 1.0 / A[2];
+  A[2] = piv;
+  A[0] = A[0] * piv;
+  A[1] = A[1] * piv;
+}
+
+__device__ __forceinline__ double2 step1(double2 x, const double A[5], double2 x1, double2 x2) {
+  double2 s = rmul(A[3], x1);
+  s = s + rmul(A[4], x2);
+  return rmul(A[2], x - s);
+}
+
+__device__ __forceinline__ double2 step2(double2 b, double lm2, double lm1, double2 bm2, double2 bm1) {
+  double2 s = rmul(lm2, bm2);
+  s = s + rmul(lm1, bm1);
+  return b - s;
+}
+
+__device__ __forceinline__ double2 dot3(const double2* v, const double* c) {  // sum(v(1:3)*c(0:2))
+  double2 s = rmul(c[0], v[0]);
+  s = s + rmul(c[1], v[1]);
+  return s + rmul(c[2], v[2]);
+}
+__device__ __forceinline__ double2 dot4(const double2* v, const double* c) {
+  double2 s = rmul(c[0], v[0]);
+  s = s + rmul(c[1], v[1]);
+  s = s + rmul(c[2], v[2]);
+  return s + rmul(c[3], v[3]);
+}
+__device__ __forceinline__ double2 dot5(const double2* v, const double* c) {
+  double2 s = rmul(c[0], v[0]);
+#pragma unroll
+  for (int j = 1; j < 5; ++j) s = s + rmul(c[j], v[j]);
+  return s;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(128) k_linsolve(double2* __restrict__ V, const double2* rhs, size_t rcs, int roff,
+                                                  double* __restrict__ fac, const double* __restrict__ der,
+                                                  const double* __restrict__ d0lu, const double* __restrict__ yint,
+                                                  BcRows bc, Dims d, double lambda_in, double ode1,
+                                                  int lambda_from_dt, DevScalars* __restrict__ sc) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= d.npairs) return;
+  const int ny = d.ny, nz = d.nz;
+  const int ix = q / (nz + 1);
+  const int a = q - ix * (nz + 1);
+  const int nm = (a == 0) ? 1 : 2;
+  int mm[2];
+  mm[0] = ix * d.nzt + nz + a;
+  mm[1] = ix * d.nzt + nz - a;
+  const bool is00 = (ix == 0 && a == 0);
+  const double ka = ix * d.alfa0, kb = a * d.beta0;
+  const double k2 = ka * ka + kb * kb;
+  const double lambda = lambda_from_dt ? ode1 / sc->deltat : lambda_in;
+  const double ni = d.ni;
+  const size_t P = d.npairs;
+  const double b0eta = is00 ? sc->u0 : 0.0, bneta = is00 ? sc->uN : 0.0;
+
+  // ---- pass A: bottom-up assembly + BC fold + factor + Step1 ----
+  double Lv1[2] = {0, 0}, Lv2[2] = {0, 0}, Le1[2] = {0, 0}, Le2[2] = {0, 0};
+  double2 xv1[2] = {cz(), cz()}, xv2[2] = {cz(), cz()}, xe1[2] = {cz(), cz()}, xe2[2] = {cz(), cz()};
+  double2 xc1 = cz(), xc2 = cz();  // unit-forcing response of the mean mode
+  for (int iy = ny - 1; iy >= 1; --iy) {
+    double Dv[5], De[5];
+    assemble(der + (size_t)iy * 20, lambda, k2, ni, Dv, De);
+    if (iy == ny - 1) { bc_top1(Dv, bc.vnbc, bc.vnp1bc); bc_top1(De, bc.etanbc, bc.etanp1bc); }
+    if (iy == ny - 2) { bc_top2(Dv, bc.vnbc); bc_top2(De, bc.etanbc); }
+    if (iy == 1) { bc_bot1(Dv, bc.v0bc, bc.v0m1bc); bc_bot1(De, bc.eta0bc, bc.eta0m1bc); }
+    if (iy == 2) { bc_bot2(Dv, bc.v0bc); bc_bot2(De, bc.eta0bc); }
+    double2 bv[2], be[2];
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      if (t < nm) {
+        bv[t] = rhs[rcs + (size_t)(iy + roff) * d.nmodes + mm[t]];
+        be[t] = rhs[(size_t)(iy + roff) * d.nmodes + mm[t]];
+      }
+    }
+    if (is00) {  // wall values of the mean mode's packed U+iW (linsolve_blocking.inc:26-27,40-41)
+      if (iy == 1) be[0] = be[0] - make_double2(De[1] * b0eta / bc.eta0bc[1], De[1] * 0.0 / bc.eta0bc[1]);
+      if (iy == 2) be[0] = be[0] - make_double2(De[0] * b0eta / bc.eta0bc[1], De[0] * 0.0 / bc.eta0bc[1]);
+      if (iy == ny - 1) be[0] = be[0] - make_double2(De[3] * bneta / bc.etanbc[3], De[3] * 0.0 / bc.etanbc[3]);
+      if (iy == ny - 2) be[0] = be[0] - make_double2(De[4] * bneta / bc.etanbc[3], De[4] * 0.0 / bc.etanbc[3]);
+    }
+    if (iy == ny - 1) { Dv[3] = Dv[4] = 0; De[3] = De[4] = 0; }  // rbparmat_blocking.f90:29
+    if (iy == ny - 2) { Dv[4] = 0; De[4] = 0; }
+    lu_row(Dv, Lv1, Lv2);
+    lu_row(De, Le1, Le2);
+    const double2 cu = make_double2(1.0, 0.0);
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      if (t < nm) {
+        const double2 nv = step1(bv[t], Dv, xv1[t], xv2[t]);
+        const double2 ne = step1(be[t], De, xe1[t], xe2[t]);
+        xv2[t] = xv1[t]; xv1[t] = nv;
+        xe2[t] = xe1[t]; xe1[t] = ne;
+        V[vidx(d, 1, iy, mm[t])] = nv;
+        V[vidx(d, 0, iy, mm[t])] = ne;
+      }
+    }
+    if (is00) {
+      const double2 nc = step1(cu, De, xc1, xc2);
+      xc2 = xc1; xc1 = nc;
+      V[vidx(d, 2, iy, mm[0])] = nc;
+    }
+    Lv2[0] = Lv1[0]; Lv2[1] = Lv1[1]; Lv1[0] = Dv[0]; Lv1[1] = Dv[1];
+    Le2[0] = Le1[0]; Le2[1] = Le1[1]; Le1[0] = De[0]; Le1[1] = De[1];
+    if (iy == 1) { Dv[0] = Dv[1] = 0; De[0] = De[1] = 0; }  // rbparmat_blocking.f90:45
+    if (iy == 2) { Dv[0] = 0; De[0] = 0; }
+    double* f = fac + (size_t)(iy - 1) * 4 * P + q;
+    f[0] = Dv[0]; f[P] = Dv[1]; f[2 * P] = De[0]; f[3 * P] = De[1];
+  }
+
+  // ---- pass B: top-down Step2, keeping the rows the wall closures need ----
+  double2 v[2][7], e[2][7], cc[7];  // rows 1..3 at [0..2], ny-3..ny-1 at [3..5]
+  {
+    double2 vm2[2] = {cz(), cz()}, vm1[2] = {cz(), cz()}, em2[2] = {cz(), cz()}, em1[2] = {cz(), cz()};
+    double2 cm2 = cz(), cm1 = cz();
+    for (int iy = 1; iy <= ny - 1; ++iy) {
+      const double* f = fac + (size_t)(iy - 1) * 4 * P + q;
+      const double lv2 = f[0], lv1 = f[P], le2 = f[2 * P], le1 = f[3 * P];
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        if (t < nm) {
+          const double2 nv = step2(V[vidx(d, 1, iy, mm[t])], lv2, lv1, vm2[t], vm1[t]);
+          const double2 ne = step2(V[vidx(d, 0, iy, mm[t])], le2, le1, em2[t], em1[t]);
+          V[vidx(d, 1, iy, mm[t])] = nv;
+          V[vidx(d, 0, iy, mm[t])] = ne;
+          vm2[t] = vm1[t]; vm1[t] = nv;
+          em2[t] = em1[t]; em1[t] = ne;
+          if (iy <= 3) { v[t][iy - 1] = nv; e[t][iy - 1] = ne; }
+          if (iy >= ny - 3) { v[t][iy - (ny - 3) + 3] = nv; e[t][iy - (ny - 3) + 3] = ne; }
+        }
+      }
+      if (is00) {
+        const double2 nc = step2(V[vidx(d, 2, iy, mm[0])], le2, le1, cm2, cm1);
+        V[vidx(d, 2, iy, mm[0])] = nc;
+        cm2 = cm1; cm1 = nc;
+        if (iy <= 3) cc[iy - 1] = nc;
+        if (iy >= ny - 3) cc[iy - (ny - 3) + 3] = nc;
+      }
+    }
+  }
+  // wall and ghost values (linsolve_blocking.inc:50-61); boundary values are
+  // zero except the mean mode's eta (packed wall velocity)
+  double2 vw[2][4], ew[2][4];  // [0]=iy -1, [1]=iy 0, [2]=iy ny, [3]=iy ny+1
+#pragma unroll
+  for (int t = 0; t < 2; ++t) {
+    if (t < nm) {
+      const double2* vb = &v[t][0];
+      const double2* eb = &e[t][0];
+      double2 w0 = rmul(-1.0, dot3(vb, bc.v0bc + 2));
+      w0 = cdivr(w0, bc.v0bc[1]);
+      double2 tmp[4] = {w0, vb[0], vb[1], vb[2]};
+      double2 wm1 = cdivr(rmul(-1.0, dot4(tmp, bc.v0m1bc + 1)), bc.v0m1bc[0]);
+      double2 e0 = cdivr(make_double2(b0eta, 0.0) - dot3(eb, bc.eta0bc + 2), bc.eta0bc[1]);
+      double2 tmpe[4] = {e0, eb[0], eb[1], eb[2]};
+      double2 em1 = cdivr(rmul(-1.0, dot4(tmpe, bc.eta0m1bc + 1)), bc.eta0m1bc[0]);
+      const double2* vt = &v[t][3];
+      const double2* et = &e[t][3];
+      double2 wn = cdivr(rmul(-1.0, dot3(vt, bc.vnbc)), bc.vnbc[3]);
+      double2 tmpt[4] = {vt[0], vt[1], vt[2], wn};
+      double2 wn1 = cdivr(rmul(-1.0, dot4(tmpt, bc.vnp1bc)), bc.vnp1bc[4]);
+      double2 en = cdivr(make_double2(bneta, 0.0) - dot3(et, bc.etanbc), bc.etanbc[3]);
+      double2 tmpte[4] = {et[0], et[1], et[2], en};
+      double2 en1 = cdivr(rmul(-1.0, dot4(tmpte, bc.etanp1bc)), bc.etanp1bc[4]);
+      vw[t][0] = wm1; vw[t][1] = w0; vw[t][2] = wn; vw[t][3] = wn1;
+      ew[t][0] = em1; ew[t][1] = e0; ew[t][2] = en; ew[t][3] = en1;
+      V[vidx(d, 1, -1, mm[t])] = wm1;
+      V[vidx(d, 1, 0, mm[t])] = w0;
+      V[vidx(d, 1, ny, mm[t])] = wn;
+      V[vidx(d, 1, ny + 1, mm[t])] = wn1;
+      V[vidx(d, 0, -1, mm[t])] = em1;
+      V[vidx(d, 0, 0, mm[t])] = e0;
+      V[vidx(d, 0, ny, mm[t])] = en;
+      V[vidx(d, 0, ny + 1, mm[t])] = en1;
+    }
+  }
+
+  if (is00) {  // mean flow (linsolve_blocking.inc:62-97)
+    const int m = mm[0];
+    double2 c0 = cdivr(rmul(-1.0, dot3(&cc[0], bc.eta0bc + 2)), bc.eta0bc[1]);
+    double2 tmp[4] = {c0, cc[0], cc[1], cc[2]};
+    double2 cm1 = cdivr(rmul(-1.0, dot4(tmp, bc.eta0m1bc + 1)), bc.eta0m1bc[0]);
+    double2 cn = cdivr(rmul(-1.0, dot3(&cc[3], bc.etanbc)), bc.etanbc[3]);
+    double2 tmpt[4] = {cc[3], cc[4], cc[5], cn};
+    double2 cn1 = cdivr(rmul(-1.0, dot4(tmpt, bc.etanp1bc)), bc.etanp1bc[4]);
+    V[vidx(d, 2, -1, m)] = cm1;
+    V[vidx(d, 2, 0, m)] = c0;
+    V[vidx(d, 2, ny, m)] = cn;
+    V[vidx(d, 2, ny + 1, m)] = cn1;
+    // flow rates by the non-uniform Simpson rule (dnsdata.f90:312-324)
+    double fu = 0.0, fw = 0.0, fc = 0.0;
+    for (int iy = 1, k = 0; iy <= ny - 1; iy += 2, ++k) {
+      const double a1 = yint[3 * k], a2 = yint[3 * k + 1], a3 = yint[3 * k + 2];
+      const double2 e0 = V[vidx(d, 0, iy - 1, m)], e1 = V[vidx(d, 0, iy, m)], e2 = V[vidx(d, 0, iy + 1, m)];
+      const double2 u0 = V[vidx(d, 2, iy - 1, m)], u1 = V[vidx(d, 2, iy, m)], u2 = V[vidx(d, 2, iy + 1, m)];
+      fu = fu + a1 * e0.x + a2 * e1.x + a3 * e2.x;
+      fw = fw + a1 * e0.y + a2 * e1.y + a3 * e2.y;
+      fc = fc + a1 * u0.x + a2 * u1.x + a3 * u2.x;
+    }
+    double corrpx = sc->corrpx, corrpz = sc->corrpz;
+    const bool cx = fabs(d.meanflowx) > 1.0e-7 && !d.cpi;
+    const bool cz_ = fabs(d.meanflowz) > 1.0e-7 && !d.cpi;
+    if (cx) corrpx = (d.meanflowx - fu) / fc;
+    if (cz_) corrpz = (d.meanflowz - fw) / fc;
+    for (int iy = -1; iy <= ny + 1; ++iy) {
+      const double2 et = V[vidx(d, 0, iy, m)];
+      const double uc = V[vidx(d, 2, iy, m)].x;
+      double U = et.x, W = et.y;
+      if (cx) U = U + corrpx * uc;
+      if (cz_) W = W + corrpz * uc;
+      V[vidx(d, 0, iy, m)] = make_double2(U, 0.0);
+      V[vidx(d, 2, iy, m)] = make_double2(W, 0.0);
+    }
+    sc->fr[0] = fu; sc->fr[1] = fw; sc->fr[2] = fc;
+    sc->corrpx = corrpx; sc->corrpz = corrpz;
+    if (d.cpi) {
+      if (d.cpi_type == 0) sc->meanpx = (1 - d.gamma) * 6 * ni / fu;
+      else sc->meanpx = (1.5 / d.gamma) * fu * ni;
+    }
+    return;
+  }
+
+  // ---- pass C: bottom-up COMPLEXderiv + Step1(D0mat) into the w slot ----
+  double2 f0w[2], fm1w[2], fnw[2], fn1w[2];
+#pragma unroll
+  for (int t = 0; t < 2; ++t) {
+    if (t < nm) {
+      double2 lo[5] = {vw[t][0], vw[t][1], v[t][0], v[t][1], v[t][2]};
+      double2 hi[5] = {v[t][3], v[t][4], v[t][5], vw[t][2], vw[t][3]};
+      f0w[t] = dot5(lo, bc.d140);
+      fm1w[t] = dot5(lo, bc.d14m1);
+      fnw[t] = dot5(hi, bc.d14n);
+      fn1w[t] = dot5(hi, bc.d14np1);
+    }
+  }
+  {
+    double2 win[2][5];  // v(iy-2..iy+2) sliding downwards
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      if (t < nm) {
+        win[t][1] = V[vidx(d, 1, ny - 2, mm[t])];
+        win[t][2] = V[vidx(d, 1, ny - 1, mm[t])];
+        win[t][3] = vw[t][2];
+        win[t][4] = vw[t][3];
+      }
+    }
+    double2 x1[2] = {cz(), cz()}, x2[2] = {cz(), cz()};
+    for (int iy = ny - 1; iy >= 1; --iy) {
+      const double* dr = der + (size_t)iy * 20;
+      double c1[5];
+#pragma unroll
+      for (int j = 0; j < 5; ++j) c1[j] = __ldg(dr + 5 + j);
+      double A[5];
+#pragma unroll
+      for (int j = 0; j < 5; ++j) A[j] = __ldg(d0lu + (size_t)(iy - 1) * 5 + j);
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        if (t < nm) {
+          win[t][0] = (iy - 2 >= 1) ? V[vidx(d, 1, iy - 2, mm[t])] : (iy - 2 == 0 ? vw[t][1] : vw[t][0]);
+          double2 f = dot5(win[t], c1);
+          if (iy == ny - 1) f = f - (rmul(__ldg(dr + 3), fnw[t]) + rmul(__ldg(dr + 4), fn1w[t]));
+          if (iy == ny - 2) f = f - rmul(__ldg(dr + 4), fnw[t]);
+          if (iy == 1) f = f - (rmul(__ldg(dr + 1), f0w[t]) + rmul(__ldg(dr + 0), fm1w[t]));
+          if (iy == 2) f = f - rmul(__ldg(dr + 0), f0w[t]);
+          const double2 x = step1(f, A, x1[t], x2[t]);
+          x2[t] = x1[t]; x1[t] = x;
+          V[vidx(d, 2, iy, mm[t])] = x;
+#pragma unroll
+          for (int j = 4; j > 0; --j) win[t][j] = win[t][j - 1];
+        }
+      }
+    }
+  }
+  // ---- pass D: top-down Step2(D0mat) and u, w recovery ----
+  {
+    double2 bm2[2], bm1[2];
+    for (int iy = -1; iy <= ny + 1; ++iy) {
+      double l2 = 0, l1 = 0;
+      if (iy >= 1 && iy <= ny - 1) {
+        l2 = __ldg(d0lu + (size_t)(iy - 1) * 5 + 0);
+        l1 = __ldg(d0lu + (size_t)(iy - 1) * 5 + 1);
+      }
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        if (t < nm) {
+          double2 vp;
+          if (iy == -1) vp = fm1w[t];
+          else if (iy == 0) vp = f0w[t];
+          else if (iy == ny) vp = fnw[t];
+          else if (iy == ny + 1) vp = fn1w[t];
+          else vp = step2(V[vidx(d, 2, iy, mm[t])], l2, l1, bm2[t], bm1[t]);
+          if (iy <= ny - 1) { bm2[t] = (iy == -1) ? cz() : bm1[t]; bm1[t] = vp; }
+          if (iy == -1) { bm2[t] = cz(); bm1[t] = vp; }
+          const double bz = (t == 0 ? 1.0 : -1.0) * kb;
+          const double2 et = V[vidx(d, 0, iy, mm[t])];
+          const double2 u = cdivr(mul_ia<double2>(ka, vp) - mul_ia<double2>(bz, et), k2);
+          const double2 w = cdivr(mul_ia<double2>(bz, vp) + mul_ia<double2>(ka, et), k2);
+          V[vidx(d, 0, iy, mm[t])] = u;
+          V[vidx(d, 2, iy, mm[t])] = w;
+        }
+      }
+    }
+  }
+}
+
+void launch_linsolve(const SolveLaunch& L, cudaStream_t s) {
+  dim3 grid((L.d.npairs + 127) / 128);
+  k_linsolve<<<grid, 128, 0, s>>>(L.V, L.rhs_src, L.rhs_cstride, L.rhs_plane_off, L.fac, L.der, L.d0lu, L.yint, L.bc, L.d, L.lambda, L.ode[0],
+                                  L.lambda_from_dt, L.sc);
+}
+
+// ---------------------------------------------------------------------------
+// small scalar kernels
+// ---------------------------------------------------------------------------
+__global__ void k_advance_time(DevScalars* sc, double coef, int new_step) {
+  if (new_step) sc->istep += 1;
+  sc->time = sc->time + coef * sc->deltat;  // channel.f90:128,141,154
+}
+
+void launch_advance_time(DevScalars* sc, double coef, int new_step, cudaStream_t s) {
+  k_advance_time<<<1, 1, 0, s>>>(sc, coef, new_step);
+}
+
+// outstats without file output (dnsdata.f90:861-879)
+__global__ void k_outstats(const double2* __restrict__ V, Dims d, BcRows bc, DevScalars* sc) {
+  const double rg = sc->cfl;
+  sc->cfl = 0.0;
+  if (d.cflmax > 0) sc->deltat = d.cflmax / rg;
+  const int m = d.nz;  // ix=0, iz=0
+  const int ny = d.ny;
+  double lo1[5], lo3[5], hi1[5], hi3[5];
+  for (int j = 0; j < 5; ++j) {
+    lo1[j] = V[vidx(d, 0, -1 + j, m)].x;
+    lo3[j] = V[vidx(d, 2, -1 + j, m)].x;
+    hi1[j] = V[vidx(d, 0, ny - 3 + j, m)].x;
+    hi3[j] = V[vidx(d, 2, ny - 3 + j, m)].x;
+  }
+  double d11 = bc.d140[0] * lo1[0], d21 = bc.d140[0] * lo3[0], d12 = bc.d14n[0] * hi1[0], d22 = bc.d14n[0] * hi3[0];
+  for (int j = 1; j < 5; ++j) {
+    d11 = d11 + bc.d140[j] * lo1[j];
+    d21 = d21 + bc.d140[j] * lo3[j];
+    d12 = d12 + bc.d14n[j] * hi1[j];
+    d22 = d22 + bc.d14n[j] * hi3[j];
+  }
+  double* o = sc->line;
+  o[0] = sc->time;
+  o[1] = d11; o[2] = -d12; o[3] = d21; o[4] = -d22;
+  o[5] = sc->fr[0] + sc->corrpx * sc->fr[2];
+  o[6] = sc->meanpx + sc->corrpx;
+  o[7] = sc->fr[1] + sc->corrpz * sc->fr[2];
+  o[8] = sc->meanpz + sc->corrpz;
+  o[9] = rg * sc->deltat;
+  o[10] = sc->deltat;
+  sc->runtime_global = rg;
+  bool bad = !isfinite(rg);
+  for (int i = 0; i < 11; ++i) bad = bad || !isfinite(o[i]);
+  if (bad) sc->error |= 1;
+}
+
+void launch_outstats(const SolveLaunch& L, cudaStream_t s) { k_outstats<<<1, 1, 0, s>>>(L.V, L.d, L.bc, L.sc); }
+
+// initial flow rate and CPI gradient (channel.f90:101-115)
+__global__ void k_flowrate(const double2* __restrict__ V, const double* __restrict__ yint, Dims d, DevScalars* sc) {
+  const int m = d.nz;
+  double fu = 0.0, fw = 0.0;
+  for (int iy = 1, k = 0; iy <= d.ny - 1; iy += 2, ++k) {
+    const double a1 = yint[3 * k], a2 = yint[3 * k + 1], a3 = yint[3 * k + 2];
+    fu = fu + a1 * V[vidx(d, 0, iy - 1, m)].x + a2 * V[vidx(d, 0, iy, m)].x + a3 * V[vidx(d, 0, iy + 1, m)].x;
+    fw = fw + a1 * V[vidx(d, 2, iy - 1, m)].x + a2 * V[vidx(d, 2, iy, m)].x + a3 * V[vidx(d, 2, iy + 1, m)].x;
+  }
+  sc->fr[0] = fu;
+  sc->fr[1] = fw;
+  sc->fr[2] = 0.0;  // the driver's frl(3) is never assigned
+  if (d.cpi) {
+    if (d.cpi_type == 0) sc->meanpx = (1 - d.gamma) * 6 * d.ni / fu;
+    else sc->meanpx = (1.5 / d.gamma) * fu * d.ni;
+  }
+}
+
+void launch_flowrate(const SolveLaunch& L, cudaStream_t s) { k_flowrate<<<1, 1, 0, s>>>(L.V, L.yint, L.d, L.sc); }
+
+// ---------------------------------------------------------------------------
+// layout transposes between the restart-file order (y fastest) and the
+// device order (mode fastest): batch of [rows][cols] -> [cols][rows]
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_transpose(const double2* __restrict__ in, double2* __restrict__ out, int rows,
+                                                   int cols) {
+  __shared__ double2 tile[32][33];
+  const size_t base = (size_t)blockIdx.z * rows * cols;
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  for (int i = threadIdx.y; i < 32; i += 8) {
+    const int r = r0 + i, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) tile[i][threadIdx.x] = in[base + (size_t)r * cols + c];
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += 8) {
+    const int c = c0 + i, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) out[base + (size_t)c * rows + r] = tile[threadIdx.x][i];
+  }
+}
+
+void launch_transpose(const double2* in, double2* out, int rows, int cols, int batch, cudaStream_t s) {
+  dim3 grid((cols + 31) / 32, (rows + 31) / 32, batch);
+  k_transpose<<<grid, dim3(32, 8), 0, s>>>(in, out, rows, cols);
+}
+
+}  // namespace chgpu

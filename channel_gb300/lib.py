@@ -1,0 +1,202 @@
+"""ctypes binding of libchgpu.so (include/chgpu.h).
+
+``Channel`` mirrors the module procedures channel.f90 calls on its hot path:
+``start`` (the start-up CFL pass, flow rate and first outstats,
+channel.f90:64-116), ``buildrhs(ODE, compute_cfl)`` (dnsdata.f90:611),
+``linsolve(lambda)`` (linsolve_blocking.inc:3), ``outstats()``
+(dnsdata.f90:853) and ``step()`` (one whole time-loop iteration,
+channel.f90:118-167, replayed from a CUDA graph).  Fields cross the boundary
+in the restart-file layout: numpy complex128 of shape (3, nx+1, 2nz+1, ny+3).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from .dnsin import DnsIn
+
+PKG = Path(__file__).resolve().parent
+RK = [(120.0 / 32.0, 2.0, 0.0), (120.0 / 8.0, 50.0 / 8.0, 34.0 / 8.0), (120.0 / 20.0, 90.0 / 20.0, 50.0 / 20.0)]
+FP64, MIXED = 0, 1
+
+
+class ChannelError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("alfa0", C.c_double), ("beta0", C.c_double), ("ni", C.c_double),
+        ("a", C.c_double), ("ymin", C.c_double), ("ymax", C.c_double),
+        ("cpi", C.c_int), ("cpi_type", C.c_int), ("gamma", C.c_double),
+        ("meanpx", C.c_double), ("meanpz", C.c_double),
+        ("meanflowx", C.c_double), ("meanflowz", C.c_double),
+        ("u0", C.c_double), ("uN", C.c_double),
+        ("deltat", C.c_double), ("cflmax", C.c_double), ("time", C.c_double),
+        ("dt_field", C.c_double), ("dt_save", C.c_double), ("t_max", C.c_double),
+        ("time_from_restart", C.c_int), ("nstep", C.c_longlong), ("npy", C.c_int),
+        ("precision", C.c_int),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [("line", C.c_double * 11), ("fr", C.c_double * 3), ("corrpx", C.c_double), ("corrpz", C.c_double),
+                ("meanpx", C.c_double), ("meanpz", C.c_double), ("cfl", C.c_double), ("deltat", C.c_double),
+                ("time", C.c_double), ("istep", C.c_longlong)]
+
+
+# name -> (restype, argtypes), one per declaration in include/chgpu.h
+_P = C.c_void_p
+_DP = C.POINTER(C.c_double)
+SIGNATURES = {
+    "chgpu_create": (C.c_int, [C.POINTER(Params), C.POINTER(C.c_void_p)]),
+    "chgpu_destroy": (C.c_int, [_P]),
+    "chgpu_upload_field": (C.c_int, [_P, _DP]),
+    "chgpu_download_field": (C.c_int, [_P, _DP]),
+    "chgpu_field_doubles": (C.c_size_t, [_P]),
+    "chgpu_start": (C.c_int, [_P, C.c_double, C.c_double, C.POINTER(Stats)]),
+    "chgpu_set_wall_velocity": (C.c_int, [_P, C.c_double, C.c_double]),
+    "chgpu_buildrhs": (C.c_int, [_P, _DP, C.c_int]),
+    "chgpu_linsolve": (C.c_int, [_P, C.c_double]),
+    "chgpu_outstats": (C.c_int, [_P, C.POINTER(Stats)]),
+    "chgpu_step": (C.c_int, [_P, C.POINTER(Stats)]),
+    "chgpu_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
+    "chgpu_synchronize": (C.c_int, [_P]),
+    "chgpu_stream": (C.c_void_p, [_P]),
+    "chgpu_launch_count": (C.c_longlong, [_P]),
+    "chgpu_last_error": (C.c_char_p, [_P]),
+}
+
+
+def library_path() -> Path:
+    return Path(os.environ.get("CHGPU_LIB", PKG / "_build" / "libchgpu.so"))
+
+
+_lib = None
+
+
+def load_library():
+    """Load libchgpu.so; raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not path.exists():
+            raise FileNotFoundError(f"{path} not built: run `python -m channel_gb300.build`")
+        L = C.CDLL(str(path))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def params_struct(p: DnsIn, precision: int = FP64) -> Params:
+    return Params(p.nx, p.ny, p.nz, p.alfa0, p.beta0, p.ni, p.a, p.ymin, p.ymax, int(p.cpi), p.cpi_type, p.gamma,
+                  p.meanpx, p.meanpz, p.meanflowx, p.meanflowz, p.u0, p.uN, p.deltat, p.cflmax, p.time,
+                  p.dt_field, p.dt_save, p.t_max, int(p.time_from_restart), p.nstep, p.npy, precision)
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_DP)
+
+
+class Channel:
+    """One channel run on the current CUDA device."""
+
+    def __init__(self, p: DnsIn, precision: str | int = "fp64"):
+        self.lib = load_library()
+        self.p = p
+        prec = {"fp64": FP64, "mixed": MIXED}.get(precision, precision) if isinstance(precision, str) else precision
+        self.precision = prec
+        self._params = params_struct(p, prec)
+        h = C.c_void_p()
+        rc = self.lib.chgpu_create(C.byref(self._params), C.byref(h))
+        if rc != 0:
+            raise ChannelError(rc, self.lib.chgpu_last_error(None).decode())
+        self.h = h
+        self.shape = (3, p.nx + 1, 2 * p.nz + 1, p.ny + 3)
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise ChannelError(rc, self.lib.chgpu_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.chgpu_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, V: np.ndarray):
+        a = np.ascontiguousarray(V, dtype=np.complex128)
+        if a.shape != self.shape:
+            raise ValueError(f"field shape {a.shape} != {self.shape}")
+        self._check(self.lib.chgpu_upload_field(self.h, _dp(a.view(np.float64))))
+
+    def download(self, out: np.ndarray | None = None) -> np.ndarray:
+        a = out if out is not None else np.empty(self.shape, dtype=np.complex128)
+        self._check(self.lib.chgpu_download_field(self.h, _dp(a.view(np.float64))))
+        return a
+
+    def start(self, time: float | None = None, deltat: float | None = None) -> np.ndarray:
+        st = Stats()
+        t = self.p.time if time is None else time
+        dt = self.p.deltat if deltat is None else deltat
+        self._check(self.lib.chgpu_start(self.h, t, dt, C.byref(st)))
+        return np.array(st.line)
+
+    def set_wall_velocity(self, u0: float, uN: float):
+        self._check(self.lib.chgpu_set_wall_velocity(self.h, u0, uN))
+
+    def buildrhs(self, ode, compute_cfl: bool):
+        o = np.array(ode, dtype=np.float64)
+        self._check(self.lib.chgpu_buildrhs(self.h, _dp(o), int(compute_cfl)))
+
+    def linsolve(self, lam: float):
+        self._check(self.lib.chgpu_linsolve(self.h, lam))
+
+    def outstats(self) -> Stats:
+        st = Stats()
+        self._check(self.lib.chgpu_outstats(self.h, C.byref(st)))
+        return st
+
+    def step(self, sync: bool = True) -> np.ndarray | None:
+        if not sync:
+            self._check(self.lib.chgpu_step(self.h, None))
+            return None
+        st = Stats()
+        self._check(self.lib.chgpu_step(self.h, C.byref(st)))
+        return np.array(st.line)
+
+    def stats(self) -> Stats:
+        st = Stats()
+        self._check(self.lib.chgpu_get_stats(self.h, C.byref(st)))
+        return st
+
+    def synchronize(self):
+        self._check(self.lib.chgpu_synchronize(self.h))
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.chgpu_launch_count(self.h))
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.chgpu_stream(self.h) or 0)

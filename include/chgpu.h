@@ -1,0 +1,135 @@
+/*
+ * chgpu.h -- C ABI of the GB300 channel-flow time step (libchgpu.so).
+ *
+ * Drop-in replacement for the module procedures that channel.f90 calls on
+ * its hot path.  Plain pointers and sizes only; no exit() inside; every
+ * entry point returns 0 on success or a negative CHGPU_E* code, with the
+ * message in chgpu_last_error().  One handle owns one run's device state
+ * (field, RK history, spectra of the products, work buffers, tables) on the
+ * current CUDA device and one CUDA stream; call it from one host thread.
+ *
+ * Field layout at this boundary is the reference's: complex128 interleaved,
+ * Fortran order V(iy,iz,ix,ic), iy=-1..ny+1 fastest, then iz=-nz..nz,
+ * ix=0..nx, ic=1..3  (dnsdata.f90:132; restart files, dnsdata.f90:821-848).
+ *
+ * A Fortran 2008 iso_c_binding interface for these entry points ships in
+ * channel_gb300/fortran/chgpu_interface.f90.
+ */
+#ifndef CHGPU_H
+#define CHGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CHGPU_OK 0
+#define CHGPU_E_PARAM -1     /* bad parameters or sizes */
+#define CHGPU_E_CUDA -2      /* CUDA runtime error (message has the name) */
+#define CHGPU_E_NOMEM -3     /* device allocation failed */
+#define CHGPU_E_NONFINITE -4 /* NaN/Inf met in the flow field or CFL */
+#define CHGPU_E_STATE -5     /* call out of order (e.g. step before upload) */
+
+#define CHGPU_FP64 0  /* every stage in FP64 */
+#define CHGPU_MIXED 1 /* FFTs, products, nonlinear stencils in FP32; solves FP64 */
+
+/* dns.in after read_dnsin (dnsdata.f90:98-125). `ni` holds 1/Re, the value
+ * read_dnsin leaves in `ni`. Logical flags are 0/1. */
+typedef struct chgpu_params {
+  int nx, ny, nz;
+  double alfa0, beta0;
+  double ni;
+  double a, ymin, ymax;
+  int cpi, cpi_type;
+  double gamma;
+  double meanpx, meanpz;
+  double meanflowx, meanflowz;
+  double u0, uN;
+  double deltat, cflmax, time;
+  double dt_field, dt_save, t_max;
+  int time_from_restart;
+  long long nstep;
+  int npy;
+  int precision; /* CHGPU_FP64 or CHGPU_MIXED */
+} chgpu_params;
+
+/* The numbers outstats prints (dnsdata.f90:876-879), plus the scalars the
+ * driver needs: line[11] = time, dudy_bot, -dudy_top, dwdy_bot, -dwdy_top,
+ * fr_x, meanpx+corrpx, fr_z, meanpz+corrpz, CFL*deltat, deltat. */
+typedef struct chgpu_stats {
+  double line[11];
+  double fr[3];
+  double corrpx, corrpz, meanpx, meanpz;
+  double cfl;    /* max CFL number measured (runtime_global) */
+  double deltat; /* time step for the next step */
+  double time;
+  long long istep;
+} chgpu_stats;
+
+typedef struct chgpu_handle chgpu_handle;
+
+/* init_memory + init_fft + setup_derivatives + setup_boundary_conditions
+ * (dnsdata.f90:129-177, ffts.f90:35-76, dnsdata.f90:241-286, 290-308).
+ * Allocates everything the step needs on the current device. */
+int chgpu_create(const chgpu_params* p, chgpu_handle** out);
+
+/* free_fft + free_memory (ffts.f90:110-115, dnsdata.f90:222-229). */
+int chgpu_destroy(chgpu_handle* h);
+
+/* Copy the field in after read_restart_file (dnsdata.f90:677-720) or out
+ * before save_restart_file (dnsdata.f90:821-848). `V` holds
+ * 3*(nx+1)*(2nz+1)*(ny+3) complex values (twice as many doubles). */
+int chgpu_upload_field(chgpu_handle* h, const double* V);
+int chgpu_download_field(chgpu_handle* h, double* V);
+size_t chgpu_field_doubles(const chgpu_handle* h);
+
+/* The driver's start-up (channel.f90:64-116): sets time and deltat as the
+ * driver holds them after re-reading dns.in, runs the initial CFL pass over
+ * iy=1..ny-1 (channel.f90:96-99: convolutions with compute_cfl), the flow
+ * rate and CPI pressure gradient (channel.f90:101-115), then outstats. */
+int chgpu_start(chgpu_handle* h, double time, double deltat, chgpu_stats* st);
+
+/* bc0(0,0)%u=u0; bcn(0,0)%u=uN (channel.f90:122-124). */
+int chgpu_set_wall_velocity(chgpu_handle* h, double u0, double uN);
+
+/* buildrhs(ODE, compute_cfl) (dnsdata.f90:611-673): convolutions of every
+ * y-plane and the explicit right-hand sides; uses the handle's deltat. */
+int chgpu_buildrhs(chgpu_handle* h, const double ode[3], int compute_cfl);
+
+/* linsolve(lambda) (linsolve_blocking.inc:3-107): implicit v and eta solves,
+ * wall/ghost values, mean-flow correction, velocity recovery. */
+int chgpu_linsolve(chgpu_handle* h, double lambda);
+
+/* outstats (dnsdata.f90:853-880) without file output: CFL max -> deltat
+ * (when cflmax>0), wall gradients, the Runtimedata numbers. */
+int chgpu_outstats(chgpu_handle* h, chgpu_stats* st);
+
+/* One whole time-loop iteration (channel.f90:118-167): istep+1, three RK
+ * substeps (time advance, buildrhs, linsolve) and outstats, all on the
+ * device; the step is captured once into a CUDA graph and replayed.
+ * `st` may be NULL (then no host synchronisation happens). */
+int chgpu_step(chgpu_handle* h, chgpu_stats* st);
+
+/* Read the statistics of the last completed step (synchronises). */
+int chgpu_get_stats(chgpu_handle* h, chgpu_stats* st);
+
+/* Wait for all work queued on the handle's stream; reports device-side
+ * error flags (non-finite CFL) as CHGPU_E_NONFINITE. */
+int chgpu_synchronize(chgpu_handle* h);
+
+/* The handle's CUDA stream (cudaStream_t), for callers that order their own
+ * work against the solver's. */
+void* chgpu_stream(chgpu_handle* h);
+
+/* Kernel launches issued by the handle since creation (for accounting). */
+long long chgpu_launch_count(const chgpu_handle* h);
+
+/* Message of the last failing call on this handle (or of chgpu_create when
+ * h is NULL). Never NULL. */
+const char* chgpu_last_error(const chgpu_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CHGPU_H */
