@@ -1,0 +1,484 @@
+"""Benchmark of the channel RK3/CN time step on GB300.
+
+Headline: RK3 steps/s of the plain FP64 step on the Re_tau~180 channel
+(127x192x127 modes, 384x193x384 physical grid after 3/2 padding), with the
+mixed-precision step measured side by side from the same seeded field and its
+statistics error against FP64.  One JSON line on stdout (rank 0).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload retau180|small|retau550|coarse]
+
+--impl reference times the reference algorithm on the host cores.  The
+reference itself (Fortran 2008 + MPI + FFTW3) cannot be built on these
+machines (no gfortran, MPI or FFTW), so that arm runs the C restatement of
+it (oracle/), with every host thread.
+
+Multi-GPU: independent replicas, one per rank (the step does not shard on one
+node without MPI; runs are independent), value = all ranks' steps / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "RK3 steps/s & ns/pt/step, FP64 vs mixed on 1 GB300 at ≤1e-4 stats error"
+AMPLITUDE = {"small": 0.01, "retau180": 0.05, "retau550": 0.05, "coarse": 0.05}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload_desc(p, prec: str) -> str:
+    return (f"channel {p.nx}x{p.ny}x{p.nz} modes (physical {2 * p.nxd}x{p.ny + 1}x{p.nzd} with 3/2 padding), "
+            f"alfa0={p.alfa0} beta0={p.beta0} Re={p.re} a={p.a}, "
+            + (f"cflmax={p.cflmax} (adaptive dt)" if p.cflmax > 0 else f"fixed dt={p.deltat}") + f", {prec}")
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes / flops per kernel launch (one substep over all planes)
+# ---------------------------------------------------------------------------
+def fft_flops(n: int) -> float:
+    """Real flops of the radix-4/2/3 Stockham transform of length n."""
+    cost = {4: 34.0, 2: 10.0, 3: 28.0}
+    f, m = 0.0, n
+    rs = []
+    while m % 4 == 0:
+        rs.append(4)
+        m //= 4
+    if m % 2 == 0:
+        rs.append(2)
+        m //= 2
+    if m % 3 == 0:
+        rs.append(3)
+    for r in rs:
+        f += n / r * cost[r]
+    return f
+
+
+def kernel_model(p, mixed: bool) -> dict:
+    """Per-launch algorithmic HBM bytes and FP flops of each kernel kind."""
+    ts = 8 if mixed else 16
+    nplanes, nxp, nzd, M = p.ny + 3, p.nx + 1, p.nzd, p.nxd
+    nmodes = nxp * (2 * p.nz + 1)
+    rows = (p.ny - 1) * nmodes
+    zinv_b = 3 * nplanes * nmodes * 16 + 3 * nplanes * nxp * nzd * ts
+    xrow_b = 9 * nplanes * nxp * nzd * ts
+    zfwd_b = 6 * nplanes * nxp * nzd * ts + 6 * nplanes * nmodes * ts
+    rhs_b = 6 * nplanes * nmodes * ts + 3 * nplanes * nmodes * 16 + 4 * rows * ts + 2 * rows * 16
+    lin_b = 2 * rows * 16 + 3 * nplanes * nmodes * 16
+    xrow_f = nplanes * nzd * (9 * fft_flops(M) + 3 * M * 12 + 2 * M * (6 * 2 + 8) + 6 * nxp * 16)
+    return {
+        "k_zinv": {"bytes": zinv_b, "flops": 3 * nplanes * nxp * fft_flops(nzd)},
+        "k_xrow": {"bytes": xrow_b, "flops": xrow_f},
+        "k_zfwd": {"bytes": zfwd_b, "flops": 6 * nplanes * nxp * fft_flops(nzd)},
+        "k_rhs": {"bytes": rhs_b, "flops": rows * 330.0},
+        "k_linsolve": {"bytes": lin_b, "flops": rows * 150.0},
+    }
+
+
+def measured_peaks() -> dict:
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            return json.loads(f.read_text())
+        except Exception:
+            pass
+    return {}
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in (getattr(self, "out", "") or "").splitlines():
+            t = [x.strip() for x in ln.split(",")]
+            if len(t) < 9:
+                continue
+            try:
+                sm.append(float(t[1]))
+                mx.append(float(t[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, t[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arms
+# ---------------------------------------------------------------------------
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, ws: int) -> float:
+    """Max of a per-rank time over the replicas (NCCL on GPUs, gloo on CPU)."""
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_steps_per_s(max_ms: float, steps: int, ws: int) -> float:
+    """Replicas: every rank advances its own run `steps` times; the job's
+    throughput is all ranks' steps over the slowest rank's time."""
+    return ws * steps / (max_ms * 1e-3)
+
+
+def timed_run(p, V0, prec, K, W, ws, clocks_gpu=None):
+    import torch
+
+    from channel_gb300 import Channel
+
+    g = Channel(p, prec)
+    g.upload(V0)
+    g.start()
+    for _ in range(W):
+        g.step(sync=False)
+    g.synchronize()
+    stream = torch.cuda.ExternalStream(g.stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier(ws)
+    torch.cuda.synchronize()
+    l0 = g.launches
+    sampler = ClockSampler(clocks_gpu) if clocks_gpu is not None else None
+    if sampler:
+        sampler.__enter__()
+    e0.record(stream)
+    for _ in range(K):
+        g.step(sync=False)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    if sampler:
+        sampler.__exit__()
+    barrier(ws)
+    ms = e0.elapsed_time(e1)
+    launches = g.launches - l0
+    g.synchronize()
+    st = g.stats()
+    V = g.download()
+    g.close()
+    return {"ms": max_over_ranks(ms, ws), "launches": launches, "V": V, "line": np.array(st.line),
+            "clocks": sampler.summary() if sampler else None}
+
+
+def kernel_attribution(p, V0, prec, nsteps):
+    from channel_gb300 import Channel
+
+    g = Channel(p, prec)
+    g.upload(V0)
+    g.start()
+    g.step()
+    g.set_profiling(True)
+    for _ in range(nsteps):
+        g.step(sync=False)
+    kt = g.kernel_times()
+    g.close()
+    return kt
+
+
+def e2e_run(p, V0, prec, K, W):
+    """Steps through the C ABI with the field in pinned host memory: every
+    step uploads the field, advances one RK3 step and reads the field and the
+    Runtimedata numbers back (the drop-in usage where the Fortran host owns V)."""
+    import torch
+
+    from channel_gb300 import Channel
+
+    host = torch.empty(V0.shape, dtype=torch.complex128, pin_memory=True).numpy()
+    host[...] = V0
+    g = Channel(p, prec)
+    g.upload(host)
+    g.start()
+    for _ in range(W):
+        g.upload(host)
+        g.step()
+        g.download(host)
+    t0 = time.perf_counter()
+    for _ in range(K):
+        g.upload(host)
+        g.step()
+        g.download(host)
+    t1 = time.perf_counter()
+    g.close()
+    nbytes = host.nbytes
+    return {"s": t1 - t0, "h2d": nbytes, "d2h": nbytes + 8 * 24}
+
+
+def profiles(V):
+    nz = V.shape[2] // 2
+    U = V[0, 0, nz, :].real
+    w = np.ones(V.shape[1])
+    w[1:] = 2.0
+    D = V.copy()
+    D[:, 0, nz, :] = 0.0
+    rms = np.sqrt(np.einsum("x,cxzy->cy", w, np.abs(D) ** 2))
+    return U, rms
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def cpu_baseline(p, V0, max_seconds=20.0):
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+
+    threads = os.cpu_count() or 1
+    o = pyoracle.Oracle(p, nthreads=threads)
+    o.set_field(V0)
+    o.start()
+    n, t = 0, 0.0
+    while n == 0 or (t + t / n <= max_seconds and n < 50):
+        t0 = time.perf_counter()
+        o.step()
+        t += time.perf_counter() - t0
+        n += 1
+    o.close()
+    return {"value": n / t, "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": f"{n} RK3 step(s) of the same workload after start-up, oracle C restatement "
+                      f"(reference Fortran/MPI/FFTW not buildable here), OpenMP over planes and modes"}
+
+
+def run_ours(args):
+    from channel_gb300 import dnsin, initial
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import torch
+
+    torch.cuda.set_device(local)
+    p = dnsin.workload(args.workload)
+    amp = AMPLITUDE[args.workload]
+    V0 = initial.perturbed_laminar(p, amp, seed=rank)
+    K, W = args.steps, args.warmup
+    gpts = p.grid_points()
+    gpu_id = str(local)
+    try:
+        gpu_id = "GPU-" + str(torch.cuda.get_device_properties(local).uuid)
+    except Exception:
+        pass
+    r64 = timed_run(p, V0, "fp64", K, W, ws, clocks_gpu=gpu_id)
+    rmx = timed_run(p, V0, "mixed", K, W, ws)
+    ms64 = r64["ms"] / K
+    msmx = rmx["ms"] / K
+    if args.mode == "timed":  # short form for profiler captures
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": ws * 1000.0 / ms64, "unit": "steps/s", "ms_per_step": ms64,
+                              "mixed_ms_per_step": msmx, "mode": "timed"}), flush=True)
+        return
+    U64, rr64 = profiles(r64["V"])
+    Umx, rrmx = profiles(rmx["V"])
+    stats_err = {"mean_U": rel(Umx, U64), "rms_u": rel(rrmx[0], rr64[0]), "rms_v": rel(rrmx[1], rr64[1]),
+                 "rms_w": rel(rrmx[2], rr64[2]),
+                 "wall_shear": float(abs(rmx["line"][1] - r64["line"][1]) / abs(r64["line"][1])),
+                 "fields": [rel(rmx["V"][c], r64["V"][c]) for c in range(3)], "after_steps": W + K}
+    # kernel attribution with CUDA events on the handle's stream
+    nprof = max(2, min(K, 10))
+    kt64 = kernel_attribution(p, V0, "fp64", nprof)
+    ktmx = kernel_attribution(p, V0, "mixed", nprof)
+    model64 = kernel_model(p, False)
+    modelmx = kernel_model(p, True)
+    peaks = measured_peaks()
+    hbm_peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if hbm_peak else "fallback"
+    hbm_peak = hbm_peak or 6800.0
+    fp64_peak_tflops = 1.196  # FP64 FMA throughput measured on this machine's GB300 (see profiles/)
+
+    def roof(kt, model):
+        dom = max((k for k in kt if k in model), key=lambda k: kt[k][0])
+        ms_total, n = kt[dom]
+        per = ms_total / max(n, 1) * 1e-3
+        gbs = model[dom]["bytes"] / per / 1e9
+        tfl = model[dom]["flops"] / per / 1e12
+        step_ms = sum(v[0] for v in kt.values()) / nprof
+        return dom, per, gbs, tfl, {k: {"ms_per_step": v[0] / nprof, "launches_per_step": v[1] / nprof,
+                                        "share": v[0] / max(sum(x[0] for x in kt.values()), 1e-30)}
+                                    for k, v in kt.items()}, step_ms
+
+    dom, per, gbs, tfl, kin64, _ = roof(kt64, model64)
+    domm, perm, gbsm, tflm, kinmx, _ = roof(ktmx, modelmx)
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get(f"{args.workload}:fp64:{dom}")
+        except Exception:
+            traffic = None
+    e2e = e2e_run(p, V0, "fp64", min(K, 10), 2)
+    cpu = cpu_baseline(p, V0) if rank == 0 else None
+    value = whole_job_steps_per_s(r64["ms"], K, ws)
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "steps/s",
+        "n_gpus": ws,
+        "steps": K,
+        "warmup": W,
+        "ms_per_step": ms64,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": f"synthetic: seeded perturbed-laminar field (numpy default_rng({rank}), amplitude {amp})",
+        "config": {"workload": workload_desc(p, "FP64"), "grid_points": gpts, "spectral_points": p.spectral_points(),
+                   "l2": "inputs larger than L2 (field " + f"{V0.nbytes / 1e6:.0f} MB" + " + product spectra per step)",
+                   "parallelism": f"replicas x{ws}"},
+        "ns_per_pt_step": ms64 * 1e6 / gpts,
+        "mixed": {"value": ws * 1000.0 / msmx, "unit": "steps/s", "ms_per_step": msmx,
+                  "ns_per_pt_step": msmx * 1e6 / gpts, "speedup_vs_fp64": ms64 / msmx, "stats_err_vs_fp64": stats_err,
+                  "dominant_kernel": domm, "kernels": kinmx,
+                  "roofline": {"bound": "hbm", "kernel": domm, "achieved": gbsm, "peak": hbm_peak, "unit": "GB/s",
+                               "frac": gbsm / hbm_peak, "traffic": None, "fp32_tflops": tflm}},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": gbs / hbm_peak, "traffic": traffic, "peak_source": peak_src,
+                     "launch_ms": per * 1e3,
+                     "fp64": {"achieved": tfl, "peak": fp64_peak_tflops, "unit": "TFLOP/s", "frac": tfl / fp64_peak_tflops,
+                              "note": "the FP64 pipe binds this kernel; the HBM fraction is low by design"}},
+        "kernels": kin64,
+        "e2e": {"value": min(K, 10) / e2e["s"] * ws, "unit": "steps/s", "h2d_bytes_per_step": e2e["h2d"],
+                "d2h_bytes_per_step": e2e["d2h"]},
+        "gpu_launches": r64["launches"],
+        "clocks": r64["clocks"],
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from channel_gb300 import dnsin, initial
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+
+    p = dnsin.workload(args.workload)
+    V0 = initial.perturbed_laminar(p, AMPLITUDE[args.workload], seed=0)
+    threads = os.cpu_count() or 1
+    o = pyoracle.Oracle(p, nthreads=threads)
+    o.set_field(V0)
+    o.start()
+    t0 = time.perf_counter()
+    o.step()
+    t_one = time.perf_counter() - t0
+    budget = 150.0
+    W = max(0, min(args.warmup - 1, int(budget / 4 / max(t_one, 1e-9))))
+    for _ in range(W):
+        o.step()
+    K = max(1, min(args.steps, int(budget / max(t_one, 1e-9))))
+    t0 = time.perf_counter()
+    for _ in range(K):
+        o.step()
+    t = time.perf_counter() - t0
+    o.close()
+    v = K / t
+    line = {
+        "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": ws, "steps": K, "steps_requested": args.steps,
+        "warmup": W + 1, "ms_per_step": 1000.0 * t / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded perturbed-laminar field (numpy default_rng(0))",
+        "config": {"workload": workload_desc(p, "FP64"), "grid_points": p.grid_points(),
+                   "spectral_points": p.spectral_points()},
+        "ns_per_pt_step": 1e9 * t / K / p.grid_points(),
+        "impl": "reference",
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{K} RK3 steps after start-up; the reference Fortran/MPI/FFTW build is not "
+                                   f"possible here (no gfortran, MPI or FFTW), so its C restatement runs"},
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="retau180", choices=list(AMPLITUDE))
+    ap.add_argument("--mode", default="full", choices=["full", "timed"],
+                    help="timed: only the FP64 and mixed timed runs (for profiler captures)")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    from channel_gb300 import build as b
+
+    if args.impl == "ours":
+        b.build()
+        run_ours(args)
+    else:
+        run_reference(args)
+
+
+if __name__ == "__main__":
+    main()

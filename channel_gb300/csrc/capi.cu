@@ -64,6 +64,12 @@ struct chgpu_handle {
   DevScalars* sc_host = nullptr;  // pinned
   cudaGraphExec_t graph = nullptr;
   bool field_set = false;
+  // per-kernel timing
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
+  double kind_ms[CHGPU_NKINDS] = {0};
+  long long kind_n[CHGPU_NKINDS] = {0};
   long long launches = 0;
   std::string err;
 };
@@ -106,6 +112,31 @@ int upload_roots(chgpu_handle* h, void** dst, int n) {
   CK(h, cudaMalloc(dst, sizeof(V2) * n));
   CK(h, cudaMemcpy(*dst, w.data(), sizeof(V2) * n, cudaMemcpyHostToDevice));
   return 0;
+}
+
+cudaEvent_t take_event(chgpu_handle* h) {
+  if (!h->ev_pool.empty()) {
+    cudaEvent_t e = h->ev_pool.back();
+    h->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Brackets the launches of `fn` with an event pair when profiling.
+template <typename F>
+void timed(chgpu_handle* h, int kind, F fn) {
+  if (!h->profiling) {
+    fn();
+    return;
+  }
+  cudaEvent_t a = take_event(h), b = take_event(h);
+  cudaEventRecord(a, h->stream);
+  fn();
+  cudaEventRecord(b, h->stream);
+  h->ev_pending.push_back({kind, {a, b}});
 }
 
 ConvLaunch conv_launch(chgpu_handle* h, int compute_cfl, int products, int plane0, int nplanes) {
@@ -154,15 +185,21 @@ SolveLaunch solve_launch(chgpu_handle* h, const double* ode) {
 
 void run_convolutions(chgpu_handle* h, int compute_cfl, int products, int plane0, int nplanes) {
   ConvLaunch L = conv_launch(h, compute_cfl, products, plane0, nplanes);
-  if (h->mixed) launch_convolutions<float>(L, h->stream);
-  else launch_convolutions<double>(L, h->stream);
-  h->launches += products ? 3 : 2;
+  const int nst = products ? 3 : 2;
+  for (int stage = 0; stage < nst; ++stage)
+    timed(h, stage, [&] {
+      if (h->mixed) launch_convolutions<float>(L, h->stream, stage);
+      else launch_convolutions<double>(L, h->stream, stage);
+    });
+  h->launches += nst;
 }
 
 void run_rhs(chgpu_handle* h, const double* ode) {
   SolveLaunch L = solve_launch(h, ode);
-  if (h->mixed) launch_rhs<float>(L, h->stream);
-  else launch_rhs<double>(L, h->stream);
+  timed(h, 3, [&] {
+    if (h->mixed) launch_rhs<float>(L, h->stream);
+    else launch_rhs<double>(L, h->stream);
+  });
   h->launches += 1;
 }
 
@@ -182,20 +219,20 @@ void run_linsolve(chgpu_handle* h, double ode1, double lambda, int from_dt, bool
     L.rhs_cstride = (size_t)(h->d.ny - 1) * h->d.nmodes;
     L.rhs_plane_off = -1;
   }
-  launch_linsolve(L, h->stream);
+  timed(h, 4, [&] { launch_linsolve(L, h->stream); });
   h->launches += 1;
 }
 
 void run_outstats(chgpu_handle* h) {
   SolveLaunch L = solve_launch(h, nullptr);
-  launch_outstats(L, h->stream);
+  timed(h, 5, [&] { launch_outstats(L, h->stream); });
   h->launches += 1;
 }
 
 // One time-loop iteration (channel.f90:118-167) on the stream.
 void enqueue_step(chgpu_handle* h) {
   for (int k = 0; k < 3; ++k) {
-    launch_advance_time(h->sc, 2.0 / RK[k][0], k == 0, h->stream);
+    timed(h, 5, [&] { launch_advance_time(h->sc, 2.0 / RK[k][0], k == 0, h->stream); });
     h->launches += 1;
     run_convolutions(h, k == 2, 1, 0, h->d.nplanes);
     run_rhs(h, RK[k]);
@@ -227,6 +264,11 @@ int pull_scalars(chgpu_handle* h) {
 
 void release(chgpu_handle* h) {
   if (h->graph) cudaGraphExecDestroy(h->graph);
+  for (auto& pe : h->ev_pending) {
+    cudaEventDestroy(pe.second.first);
+    cudaEventDestroy(pe.second.second);
+  }
+  for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   void* bufs[] = {h->V, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->d0lu, h->yint, h->dy,
                   h->twz, h->twx, h->twh, h->sc};
   for (void* b : bufs)
@@ -464,6 +506,16 @@ int chgpu_outstats(chgpu_handle* h, chgpu_stats* st) {
 int chgpu_step(chgpu_handle* h, chgpu_stats* st) {
   if (!h) return fail(h, CHGPU_E_PARAM, "chgpu_step: null handle");
   if (!h->field_set) return fail(h, CHGPU_E_STATE, "chgpu_step: upload the field first");
+  if (h->profiling) {
+    enqueue_step(h);
+    CK(h, cudaGetLastError());
+    if (st) {
+      int rc = pull_scalars(h);
+      fill_stats(h, st);
+      return rc;
+    }
+    return 0;
+  }
   if (!h->graph) {
     cudaGraph_t g = nullptr;
     CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -499,6 +551,40 @@ int chgpu_get_stats(chgpu_handle* h, chgpu_stats* st) {
 int chgpu_synchronize(chgpu_handle* h) {
   if (!h) return fail(h, CHGPU_E_PARAM, "null handle");
   return pull_scalars(h);
+}
+
+int chgpu_set_profiling(chgpu_handle* h, int on) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "null handle");
+  h->profiling = on != 0;
+  for (int k = 0; k < CHGPU_NKINDS; ++k) {
+    h->kind_ms[k] = 0;
+    h->kind_n[k] = 0;
+  }
+  return 0;
+}
+
+int chgpu_kernel_times(chgpu_handle* h, double ms[CHGPU_NKINDS], long long launches[CHGPU_NKINDS]) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "null handle");
+  CK(h, cudaStreamSynchronize(h->stream));
+  for (auto& pe : h->ev_pending) {
+    float t = 0.f;
+    CK(h, cudaEventElapsedTime(&t, pe.second.first, pe.second.second));
+    h->kind_ms[pe.first] += t;
+    h->kind_n[pe.first] += 1;
+    h->ev_pool.push_back(pe.second.first);
+    h->ev_pool.push_back(pe.second.second);
+  }
+  h->ev_pending.clear();
+  for (int k = 0; k < CHGPU_NKINDS; ++k) {
+    if (ms) ms[k] = h->kind_ms[k];
+    if (launches) launches[k] = h->kind_n[k];
+  }
+  return 0;
+}
+
+const char* chgpu_kernel_kind_name(int kind) {
+  static const char* names[CHGPU_NKINDS] = {"k_zinv", "k_xrow", "k_zfwd", "k_rhs", "k_linsolve", "scalars"};
+  return (kind >= 0 && kind < CHGPU_NKINDS) ? names[kind] : "?";
 }
 
 void* chgpu_stream(chgpu_handle* h) { return h ? (void*)h->stream : nullptr; }

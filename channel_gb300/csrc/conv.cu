@@ -207,30 +207,30 @@ __global__ void __launch_bounds__(256) k_zfwd(const typename C2<T>::t* __restric
 }
 
 template <typename T>
-void launch_convolutions(const ConvLaunch& L, cudaStream_t s) {
+void launch_convolutions(const ConvLaunch& L, cudaStream_t s, int stage) {
   using V2 = typename C2<T>::t;
   const Dims& d = L.d;
   const int nxp = d.nx + 1;
-  {
+  if (stage == 0) {
     dim3 grid((nxp + L.zcols - 1) / L.zcols, L.nplanes, 3);
     size_t sm = 2 * (size_t)L.zcols * d.nzd * sizeof(V2);
     k_zinv<T><<<grid, 256, sm, s>>>(L.V, (V2*)L.Zb, (const V2*)L.twz, d, L.rz, L.zcols, L.plane0);
   }
-  {
+  if (stage == 1) {
     dim3 grid(d.nzd / L.xrows, L.nplanes);
     size_t sm = 9 * (size_t)L.xrows * d.nxd * sizeof(V2);
     k_xrow<T><<<grid, 256, sm, s>>>((const V2*)L.Zb, (V2*)L.Pb, (const V2*)L.twx, (const V2*)L.twh, L.dy, d, L.rx,
                                     L.xrows, L.plane0, L.compute_cfl, L.sc);
   }
-  if (L.products) {
+  if (stage == 2) {
     dim3 grid((nxp + L.zcols - 1) / L.zcols, L.nplanes, 6);
     size_t sm = 2 * (size_t)L.zcols * d.nzd * sizeof(V2);
     k_zfwd<T><<<grid, 256, sm, s>>>((const V2*)L.Pb, (V2*)L.VV, (const V2*)L.twz, d, L.rz, L.zcols, L.plane0);
   }
 }
 
-template void launch_convolutions<double>(const ConvLaunch&, cudaStream_t);
-template void launch_convolutions<float>(const ConvLaunch&, cudaStream_t);
+template void launch_convolutions<double>(const ConvLaunch&, cudaStream_t, int);
+template void launch_convolutions<float>(const ConvLaunch&, cudaStream_t, int);
 
 namespace {
 template <typename K>

@@ -1,0 +1,317 @@
+// channel_gb300 -- the channel DNS driver on top of libchgpu.so.
+//
+// Restates the program flow of channel.f90 (the reference's Fortran driver,
+// which needs gfortran + MPI to build) in C++ over the C ABI of
+// include/chgpu.h, keeping its files:
+//   dns.in        read as read_dnsin does (dnsdata.f90:98-125)
+//   Dati.cart.out read (header check, dnsdata.f90:677-720) or, when absent,
+//                 the laminar start of dnsdata.f90:704-718; rewritten at the
+//                 end (channel.f90:181) and every dt_save (dnsdata.f90:882-886)
+//   Dati.cart.<n>.out  snapshots every dt_field (dnsdata.f90:895-918)
+//   Runtimedata   one line per step (dnsdata.f90:878), rewound to the restart
+//                 time when time_from_restart (get_record, dnsdata.f90:181-218)
+// Usage: channel_gb300 [--mixed] [--quiet]   (in the run directory)
+#include <chgpu.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+namespace {
+
+struct DnsIn {
+  chgpu_params p{};
+  double re = 0;
+};
+
+std::string strip_comment(const std::string& s) {
+  size_t k = s.find('!');
+  return k == std::string::npos ? s : s.substr(0, k);
+}
+
+double fortran_real(std::string t) {
+  for (char& c : t)
+    if (c == 'd' || c == 'D') c = 'e';
+  return std::strtod(t.c_str(), nullptr);
+}
+
+bool fortran_logical(std::string t) {
+  size_t i = 0;
+  while (i < t.size() && t[i] == '.') ++i;
+  char c = i < t.size() ? (char)std::toupper((unsigned char)t[i]) : 'F';
+  return c == 'T';
+}
+
+// list-directed reads: each READ takes the values it needs from the next
+// record(s); the rest of the record (the comment) is skipped
+bool read_dnsin(const char* path, DnsIn& d) {
+  std::ifstream f(path);
+  if (!f) return false;
+  const int need[12] = {3, 2, 1, 3, 3, 2, 2, 2, 3, 4, 1, 1};
+  std::vector<std::vector<std::string>> v(12);
+  std::string line;
+  for (int k = 0; k < 12; ++k) {
+    while ((int)v[k].size() < need[k]) {
+      if (!std::getline(f, line)) return false;
+      std::string s = strip_comment(line);
+      for (char& c : s)
+        if (c == ',') c = ' ';
+      std::istringstream is(s);
+      std::string tok;
+      while (is >> tok) v[k].push_back(tok);
+    }
+    v[k].resize(need[k]);
+  }
+  chgpu_params& p = d.p;
+  p.nx = std::atoi(v[0][0].c_str()); p.ny = std::atoi(v[0][1].c_str()); p.nz = std::atoi(v[0][2].c_str());
+  p.alfa0 = fortran_real(v[1][0]); p.beta0 = fortran_real(v[1][1]);
+  d.re = fortran_real(v[2][0]);
+  p.ni = 1 / d.re;  // ni=1/ni (dnsdata.f90:115)
+  p.a = fortran_real(v[3][0]); p.ymin = fortran_real(v[3][1]); p.ymax = fortran_real(v[3][2]);
+  p.cpi = fortran_logical(v[4][0]); p.cpi_type = std::atoi(v[4][1].c_str()); p.gamma = fortran_real(v[4][2]);
+  p.meanpx = fortran_real(v[5][0]); p.meanpz = fortran_real(v[5][1]);
+  p.meanflowx = fortran_real(v[6][0]); p.meanflowz = fortran_real(v[6][1]);
+  p.u0 = fortran_real(v[7][0]); p.uN = fortran_real(v[7][1]);
+  p.deltat = fortran_real(v[8][0]); p.cflmax = fortran_real(v[8][1]); p.time = fortran_real(v[8][2]);
+  p.dt_field = fortran_real(v[9][0]); p.dt_save = fortran_real(v[9][1]); p.t_max = fortran_real(v[9][2]);
+  p.time_from_restart = fortran_logical(v[9][3]);
+  p.nstep = std::atoll(v[10][0].c_str());
+  p.npy = std::atoi(v[11][0].c_str());
+  return true;
+}
+
+#pragma pack(push, 1)
+struct Header {
+  int32_t nx, ny, nz;
+  double alfa0, beta0, ni, a, ymin, ymax, time;
+};
+#pragma pack(pop)
+static_assert(sizeof(Header) == 68, "restart header is 68 bytes");
+
+size_t field_count(const chgpu_params& p) { return (size_t)3 * (p.nx + 1) * (2 * p.nz + 1) * (p.ny + 3); }
+
+bool write_restart(const std::string& path, const chgpu_params& p, double time, const std::vector<double>& V) {
+  std::FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) return false;
+  Header h{p.nx, p.ny, p.nz, p.alfa0, p.beta0, p.ni, p.a, p.ymin, p.ymax, time};
+  bool ok = std::fwrite(&h, sizeof h, 1, f) == 1 && std::fwrite(V.data(), sizeof(double), V.size(), f) == V.size();
+  return std::fclose(f) == 0 && ok;
+}
+
+// 0: read; 1: absent; -1: unreadable; -2: metadata mismatch
+int read_restart(const std::string& path, const chgpu_params& p, std::vector<double>& V, double& time) {
+  std::FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return 1;
+  Header h{};
+  if (std::fread(&h, sizeof h, 1, f) != 1) { std::fclose(f); return -1; }
+  if (h.nx != p.nx || h.ny != p.ny || h.nz != p.nz || h.alfa0 != p.alfa0 || h.beta0 != p.beta0 || h.ni != p.ni ||
+      h.a != p.a || h.ymin != p.ymin || h.ymax != p.ymax) {
+    std::fprintf(stderr, "ERROR: mismatch in metadata between restart file and dns.in. Stopping.\n"
+                         "From .out file:\n %d %d %d %.17g %.17g %.17g %.17g %.17g %.17g\nFrom dns.in:\n"
+                         " %d %d %d %.17g %.17g %.17g %.17g %.17g %.17g\n",
+                 h.nx, h.ny, h.nz, h.alfa0, h.beta0, h.ni, h.a, h.ymin, h.ymax, p.nx, p.ny, p.nz, p.alfa0, p.beta0,
+                 p.ni, p.a, p.ymin, p.ymax);
+    std::fclose(f);
+    return -2;
+  }
+  V.assign(2 * field_count(p), 0.0);
+  size_t got = std::fread(V.data(), sizeof(double), V.size(), f);
+  std::fclose(f);
+  if (got != V.size()) return -1;
+  time = h.time;
+  return 0;
+}
+
+// the laminar start of read_restart_file when no file exists (dnsdata.f90:704-718)
+void laminar_start(const chgpu_params& p, std::vector<double>& V) {
+  V.assign(2 * field_count(p), 0.0);
+  const int nyt = p.ny + 3, nzt = 2 * p.nz + 1;
+  for (int iy = -1; iy <= p.ny + 1; ++iy) {
+    double y = p.ymin + 0.5 * (p.ymax - p.ymin) * (std::tanh(p.a * (2.0 * iy / (double)p.ny - 1)) / std::tanh(p.a) + 1);
+    size_t idx = (size_t)(iy + 1) + (size_t)nyt * (size_t)p.nz;  // iz=0, ix=0, ic=1
+    V[2 * idx] = 3 * 0.5 * y * (2 - y);
+  }
+  (void)nzt;
+}
+
+std::string fmt_line(const double* v) {  // one Runtimedata record
+  std::string s;
+  char buf[40];
+  for (int i = 0; i < 11; ++i) {
+    std::snprintf(buf, sizeof buf, " %25.16E", v[i]);
+    s += buf;
+  }
+  return s + "\n";
+}
+
+void echo_line(const double* v) {  // dnsdata.f90:876
+  std::printf("%10.4f   ", v[0]);
+  for (int i = 1; i <= 4; ++i) std::printf("%11.6f   ", v[i]);
+  for (int i = 5; i <= 8; ++i) std::printf("%9.4f   ", v[i]);
+  for (int i = 9; i <= 10; ++i) std::printf("%9.6f   ", v[i]);
+  std::printf("\n");
+  std::fflush(stdout);
+}
+
+// get_record (dnsdata.f90:181-218): keep the records before the one whose
+// time matches the restart time; returns that record's deltat (or 0).
+double rewind_runtimedata(const char* path, double threshold, bool& found) {
+  found = false;
+  std::ifstream f(path);
+  if (!f) return 0.0;
+  std::vector<std::string> keep;
+  std::string line;
+  double dt = 0.0;
+  while (std::getline(f, line)) {
+    std::istringstream is(line);
+    double v[11];
+    int n = 0;
+    while (n < 11 && (is >> v[n])) ++n;
+    if (n == 11 && std::fabs(v[0] - threshold) < 0.5 * v[10]) {
+      found = true;
+      dt = v[10];
+      break;
+    }
+    keep.push_back(line);
+  }
+  f.close();
+  std::ofstream o(path, std::ios::trunc);
+  for (auto& l : keep) o << l << "\n";
+  if (!found) o << "\n";  // "Skipping one line and appending."
+  return dt;
+}
+
+int check(int rc, chgpu_handle* h, const char* what) {
+  if (rc != 0) {
+    std::fprintf(stderr, "%s failed (%d): %s\n", what, rc, chgpu_last_error(h));
+    std::exit(1);
+  }
+  return rc;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  bool mixed = false, quiet = false;
+  for (int i = 1; i < argc; ++i) {
+    if (!std::strcmp(argv[i], "--mixed")) mixed = true;
+    else if (!std::strcmp(argv[i], "--quiet")) quiet = true;
+    else {
+      std::fprintf(stderr, "usage: %s [--mixed] [--quiet]\n", argv[0]);
+      return 2;
+    }
+  }
+  DnsIn d;
+  if (!read_dnsin("dns.in", d)) {
+    std::fprintf(stderr, "cannot read dns.in\n");
+    return 1;
+  }
+  const double deltat_from_dnsin = d.p.deltat;
+  d.p.precision = mixed ? CHGPU_MIXED : CHGPU_FP64;
+  chgpu_handle* h = nullptr;
+  check(chgpu_create(&d.p, &h), nullptr, "chgpu_create");
+  chgpu_params& p = d.p;
+  std::vector<double> V;
+  double time = p.time;
+  int rr = read_restart("Dati.cart.out", p, V, time);
+  if (rr == -2) return 1;
+  if (rr == -1) {
+    std::fprintf(stderr, "Dati.cart.out is truncated or unreadable\n");
+    return 1;
+  }
+  if (rr == 1) {
+    std::printf(" Generating initial field...\n");
+    laminar_start(p, V);
+    time = p.time;
+  } else {
+    std::printf(" Reading from file Dati.cart.out\n");
+  }
+  bool have_rtd = std::ifstream("Runtimedata").good();
+  double deltat = p.deltat;
+  if (p.time_from_restart && have_rtd) {
+    bool found = false;
+    double dt = rewind_runtimedata("Runtimedata", time, found);
+    if (found) {
+      std::printf(" In Runtimedata: starting from time %g\n", time);
+      deltat = dt;
+    } else {
+      std::printf(" WARNING: No instant of time matching restart file has been found in Runtimedata.\n"
+                  " Skipping one line and appending.\n");
+    }
+  } else if (!p.time_from_restart) {
+    time = p.time;  // read_dnsin again (channel.f90:57)
+    deltat = p.deltat;
+  }
+  std::ofstream rtd("Runtimedata", (p.time_from_restart && have_rtd) ? std::ios::app : std::ios::trunc);
+  long long ifield = (long long)std::floor((time + 0.5 * deltat) / p.dt_field);
+  const double time0 = time;
+  if (p.cflmax == 0) deltat = deltat_from_dnsin;
+  int nxd = 3 * (p.nx + 1) / 2, nzd = 3 * p.nz;
+  auto fit = [](int n) { while (n % 2 == 0) n >>= 1; return n == 1 || n == 3; };
+  while (!fit(nxd)) ++nxd;
+  while (!fit(nzd)) ++nzd;
+  if (!quiet) {
+    std::printf("\n !====================================================!\n"
+                " !                     D   N   S                      !\n"
+                " !====================================================!\n\n");
+    std::printf("   nx =%5d   ny =%5d   nz =%5d\n   nxd =%5d  nzd =%5d\n", p.nx, p.ny, p.nz, nxd, nzd);
+    std::printf("   alfa0 =%11.6f       beta0 =%11.6f   ni =%8.6f\n", p.alfa0, p.beta0, p.ni);
+    std::printf("   meanpx =%11.6f      meanpz =%11.6f\n", p.meanpx, p.meanpz);
+    std::printf("   meanflowx =%11.6f   meanflowz =%11.6f\n", p.meanflowx, p.meanflowz);
+    std::printf("   nsteps =%6lld   time_from_restart =%c   precision = %s\n\n", p.nstep,
+                p.time_from_restart ? 'T' : 'F', mixed ? "mixed" : "fp64");
+  }
+  check(chgpu_upload_field(h, V.data()), h, "upload");
+  chgpu_stats st{};
+  check(chgpu_start(h, time, deltat, &st), h, "start");
+  check(chgpu_set_wall_velocity(h, p.u0, p.uN), h, "wall velocity");
+  rtd << fmt_line(st.line);
+  rtd.flush();
+  if (!quiet) echo_line(st.line);
+  bool prev_was_close = false;
+  long long istep = 0;
+  deltat = st.deltat;
+  time = st.time;
+  while (time < p.t_max - deltat / 2.0 && istep < p.nstep) {
+    check(chgpu_step(h, &st), h, "step");
+    istep = st.istep;
+    time = st.time;
+    deltat = st.deltat;
+    rtd << fmt_line(st.line);
+    rtd.flush();
+    if (!quiet) echo_line(st.line);
+    // restart and snapshot cadence (dnsdata.f90:882-918)
+    if (p.dt_save > 0 && std::floor((time + 0.5 * deltat) / p.dt_save) > std::floor((time - 0.5 * deltat) / p.dt_save) &&
+        istep > 1) {
+      std::printf(" Writing Dati.cart.out at time %g\n", time);
+      check(chgpu_download_field(h, V.data()), h, "download");
+      write_restart("Dati.cart.out", p, time, V);
+    }
+    if (time + deltat >= (ifield + 1) * p.dt_field) {
+      if (prev_was_close || (std::floor((time + 0.5 * deltat) / p.dt_field) >
+                                 std::floor((time - 0.5 * deltat) / p.dt_field) &&
+                             time > time0)) {
+        ++ifield;
+        std::string name = "Dati.cart." + std::to_string(ifield) + ".out";
+        std::printf(" Writing %s at time %g\n", name.c_str(), time);
+        check(chgpu_download_field(h, V.data()), h, "download");
+        write_restart(name, p, time, V);
+        prev_was_close = false;
+      } else {
+        prev_was_close = true;
+      }
+    }
+  }
+  std::printf(" End of time/iterations loop: writing restart file at time %g\n", time);
+  check(chgpu_download_field(h, V.data()), h, "download");
+  write_restart("Dati.cart.out", p, time, V);
+  chgpu_destroy(h);
+  return 0;
+}

@@ -45,7 +45,8 @@ struct ConvLaunch {
   int products;  // 0: stop after the x pass (the start-up CFL pass)
 };
 
-template <typename T> void launch_convolutions(const ConvLaunch& L, cudaStream_t s);
+// stage 0: z-inverse, 1: x rows, 2: z-forward
+template <typename T> void launch_convolutions(const ConvLaunch& L, cudaStream_t s, int stage);
 cudaError_t conv_set_smem_limits();
 
 struct SolveLaunch {

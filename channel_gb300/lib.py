@@ -71,7 +71,11 @@ SIGNATURES = {
     "chgpu_stream": (C.c_void_p, [_P]),
     "chgpu_launch_count": (C.c_longlong, [_P]),
     "chgpu_last_error": (C.c_char_p, [_P]),
+    "chgpu_set_profiling": (C.c_int, [_P, C.c_int]),
+    "chgpu_kernel_times": (C.c_int, [_P, _DP, C.POINTER(C.c_longlong)]),
+    "chgpu_kernel_kind_name": (C.c_char_p, [C.c_int]),
 }
+NKINDS = 6
 
 
 def library_path() -> Path:
@@ -192,6 +196,16 @@ class Channel:
 
     def synchronize(self):
         self._check(self.lib.chgpu_synchronize(self.h))
+
+    def set_profiling(self, on: bool):
+        self._check(self.lib.chgpu_set_profiling(self.h, int(on)))
+
+    def kernel_times(self) -> dict:
+        """{kernel kind: (summed device ms, launches)} since profiling was enabled."""
+        ms = np.zeros(NKINDS)
+        n = (C.c_longlong * NKINDS)()
+        self._check(self.lib.chgpu_kernel_times(self.h, _dp(ms), n))
+        return {self.lib.chgpu_kernel_kind_name(k).decode(): (float(ms[k]), int(n[k])) for k in range(NKINDS)}
 
     @property
     def launches(self) -> int:

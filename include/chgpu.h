@@ -122,6 +122,17 @@ int chgpu_synchronize(chgpu_handle* h);
  * work against the solver's. */
 void* chgpu_stream(chgpu_handle* h);
 
+/* Per-kernel device timing (the per-step timing of the reference's `chron`
+ * flag, channel.f90:119-121,175-178, refined to kernels).  While profiling is
+ * on, chgpu_step issues its launches directly on the stream with a CUDA event
+ * pair around each kernel instead of replaying the graph.
+ * chgpu_kernel_times synchronises and returns, per kernel kind, the summed
+ * device milliseconds and launch counts since profiling was switched on. */
+#define CHGPU_NKINDS 6 /* z-inverse, x-rows, z-forward, rhs, linsolve, scalars */
+int chgpu_set_profiling(chgpu_handle* h, int on);
+int chgpu_kernel_times(chgpu_handle* h, double ms[CHGPU_NKINDS], long long launches[CHGPU_NKINDS]);
+const char* chgpu_kernel_kind_name(int kind);
+
 /* Kernel launches issued by the handle since creation (for accounting). */
 long long chgpu_launch_count(const chgpu_handle* h);
 

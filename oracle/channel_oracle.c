@@ -373,6 +373,7 @@ static void setup_boundary_conditions(orc_state* s) {
 }
 
 orc_state* orc_create(const orc_params* p, int nthreads) {
+  if (p->ny < 8 || p->nx < 1 || p->nz < 1) return NULL;
   orc_state* s = (orc_state*)calloc(1, sizeof(orc_state));
   s->p = *p;
   s->nx = p->nx; s->ny = p->ny; s->nz = p->nz;
@@ -700,6 +701,10 @@ static void complex_deriv(const orc_state* s, const cplx* f0, cplx* f1) {
   LeftLU5divStep2(s->D0mat, f1, ny + 1);
 #undef F0
 #undef F1
+}
+
+void orc_deriv(const orc_state* s, const double* f0, double* f1) {
+  complex_deriv(s, (const cplx*)f0, (cplx*)f1);
 }
 
 static void applybc_0(double* EQ, const double* bc0, const double* bc0m1) { /* dnsdata.f90:458-464 */

@@ -81,6 +81,7 @@ def lib():
         L.orc_step.argtypes = [P, C.POINTER(Line)]
         L.orc_start.argtypes = [P, C.POINTER(Line)]
         L.orc_fft.argtypes = [C.c_int, C.c_int, C.c_int, D]
+        L.orc_deriv.argtypes = [P, D, D]
         L.orc_fftfit.restype = C.c_int
         L.orc_fftfit.argtypes = [C.c_int]
         _lib = L
@@ -168,6 +169,13 @@ class Oracle:
         out = np.empty((6, self.p.nx + 1, 2 * self.p.nz + 1), dtype=np.complex128)
         c = lib().orc_convolve_plane(self.h, iy, _dp(out.view(np.float64)))
         return out, c
+
+    def deriv(self, f: np.ndarray) -> np.ndarray:
+        """Compact first y-derivative of a complex y-line (iy=-1..ny+1)."""
+        a = np.ascontiguousarray(f, dtype=np.complex128)
+        out = np.empty_like(a)
+        lib().orc_deriv(self.h, _dp(a.view(np.float64)), _dp(out.view(np.float64)))
+        return out
 
     def yintegr(self, f: np.ndarray) -> float:
         a = np.ascontiguousarray(f, dtype=np.float64)
