@@ -1,0 +1,122 @@
+!==============================================================!
+! Fortran 2008 interface to libchgpu.so (include/chgpu.h).    !
+! Lets a Fortran driver shaped like channel.f90 call the GB300 !
+! time step through iso_c_binding.  Compile with the driver    !
+! and link -lchgpu (see INTEGRATION.md).                       !
+!==============================================================!
+MODULE chgpu_interface
+  USE, INTRINSIC :: iso_c_binding
+  IMPLICIT NONE
+
+  INTEGER(C_INT), PARAMETER :: CHGPU_FP64 = 0, CHGPU_MIXED = 1
+
+  ! Mirrors chgpu_params field by field (C layout).
+  TYPE, BIND(C) :: chgpu_params
+    INTEGER(C_INT)       :: nx, ny, nz
+    REAL(C_DOUBLE)       :: alfa0, beta0
+    REAL(C_DOUBLE)       :: ni
+    REAL(C_DOUBLE)       :: a, ymin, ymax
+    INTEGER(C_INT)       :: cpi, cpi_type
+    REAL(C_DOUBLE)       :: gamma
+    REAL(C_DOUBLE)       :: meanpx, meanpz
+    REAL(C_DOUBLE)       :: meanflowx, meanflowz
+    REAL(C_DOUBLE)       :: u0, uN
+    REAL(C_DOUBLE)       :: deltat, cflmax, time
+    REAL(C_DOUBLE)       :: dt_field, dt_save, t_max
+    INTEGER(C_INT)       :: time_from_restart
+    INTEGER(C_LONG_LONG) :: nstep
+    INTEGER(C_INT)       :: npy
+    INTEGER(C_INT)       :: precision
+  END TYPE chgpu_params
+
+  ! Mirrors chgpu_stats: line(1:11) is one Runtimedata record.
+  TYPE, BIND(C) :: chgpu_stats
+    REAL(C_DOUBLE)       :: line(11)
+    REAL(C_DOUBLE)       :: fr(3)
+    REAL(C_DOUBLE)       :: corrpx, corrpz, meanpx, meanpz
+    REAL(C_DOUBLE)       :: cfl, deltat, time
+    INTEGER(C_LONG_LONG) :: istep
+  END TYPE chgpu_stats
+
+  INTERFACE
+    INTEGER(C_INT) FUNCTION chgpu_create(p, h) BIND(C, name="chgpu_create")
+      IMPORT :: C_INT, C_PTR, chgpu_params
+      TYPE(chgpu_params), INTENT(IN) :: p
+      TYPE(C_PTR), INTENT(OUT) :: h
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION chgpu_destroy(h) BIND(C, name="chgpu_destroy")
+      IMPORT :: C_INT, C_PTR
+      TYPE(C_PTR), VALUE :: h
+    END FUNCTION
+    ! V is the reference's V(-1:ny+1,-nz:nz,0:nx,1:3), complex(C_DOUBLE_COMPLEX)
+    INTEGER(C_INT) FUNCTION chgpu_upload_field(h, V) BIND(C, name="chgpu_upload_field")
+      IMPORT :: C_INT, C_PTR, C_DOUBLE_COMPLEX
+      TYPE(C_PTR), VALUE :: h
+      COMPLEX(C_DOUBLE_COMPLEX), INTENT(IN) :: V(*)
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION chgpu_download_field(h, V) BIND(C, name="chgpu_download_field")
+      IMPORT :: C_INT, C_PTR, C_DOUBLE_COMPLEX
+      TYPE(C_PTR), VALUE :: h
+      COMPLEX(C_DOUBLE_COMPLEX), INTENT(OUT) :: V(*)
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION chgpu_start(h, time, deltat, st) BIND(C, name="chgpu_start")
+      IMPORT :: C_INT, C_PTR, C_DOUBLE, chgpu_stats
+      TYPE(C_PTR), VALUE :: h
+      REAL(C_DOUBLE), VALUE :: time, deltat
+      TYPE(chgpu_stats), INTENT(OUT) :: st
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION chgpu_set_wall_velocity(h, u0, uN) BIND(C, name="chgpu_set_wall_velocity")
+      IMPORT :: C_INT, C_PTR, C_DOUBLE
+      TYPE(C_PTR), VALUE :: h
+      REAL(C_DOUBLE), VALUE :: u0, uN
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION chgpu_buildrhs(h, ode, compute_cfl) BIND(C, name="chgpu_buildrhs")
+      IMPORT :: C_INT, C_PTR, C_DOUBLE
+      TYPE(C_PTR), VALUE :: h
+      REAL(C_DOUBLE), INTENT(IN) :: ode(3)
+      INTEGER(C_INT), VALUE :: compute_cfl
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION chgpu_linsolve(h, lambda) BIND(C, name="chgpu_linsolve")
+      IMPORT :: C_INT, C_PTR, C_DOUBLE
+      TYPE(C_PTR), VALUE :: h
+      REAL(C_DOUBLE), VALUE :: lambda
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION chgpu_outstats(h, st) BIND(C, name="chgpu_outstats")
+      IMPORT :: C_INT, C_PTR, chgpu_stats
+      TYPE(C_PTR), VALUE :: h
+      TYPE(chgpu_stats), INTENT(OUT) :: st
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION chgpu_step(h, st) BIND(C, name="chgpu_step")
+      IMPORT :: C_INT, C_PTR, chgpu_stats
+      TYPE(C_PTR), VALUE :: h
+      TYPE(chgpu_stats), INTENT(OUT) :: st
+    END FUNCTION
+    TYPE(C_PTR) FUNCTION chgpu_last_error(h) BIND(C, name="chgpu_last_error")
+      IMPORT :: C_PTR
+      TYPE(C_PTR), VALUE :: h
+    END FUNCTION
+  END INTERFACE
+
+CONTAINS
+
+  ! dns.in values as read_dnsin leaves them -> chgpu_params
+  FUNCTION chgpu_params_from(nx, ny, nz, alfa0, beta0, ni, a, ymin, ymax, cpi, cpi_type, gamma, meanpx, meanpz, &
+                             meanflowx, meanflowz, u0, uN, deltat, cflmax, time, dt_field, dt_save, t_max, &
+                             time_from_restart, nstep, npy, precision) RESULT(p)
+    INTEGER(C_INT), INTENT(IN) :: nx, ny, nz, cpi_type, npy, precision
+    REAL(C_DOUBLE), INTENT(IN) :: alfa0, beta0, ni, a, ymin, ymax, gamma, meanpx, meanpz, meanflowx, meanflowz
+    REAL(C_DOUBLE), INTENT(IN) :: u0, uN, deltat, cflmax, time, dt_field, dt_save, t_max
+    LOGICAL, INTENT(IN) :: cpi, time_from_restart
+    INTEGER(C_SIZE_T), INTENT(IN) :: nstep
+    TYPE(chgpu_params) :: p
+    p%nx = nx; p%ny = ny; p%nz = nz; p%alfa0 = alfa0; p%beta0 = beta0; p%ni = ni
+    p%a = a; p%ymin = ymin; p%ymax = ymax
+    p%cpi = MERGE(1, 0, cpi); p%cpi_type = cpi_type; p%gamma = gamma
+    p%meanpx = meanpx; p%meanpz = meanpz; p%meanflowx = meanflowx; p%meanflowz = meanflowz
+    p%u0 = u0; p%uN = uN; p%deltat = deltat; p%cflmax = cflmax; p%time = time
+    p%dt_field = dt_field; p%dt_save = dt_save; p%t_max = t_max
+    p%time_from_restart = MERGE(1, 0, time_from_restart)
+    p%nstep = INT(nstep, C_LONG_LONG); p%npy = npy; p%precision = precision
+  END FUNCTION chgpu_params_from
+
+END MODULE chgpu_interface

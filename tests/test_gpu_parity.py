@@ -155,3 +155,18 @@ def test_mixed_precision_close_to_fp64(gpu_lib):
     assert abs(lm[1] - l64[1]) / abs(l64[1]) <= 1e-4
     g64.close()
     gm.close()
+
+
+def test_nonfinite_field_is_reported(gpu_lib):
+    """A NaN planted (on the host) in the uploaded field surfaces as
+    CHGPU_E_NONFINITE from the next synchronising call, not as a crash."""
+    from channel_gb300 import ChannelError
+
+    _, V0, _, g = make("small", 0.01, 0)
+    V = V0.copy()
+    V[1, 2, 5, 10] = np.nan
+    g.upload(V)
+    with pytest.raises(ChannelError) as e:
+        g.start()
+    assert e.value.code == -4
+    g.close()
