@@ -22,7 +22,7 @@ DRIVER = OUT / "channel_gb300"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", str(ROOT / "include")]
-SOURCES = ["capi.cu", "conv.cu", "solve.cu", "setup.cpp"]
+SOURCES = ["capi.cu", "conv.cu", "solve.cu", "setup.cpp", "noalloc.cu"]
 
 
 def nvcc() -> str:

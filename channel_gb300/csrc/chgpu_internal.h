@@ -26,6 +26,21 @@ struct Tables {
   std::vector<double> yint;  // yintegr weights: [(iy-1)/2][3] for odd iy    (dnsdata.f90:317-323)
 };
 
+// The same tables in fixed-capacity arrays (no heap), for the entry point
+// that allocates nothing; ny <= kMaxNy.
+struct StaticTables {
+  static constexpr int kMaxNy = 1024;
+  int ny = 0, nyint = 0;
+  double y[kMaxNy + 3];
+  double der[(kMaxNy + 1) * 20];
+  double d0lu[(kMaxNy + 1) * 5];
+  double yint[3 * (kMaxNy / 2 + 1)];
+  double d140[5], d14m1[5], d14n[5], d14np1[5];
+  double v0bc[5], v0m1bc[5], eta0bc[5], eta0m1bc[5];
+  double vnbc[5], vnp1bc[5], etanbc[5], etanp1bc[5];
+};
+bool compute_tables_static(const chgpu_params& p, StaticTables& t);
+
 bool fft_fit(int n);                       // ffts.f90:78-86
 void padded_sizes(int nx, int nz, int* nxd, int* nzd);  // dnsdata.f90:110-114
 void compute_tables(const chgpu_params& p, Tables& t);

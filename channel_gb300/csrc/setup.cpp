@@ -209,4 +209,136 @@ void compute_tables(const chgpu_params& p, Tables& t) {
   }
 }
 
+namespace {
+
+// LU5decompStep of rows r=0..nrow-1 held in a plain array (see lu5_decomp).
+void lu5_decomp_array(double* A, int nrow) {
+  auto a = [&](int i, int j) -> double& { return A[(size_t)i * 5 + j + 2]; };
+  const int HI1 = nrow - 1, HI2 = 2;
+  a(HI1 - 2, 1) = 0; a(HI1 - 2, 2) = 0; a(HI1 - 3, 2) = 0;
+  for (int i = HI1 - HI2; i >= 0; --i) {
+    for (int k = HI2; k >= 1; --k) {
+      double piv = a(i, k);
+      for (int j = -1; j >= -2; --j) {
+        double below = (i + k <= HI1 - HI2) ? a(i + k, j) : 0.0;
+        a(i, j + k) = a(i, j + k) - piv * below;
+      }
+    }
+    double piv = 1.0 / a(i, 0);
+    a(i, 0) = piv;
+    a(i, -2) *= piv;
+    a(i, -1) *= piv;
+  }
+  a(0, -2) = 0; a(0, -1) = 0; a(1, -2) = 0;
+}
+
+void vander_array(const double* y, int first, double y0, double M[5][5], const double* scale) {
+  for (int i = 0; i < 5; ++i)
+    for (int j = 0; j < 5; ++j) {
+      double v = std::pow(y[first + j + 1] - y0, 4.0 - i);
+      M[i][j] = scale ? scale[i] * v : v;
+    }
+}
+
+}  // namespace
+
+// Same arithmetic as compute_tables, into fixed arrays.
+bool compute_tables_static(const chgpu_params& p, StaticTables& t) {
+  const int ny = p.ny;
+  if (ny < 8 || ny > StaticTables::kMaxNy) return false;
+  t.ny = ny;
+  double* y = t.y;
+  for (int iy = -1; iy <= ny + 1; ++iy)
+    y[iy + 1] = p.ymin + 0.5 * (p.ymax - p.ymin) * (std::tanh(p.a * (2.0 * (double)iy / (double)ny - 1)) / std::tanh(p.a) + 1);
+  std::memset(t.der, 0, sizeof(double) * (size_t)(ny + 1) * 20);
+  double M[5][5], rhs[5];
+  for (int iy = 1; iy <= ny - 1; ++iy) {
+    double* d0 = &t.der[(size_t)iy * 20 + 0];
+    double* d1 = &t.der[(size_t)iy * 20 + 5];
+    double* d2 = &t.der[(size_t)iy * 20 + 10];
+    double* d4 = &t.der[(size_t)iy * 20 + 15];
+    const double yc = y[iy + 1];
+    vander_array(y, iy - 2, yc, M, nullptr);
+    lu_decomp5(M);
+    std::memset(rhs, 0, sizeof rhs);
+    rhs[0] = 24;
+    lu_solve5(M, rhs, d4);
+    double sc[5];
+    for (int i = 0; i < 5; ++i) sc[i] = (5.0 - i) * (6.0 - i) * (7.0 - i) * (8.0 - i);
+    vander_array(y, iy - 2, yc, M, sc);
+    lu_decomp5(M);
+    for (int i = 0; i < 5; ++i) {
+      double acc = d4[0] * std::pow(y[iy - 1] - yc, 8.0 - i);
+      for (int j = 1; j < 5; ++j) acc = acc + d4[j] * std::pow(y[iy - 1 + j] - yc, 8.0 - i);
+      rhs[i] = acc;
+    }
+    lu_solve5(M, rhs, d0);
+    vander_array(y, iy - 2, yc, M, nullptr);
+    lu_decomp5(M);
+    std::memset(rhs, 0, sizeof rhs);
+    for (int i = 0; i <= 2; ++i) {
+      double acc = d0[0] * (4.0 - i) * (3.0 - i) * std::pow(y[iy - 1] - yc, 2.0 - i);
+      for (int j = 1; j < 5; ++j) acc = acc + d0[j] * (4.0 - i) * (3.0 - i) * std::pow(y[iy - 1 + j] - yc, 2.0 - i);
+      rhs[i] = acc;
+    }
+    lu_solve5(M, rhs, d2);
+    std::memset(rhs, 0, sizeof rhs);
+    for (int i = 0; i <= 3; ++i) {
+      double acc = d0[0] * (4.0 - i) * std::pow(y[iy - 1] - yc, 3.0 - i);
+      for (int j = 1; j < 5; ++j) acc = acc + d0[j] * (4.0 - i) * std::pow(y[iy - 1 + j] - yc, 3.0 - i);
+      rhs[i] = acc;
+    }
+    lu_solve5(M, rhs, d1);
+  }
+  double d040[5] = {0, 1, 0, 0, 0}, d04n[5] = {0, 0, 0, 1, 0};
+  vander_array(y, -1, y[1], M, nullptr);
+  lu_decomp5(M);
+  std::memset(rhs, 0, sizeof rhs); rhs[3] = 1.0; lu_solve5(M, rhs, t.d140);
+  vander_array(y, -1, y[0], M, nullptr);
+  lu_decomp5(M);
+  std::memset(rhs, 0, sizeof rhs); rhs[3] = 1.0; lu_solve5(M, rhs, t.d14m1);
+  vander_array(y, ny - 3, y[ny + 1], M, nullptr);
+  lu_decomp5(M);
+  std::memset(rhs, 0, sizeof rhs); rhs[3] = 1; lu_solve5(M, rhs, t.d14n);
+  vander_array(y, ny - 3, y[ny + 2], M, nullptr);
+  lu_decomp5(M);
+  std::memset(rhs, 0, sizeof rhs); rhs[3] = 1; lu_solve5(M, rhs, t.d14np1);
+  std::memset(t.d0lu, 0, sizeof(double) * (size_t)(ny + 1) * 5);
+  for (int iy = 1; iy <= ny - 1; ++iy)
+    for (int j = 0; j < 5; ++j) t.d0lu[(size_t)(iy - 1) * 5 + j] = t.der[(size_t)iy * 20 + j];
+  lu5_decomp_array(t.d0lu, ny + 1);
+  std::memcpy(t.v0bc, d040, 40);
+  std::memcpy(t.v0m1bc, t.d140, 40);
+  std::memcpy(t.eta0bc, d040, 40);
+  std::memcpy(t.eta0m1bc, &t.der[(size_t)1 * 20 + 15], 40);
+  {
+    double v[5], e[5];
+    std::memcpy(v, t.v0bc, 40); std::memcpy(e, t.eta0bc, 40);
+    for (int j = 1; j < 5; ++j) t.v0bc[j] = v[j] - v[0] * t.v0m1bc[j] / t.v0m1bc[0];
+    for (int j = 1; j < 5; ++j) t.eta0bc[j] = e[j] - e[0] * t.eta0m1bc[j] / t.eta0m1bc[0];
+  }
+  std::memcpy(t.vnbc, d04n, 40);
+  std::memcpy(t.vnp1bc, t.d14n, 40);
+  std::memcpy(t.etanbc, d04n, 40);
+  std::memcpy(t.etanp1bc, &t.der[(size_t)(ny - 1) * 20 + 15], 40);
+  {
+    double v[5], e[5];
+    std::memcpy(v, t.vnbc, 40); std::memcpy(e, t.etanbc, 40);
+    for (int j = 0; j < 4; ++j) t.vnbc[j] = v[j] - v[4] * t.vnp1bc[j] / t.vnp1bc[4];
+    for (int j = 0; j < 4; ++j) t.etanbc[j] = e[j] - e[4] * t.etanp1bc[j] / t.etanp1bc[4];
+  }
+  t.nyint = 0;
+  for (int iy = 1; iy <= ny - 1; iy += 2) {
+    double yp1 = y[iy + 2] - y[iy + 1], ym1 = y[iy] - y[iy + 1];
+    double a1 = -1.0 / 3.0 * ym1 + 1.0 / 6.0 * yp1 + 1.0 / 6.0 * yp1 * yp1 / ym1;
+    double a3 = +1.0 / 3.0 * yp1 - 1.0 / 6.0 * ym1 - 1.0 / 6.0 * ym1 * ym1 / yp1;
+    double a2 = yp1 - ym1 - a1 - a3;
+    t.yint[3 * t.nyint] = a1;
+    t.yint[3 * t.nyint + 1] = a2;
+    t.yint[3 * t.nyint + 2] = a3;
+    ++t.nyint;
+  }
+  return true;
+}
+
 }  // namespace chgpu

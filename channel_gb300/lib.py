@@ -74,6 +74,8 @@ SIGNATURES = {
     "chgpu_set_profiling": (C.c_int, [_P, C.c_int]),
     "chgpu_kernel_times": (C.c_int, [_P, _DP, C.POINTER(C.c_longlong)]),
     "chgpu_kernel_kind_name": (C.c_char_p, [C.c_int]),
+    "chgpu_linsolve_noalloc": (C.c_int, [C.POINTER(Params), C.c_double, C.c_void_p, _DP, C.c_void_p,
+                                         C.c_char_p, C.c_size_t]),
 }
 NKINDS = 6
 
