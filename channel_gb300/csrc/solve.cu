@@ -30,7 +30,6 @@ namespace {
 
 __device__ __forceinline__ double2 cz() { return make_double2(0.0, 0.0); }
 __device__ __forceinline__ double2 rmul(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
-__device__ __forceinline__ float2 rmulf(float s, float2 a) { return make_float2(s * a.x, s * a.y); }
 __device__ __forceinline__ double2 cdivr(double2 a, double s) { return make_double2(a.x / s, a.y / s); }
 // (0 + i a) * z, the product with ialfa/ibeta of the reference (the zero real
 // part contributes exact zeros)
@@ -99,22 +98,22 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
   const double ni = d.ni;
   const size_t r0 = ((size_t)0 * (d.ny - 1) + (iy - 1)) * d.nmodes + m;  // eta
   const size_t r1 = ((size_t)1 * (d.ny - 1) + (iy - 1)) * d.nmodes + m;  // d2v
-  // timescheme (dnsdata.f90:486) for D2v (:647)
+  // timescheme (dnsdata.f90:486) for D2v (:647): with S_k = Dk(V2),
+  //   unkn = S2 - k2 S0,  impl = sum OS V2 = ni (S4 - 2 k2 S2 + k2^2 S0)
+  const double odt = ode1 * (1.0 / dt);
   {
-    double2 s2 = rmul(c2[0], v2[0]), s0 = rmul(c0[0], v2[0]);
-    double os = ni * (c4[0] - 2.0 * k2 * c2[0] + k2 * k2 * c0[0]);
-    double2 impl = rmul(os, v2[0]);
+    double2 s0 = rmul(c0[0], v2[0]), s2 = rmul(c2[0], v2[0]), s4 = rmul(c4[0], v2[0]);
 #pragma unroll
     for (int j = 1; j < 5; ++j) {
-      s2 = s2 + rmul(c2[j], v2[j]);
       s0 = s0 + rmul(c0[j], v2[j]);
-      os = ni * (c4[j] - 2.0 * k2 * c2[j] + k2 * k2 * c0[j]);
-      impl = impl + rmul(os, v2[j]);
+      s2 = s2 + rmul(c2[j], v2[j]);
+      s4 = s4 + rmul(c4[j], v2[j]);
     }
     const double2 unkn = s2 - rmul(k2, s0);
+    const double2 impl = rmul(ni, s4 - rmul(2.0 * k2, s2) + rmul(k2 * k2, s0));
     const V2 o = old[r1];
     const double2 e = make_double2((double)explv.x, (double)explv.y);
-    double2 r = cdivr(rmul(ode1, unkn), dt) + impl;
+    double2 r = rmul(odt, unkn) + impl;
     r = r + rmul(ode2, e);
     r = r - rmul(ode3, make_double2((double)o.x, (double)o.y));
     old[r1] = explv;
@@ -133,27 +132,25 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
     const double2 unkn = make_double2(su, sw);
     const double2 impl = make_double2(ni * tu, ni * tw);
     const V2 o = old[r0];
-    double2 r = cdivr(rmul(ode1, unkn), dt) + impl;
+    double2 r = rmul(odt, unkn) + impl;
     r = r + rmul(ode2, e);
     r = r - rmul(ode3, make_double2((double)o.x, (double)o.y));
     old[r0] = mk<V2>((T)e.x, (T)e.y);
     rhs[r0] = r;
-  } else {  // eta (:656-661)
+  } else {  // eta (:656-661): with w = i kz V1 - i kx V3, unkn = D0(w), impl = ni (D2(w) - k2 D0(w))
     const V2 ee = mul_ia<V2>(tb, rhsu) - mul_ia<V2>(ta, rhsw);
-    double2 s1 = rmul(c0[0], v1[0]), s3 = rmul(c0[0], v3[0]);
-    double sq = ni * (c2[0] - k2 * c0[0]);
-    double2 impl = rmul(sq, mul_ia<double2>(b, v1[0]) - mul_ia<double2>(a, v3[0]));
+    double2 w = mul_ia<double2>(b, v1[0]) - mul_ia<double2>(a, v3[0]);
+    double2 s0 = rmul(c0[0], w), s2 = rmul(c2[0], w);
 #pragma unroll
     for (int j = 1; j < 5; ++j) {
-      s1 = s1 + rmul(c0[j], v1[j]);
-      s3 = s3 + rmul(c0[j], v3[j]);
-      sq = ni * (c2[j] - k2 * c0[j]);
-      impl = impl + rmul(sq, mul_ia<double2>(b, v1[j]) - mul_ia<double2>(a, v3[j]));
+      w = mul_ia<double2>(b, v1[j]) - mul_ia<double2>(a, v3[j]);
+      s0 = s0 + rmul(c0[j], w);
+      s2 = s2 + rmul(c2[j], w);
     }
-    const double2 unkn = mul_ia<double2>(b, s1) - mul_ia<double2>(a, s3);
+    const double2 impl = rmul(ni, s2 - rmul(k2, s0));
     const V2 o = old[r0];
     const double2 e = make_double2((double)ee.x, (double)ee.y);
-    double2 r = cdivr(rmul(ode1, unkn), dt) + impl;
+    double2 r = rmul(odt, s0) + impl;
     r = r + rmul(ode2, e);
     r = r - rmul(ode3, make_double2((double)o.x, (double)o.y));
     old[r0] = ee;
@@ -176,16 +173,29 @@ template void launch_rhs<float>(const SolveLaunch&, cudaStream_t);
 // ---------------------------------------------------------------------------
 namespace {
 
-// one row of the two pentadiagonal matrices (linsolve_blocking.inc:12-13)
-__device__ __forceinline__ void assemble(const double* __restrict__ dr, double lambda, double k2, double ni,
-                                         double Dv[5], double De[5]) {
+// One row of the two pentadiagonal matrices (linsolve_blocking.inc:12-13),
+//   D2vmat = lambda (d2 - k2 d0) - ni (d4 - 2 k2 d2 + k2^2 d0)
+//          = cv4 d4 + cv2 d2 + cv0 d0,
+//   etamat = lambda d0 - ni (d2 - k2 d0) = ce0 d0 + ce2 d2,
+// with the per-mode scalars of AsmCoef.
+struct AsmCoef {
+  double cv4, cv2, cv0, ce0, ce2;
+};
+__device__ __forceinline__ AsmCoef asm_coef(double lambda, double k2, double ni) {
+  AsmCoef c;
+  c.cv4 = -ni;
+  c.cv2 = lambda + 2.0 * ni * k2;
+  c.cv0 = -(lambda * k2 + ni * k2 * k2);
+  c.ce0 = lambda + ni * k2;
+  c.ce2 = -ni;
+  return c;
+}
+__device__ __forceinline__ void assemble(const double* __restrict__ dr, const AsmCoef& c, double Dv[5], double De[5]) {
 #pragma unroll
   for (int j = 0; j < 5; ++j) {
     const double d0 = __ldg(dr + j), d2 = __ldg(dr + 10 + j), d4 = __ldg(dr + 15 + j);
-    const double os = ni * (d4 - 2.0 * k2 * d2 + k2 * k2 * d0);
-    const double sq = ni * (d2 - k2 * d0);
-    Dv[j] = lambda * (d2 - k2 * d0) - os;
-    De[j] = lambda * d0 - sq;
+    Dv[j] = c.cv4 * d4 + c.cv2 * d2 + c.cv0 * d0;
+    De[j] = c.ce0 * d0 + c.ce2 * d2;
   }
 }
 
@@ -264,7 +274,7 @@ __device__ __forceinline__ double2 dot5(const double2* v, const double* c) {
 
 }  // namespace
 
-__global__ void __launch_bounds__(128) k_linsolve(double2* __restrict__ V, const double2* rhs, size_t rcs, int roff,
+__global__ void __launch_bounds__(64) k_linsolve(double2* __restrict__ V, const double2* rhs, size_t rcs, int roff,
                                                   double* __restrict__ fac, const double* __restrict__ der,
                                                   const double* __restrict__ d0lu, const double* __restrict__ yint,
                                                   BcRows bc, Dims d, double lambda_in, double ode1,
@@ -285,6 +295,8 @@ __global__ void __launch_bounds__(128) k_linsolve(double2* __restrict__ V, const
   const double ni = d.ni;
   const size_t P = d.npairs;
   const double b0eta = is00 ? sc->u0 : 0.0, bneta = is00 ? sc->uN : 0.0;
+  const AsmCoef ac = asm_coef(lambda, k2, ni);
+  const double rk2 = 1.0 / k2;  // u, w recovery divides by k2 (infinite only for the mean mode, which skips it)
 
   // ---- pass A: bottom-up assembly + BC fold + factor + Step1 ----
   double Lv1[2] = {0, 0}, Lv2[2] = {0, 0}, Le1[2] = {0, 0}, Le2[2] = {0, 0};
@@ -292,7 +304,7 @@ __global__ void __launch_bounds__(128) k_linsolve(double2* __restrict__ V, const
   double2 xc1 = cz(), xc2 = cz();  // unit-forcing response of the mean mode
   for (int iy = ny - 1; iy >= 1; --iy) {
     double Dv[5], De[5];
-    assemble(der + (size_t)iy * 20, lambda, k2, ni, Dv, De);
+    assemble(der + (size_t)iy * 20, ac, Dv, De);
     if (iy == ny - 1) { bc_top1(Dv, bc.vnbc, bc.vnp1bc); bc_top1(De, bc.etanbc, bc.etanp1bc); }
     if (iy == ny - 2) { bc_top2(Dv, bc.vnbc); bc_top2(De, bc.etanbc); }
     if (iy == 1) { bc_bot1(Dv, bc.v0bc, bc.v0m1bc); bc_bot1(De, bc.eta0bc, bc.eta0m1bc); }
@@ -524,8 +536,8 @@ __global__ void __launch_bounds__(128) k_linsolve(double2* __restrict__ V, const
           if (iy == -1) { bm2[t] = cz(); bm1[t] = vp; }
           const double bz = (t == 0 ? 1.0 : -1.0) * kb;
           const double2 et = V[vidx(d, 0, iy, mm[t])];
-          const double2 u = cdivr(mul_ia<double2>(ka, vp) - mul_ia<double2>(bz, et), k2);
-          const double2 w = cdivr(mul_ia<double2>(bz, vp) + mul_ia<double2>(ka, et), k2);
+          const double2 u = rmul(rk2, mul_ia<double2>(ka, vp) - mul_ia<double2>(bz, et));
+          const double2 w = rmul(rk2, mul_ia<double2>(bz, vp) + mul_ia<double2>(ka, et));
           V[vidx(d, 0, iy, mm[t])] = u;
           V[vidx(d, 2, iy, mm[t])] = w;
         }
@@ -535,8 +547,8 @@ __global__ void __launch_bounds__(128) k_linsolve(double2* __restrict__ V, const
 }
 
 void launch_linsolve(const SolveLaunch& L, cudaStream_t s) {
-  dim3 grid((L.d.npairs + 127) / 128);
-  k_linsolve<<<grid, 128, 0, s>>>(L.V, L.rhs_src, L.rhs_cstride, L.rhs_plane_off, L.fac, L.der, L.d0lu, L.yint, L.bc, L.d, L.lambda, L.ode[0],
+  dim3 grid((L.d.npairs + 63) / 64);
+  k_linsolve<<<grid, 64, 0, s>>>(L.V, L.rhs_src, L.rhs_cstride, L.rhs_plane_off, L.fac, L.der, L.d0lu, L.yint, L.bc, L.d, L.lambda, L.ode[0],
                                   L.lambda_from_dt, L.sc);
 }
 
