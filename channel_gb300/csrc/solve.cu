@@ -274,16 +274,22 @@ __device__ __forceinline__ double2 dot5(const double2* v, const double* c) {
 
 }  // namespace
 
+// Two threads per pair (kx, +-kz): role 0 owns the v system (D2vmat), role 1
+// the eta system (etamat; for the mean mode also the unit-forcing response).
+// A block holds 32 pairs: warp 0 the v systems, warp 1 the eta systems.  After
+// both have written v and eta, role r takes mode (kx, (1-2r)|kz|) for v' and
+// the u, w recovery.
 __global__ void __launch_bounds__(64) k_linsolve(double2* __restrict__ V, const double2* rhs, size_t rcs, int roff,
-                                                  double* __restrict__ fac, const double* __restrict__ der,
-                                                  const double* __restrict__ d0lu, const double* __restrict__ yint,
-                                                  BcRows bc, Dims d, double lambda_in, double ode1,
-                                                  int lambda_from_dt, DevScalars* __restrict__ sc) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= d.npairs) return;
+                                                 double* __restrict__ fac, const double* __restrict__ der,
+                                                 const double* __restrict__ d0lu, const double* __restrict__ yint,
+                                                 BcRows bc, Dims d, double lambda_in, double ode1,
+                                                 int lambda_from_dt, DevScalars* __restrict__ sc) {
+  const int lane = threadIdx.x & 31, role = threadIdx.x >> 5;
+  const int q = blockIdx.x * 32 + lane;
+  const bool active = q < d.npairs;
   const int ny = d.ny, nz = d.nz;
-  const int ix = q / (nz + 1);
-  const int a = q - ix * (nz + 1);
+  const int ix = active ? q / (nz + 1) : 0;
+  const int a = active ? q - ix * (nz + 1) : 0;
   const int nm = (a == 0) ? 1 : 2;
   int mm[2];
   mm[0] = ix * d.nzt + nz + a;
@@ -294,260 +300,243 @@ __global__ void __launch_bounds__(64) k_linsolve(double2* __restrict__ V, const 
   const double lambda = lambda_from_dt ? ode1 / sc->deltat : lambda_in;
   const double ni = d.ni;
   const size_t P = d.npairs;
-  const double b0eta = is00 ? sc->u0 : 0.0, bneta = is00 ? sc->uN : 0.0;
-  const AsmCoef ac = asm_coef(lambda, k2, ni);
-  const double rk2 = 1.0 / k2;  // u, w recovery divides by k2 (infinite only for the mean mode, which skips it)
-
-  // ---- pass A: bottom-up assembly + BC fold + factor + Step1 ----
-  double Lv1[2] = {0, 0}, Lv2[2] = {0, 0}, Le1[2] = {0, 0}, Le2[2] = {0, 0};
-  double2 xv1[2] = {cz(), cz()}, xv2[2] = {cz(), cz()}, xe1[2] = {cz(), cz()}, xe2[2] = {cz(), cz()};
-  double2 xc1 = cz(), xc2 = cz();  // unit-forcing response of the mean mode
-  for (int iy = ny - 1; iy >= 1; --iy) {
-    double Dv[5], De[5];
-    assemble(der + (size_t)iy * 20, ac, Dv, De);
-    if (iy == ny - 1) { bc_top1(Dv, bc.vnbc, bc.vnp1bc); bc_top1(De, bc.etanbc, bc.etanp1bc); }
-    if (iy == ny - 2) { bc_top2(Dv, bc.vnbc); bc_top2(De, bc.etanbc); }
-    if (iy == 1) { bc_bot1(Dv, bc.v0bc, bc.v0m1bc); bc_bot1(De, bc.eta0bc, bc.eta0m1bc); }
-    if (iy == 2) { bc_bot2(Dv, bc.v0bc); bc_bot2(De, bc.eta0bc); }
-    double2 bv[2], be[2];
+  const int vc = role == 0 ? 1 : 0;  // field component this role solves for (v or eta)
+  // boundary rows of this role's system, selected element by element
+  double bot[5], botm1[5], top[5], topp1[5];
 #pragma unroll
-    for (int t = 0; t < 2; ++t) {
-      if (t < nm) {
-        bv[t] = rhs[rcs + (size_t)(iy + roff) * d.nmodes + mm[t]];
-        be[t] = rhs[(size_t)(iy + roff) * d.nmodes + mm[t]];
-      }
-    }
-    if (is00) {  // wall values of the mean mode's packed U+iW (linsolve_blocking.inc:26-27,40-41)
-      if (iy == 1) be[0] = be[0] - make_double2(De[1] * b0eta / bc.eta0bc[1], De[1] * 0.0 / bc.eta0bc[1]);
-      if (iy == 2) be[0] = be[0] - make_double2(De[0] * b0eta / bc.eta0bc[1], De[0] * 0.0 / bc.eta0bc[1]);
-      if (iy == ny - 1) be[0] = be[0] - make_double2(De[3] * bneta / bc.etanbc[3], De[3] * 0.0 / bc.etanbc[3]);
-      if (iy == ny - 2) be[0] = be[0] - make_double2(De[4] * bneta / bc.etanbc[3], De[4] * 0.0 / bc.etanbc[3]);
-    }
-    if (iy == ny - 1) { Dv[3] = Dv[4] = 0; De[3] = De[4] = 0; }  // rbparmat_blocking.f90:29
-    if (iy == ny - 2) { Dv[4] = 0; De[4] = 0; }
-    lu_row(Dv, Lv1, Lv2);
-    lu_row(De, Le1, Le2);
-    const double2 cu = make_double2(1.0, 0.0);
-#pragma unroll
-    for (int t = 0; t < 2; ++t) {
-      if (t < nm) {
-        const double2 nv = step1(bv[t], Dv, xv1[t], xv2[t]);
-        const double2 ne = step1(be[t], De, xe1[t], xe2[t]);
-        xv2[t] = xv1[t]; xv1[t] = nv;
-        xe2[t] = xe1[t]; xe1[t] = ne;
-        V[vidx(d, 1, iy, mm[t])] = nv;
-        V[vidx(d, 0, iy, mm[t])] = ne;
-      }
-    }
-    if (is00) {
-      const double2 nc = step1(cu, De, xc1, xc2);
-      xc2 = xc1; xc1 = nc;
-      V[vidx(d, 2, iy, mm[0])] = nc;
-    }
-    Lv2[0] = Lv1[0]; Lv2[1] = Lv1[1]; Lv1[0] = Dv[0]; Lv1[1] = Dv[1];
-    Le2[0] = Le1[0]; Le2[1] = Le1[1]; Le1[0] = De[0]; Le1[1] = De[1];
-    if (iy == 1) { Dv[0] = Dv[1] = 0; De[0] = De[1] = 0; }  // rbparmat_blocking.f90:45
-    if (iy == 2) { Dv[0] = 0; De[0] = 0; }
-    double* f = fac + (size_t)(iy - 1) * 4 * P + q;
-    f[0] = Dv[0]; f[P] = Dv[1]; f[2 * P] = De[0]; f[3 * P] = De[1];
+  for (int j = 0; j < 5; ++j) {
+    bot[j] = role ? bc.eta0bc[j] : bc.v0bc[j];
+    botm1[j] = role ? bc.eta0m1bc[j] : bc.v0m1bc[j];
+    top[j] = role ? bc.etanbc[j] : bc.vnbc[j];
+    topp1[j] = role ? bc.etanp1bc[j] : bc.vnp1bc[j];
   }
+  // wall values: zero except the mean mode's packed U+iW (channel.f90:122-124)
+  const double bval0 = (role == 1 && is00) ? sc->u0 : 0.0;
+  const double bvaln = (role == 1 && is00) ? sc->uN : 0.0;
+  const bool ucor = role == 1 && is00;
+  const AsmCoef ac = asm_coef(lambda, k2, ni);
 
-  // ---- pass B: top-down Step2, keeping the rows the wall closures need ----
-  double2 v[2][7], e[2][7], cc[7];  // rows 1..3 at [0..2], ny-3..ny-1 at [3..5]
-  {
-    double2 vm2[2] = {cz(), cz()}, vm1[2] = {cz(), cz()}, em2[2] = {cz(), cz()}, em1[2] = {cz(), cz()};
-    double2 cm2 = cz(), cm1 = cz();
-    for (int iy = 1; iy <= ny - 1; ++iy) {
-      const double* f = fac + (size_t)(iy - 1) * 4 * P + q;
-      const double lv2 = f[0], lv1 = f[P], le2 = f[2 * P], le1 = f[3 * P];
+  if (active) {
+    // ---- pass A: bottom-up assembly + BC fold + factor + Step1 ----
+    double L1[2] = {0, 0}, L2[2] = {0, 0};
+    double2 x1[2] = {cz(), cz()}, x2[2] = {cz(), cz()};
+    double2 xc1 = cz(), xc2 = cz();
+    const double2* rsrc = rhs + (role == 0 ? rcs : 0);
+    for (int iy = ny - 1; iy >= 1; --iy) {
+      const double* dr = der + (size_t)iy * 20;
+      double A[5];
+#pragma unroll
+      for (int j = 0; j < 5; ++j) {
+        const double d0 = __ldg(dr + j), d2 = __ldg(dr + 10 + j);
+        A[j] = role ? ac.ce0 * d0 + ac.ce2 * d2 : ac.cv4 * __ldg(dr + 15 + j) + ac.cv2 * d2 + ac.cv0 * d0;
+      }
+      if (iy == ny - 1) bc_top1(A, top, topp1);
+      if (iy == ny - 2) bc_top2(A, top);
+      if (iy == 1) bc_bot1(A, bot, botm1);
+      if (iy == 2) bc_bot2(A, bot);
+      double2 b[2];
+#pragma unroll
+      for (int t = 0; t < 2; ++t)
+        if (t < nm) b[t] = rsrc[(size_t)(iy + roff) * d.nmodes + mm[t]];
+      if (role == 1 && is00) {  // the packed wall velocity enters rows 1, 2, ny-2, ny-1 (linsolve_blocking.inc:26-27,40-41)
+        if (iy == 1) b[0] = b[0] - make_double2(A[1] * bval0 / bot[1], A[1] * 0.0 / bot[1]);
+        if (iy == 2) b[0] = b[0] - make_double2(A[0] * bval0 / bot[1], A[0] * 0.0 / bot[1]);
+        if (iy == ny - 1) b[0] = b[0] - make_double2(A[3] * bvaln / top[3], A[3] * 0.0 / top[3]);
+        if (iy == ny - 2) b[0] = b[0] - make_double2(A[4] * bvaln / top[3], A[4] * 0.0 / top[3]);
+      }
+      if (iy == ny - 1) { A[3] = 0; A[4] = 0; }  // rbparmat_blocking.f90:29
+      if (iy == ny - 2) A[4] = 0;
+      lu_row(A, L1, L2);
 #pragma unroll
       for (int t = 0; t < 2; ++t) {
         if (t < nm) {
-          const double2 nv = step2(V[vidx(d, 1, iy, mm[t])], lv2, lv1, vm2[t], vm1[t]);
-          const double2 ne = step2(V[vidx(d, 0, iy, mm[t])], le2, le1, em2[t], em1[t]);
-          V[vidx(d, 1, iy, mm[t])] = nv;
-          V[vidx(d, 0, iy, mm[t])] = ne;
-          vm2[t] = vm1[t]; vm1[t] = nv;
-          em2[t] = em1[t]; em1[t] = ne;
-          if (iy <= 3) { v[t][iy - 1] = nv; e[t][iy - 1] = ne; }
-          if (iy >= ny - 3) { v[t][iy - (ny - 3) + 3] = nv; e[t][iy - (ny - 3) + 3] = ne; }
+          const double2 nx_ = step1(b[t], A, x1[t], x2[t]);
+          x2[t] = x1[t];
+          x1[t] = nx_;
+          V[vidx(d, vc, iy, mm[t])] = nx_;
         }
       }
-      if (is00) {
-        const double2 nc = step2(V[vidx(d, 2, iy, mm[0])], le2, le1, cm2, cm1);
+      if (ucor) {
+        const double2 nc = step1(make_double2(1.0, 0.0), A, xc1, xc2);
+        xc2 = xc1;
+        xc1 = nc;
         V[vidx(d, 2, iy, mm[0])] = nc;
-        cm2 = cm1; cm1 = nc;
-        if (iy <= 3) cc[iy - 1] = nc;
-        if (iy >= ny - 3) cc[iy - (ny - 3) + 3] = nc;
+      }
+      L2[0] = L1[0]; L2[1] = L1[1];
+      L1[0] = A[0]; L1[1] = A[1];
+      if (iy == 1) { A[0] = 0; A[1] = 0; }  // rbparmat_blocking.f90:45
+      if (iy == 2) A[0] = 0;
+      double* f = fac + ((size_t)(iy - 1) * 4 + 2 * role) * P + q;
+      f[0] = A[0];
+      f[P] = A[1];
+    }
+    // ---- pass B: top-down Step2; rows 1..3 and ny-3..ny-1 kept for the walls ----
+    double2 lo[2][3], hi[2][3], clo[3], chi[3];
+    {
+      double2 m2[2] = {cz(), cz()}, m1[2] = {cz(), cz()}, c2 = cz(), c1 = cz();
+      for (int iy = 1; iy <= ny - 1; ++iy) {
+        const double* f = fac + ((size_t)(iy - 1) * 4 + 2 * role) * P + q;
+        const double l2 = f[0], l1 = f[P];
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+          if (t < nm) {
+            const double2 nv = step2(V[vidx(d, vc, iy, mm[t])], l2, l1, m2[t], m1[t]);
+            V[vidx(d, vc, iy, mm[t])] = nv;
+            m2[t] = m1[t];
+            m1[t] = nv;
+            if (iy == 1) lo[t][0] = nv;
+            if (iy == 2) lo[t][1] = nv;
+            if (iy == 3) lo[t][2] = nv;
+            if (iy == ny - 3) hi[t][0] = nv;
+            if (iy == ny - 2) hi[t][1] = nv;
+            if (iy == ny - 1) hi[t][2] = nv;
+          }
+        }
+        if (ucor) {
+          const double2 nc = step2(V[vidx(d, 2, iy, mm[0])], l2, l1, c2, c1);
+          V[vidx(d, 2, iy, mm[0])] = nc;
+          c2 = c1;
+          c1 = nc;
+          if (iy == 1) clo[0] = nc;
+          if (iy == 2) clo[1] = nc;
+          if (iy == 3) clo[2] = nc;
+          if (iy == ny - 3) chi[0] = nc;
+          if (iy == ny - 2) chi[1] = nc;
+          if (iy == ny - 1) chi[2] = nc;
+        }
       }
     }
-  }
-  // wall and ghost values (linsolve_blocking.inc:50-61); boundary values are
-  // zero except the mean mode's eta (packed wall velocity)
-  double2 vw[2][4], ew[2][4];  // [0]=iy -1, [1]=iy 0, [2]=iy ny, [3]=iy ny+1
-#pragma unroll
-  for (int t = 0; t < 2; ++t) {
-    if (t < nm) {
-      const double2* vb = &v[t][0];
-      const double2* eb = &e[t][0];
-      double2 w0 = rmul(-1.0, dot3(vb, bc.v0bc + 2));
-      w0 = cdivr(w0, bc.v0bc[1]);
-      double2 tmp[4] = {w0, vb[0], vb[1], vb[2]};
-      double2 wm1 = cdivr(rmul(-1.0, dot4(tmp, bc.v0m1bc + 1)), bc.v0m1bc[0]);
-      double2 e0 = cdivr(make_double2(b0eta, 0.0) - dot3(eb, bc.eta0bc + 2), bc.eta0bc[1]);
-      double2 tmpe[4] = {e0, eb[0], eb[1], eb[2]};
-      double2 em1 = cdivr(rmul(-1.0, dot4(tmpe, bc.eta0m1bc + 1)), bc.eta0m1bc[0]);
-      const double2* vt = &v[t][3];
-      const double2* et = &e[t][3];
-      double2 wn = cdivr(rmul(-1.0, dot3(vt, bc.vnbc)), bc.vnbc[3]);
-      double2 tmpt[4] = {vt[0], vt[1], vt[2], wn};
-      double2 wn1 = cdivr(rmul(-1.0, dot4(tmpt, bc.vnp1bc)), bc.vnp1bc[4]);
-      double2 en = cdivr(make_double2(bneta, 0.0) - dot3(et, bc.etanbc), bc.etanbc[3]);
-      double2 tmpte[4] = {et[0], et[1], et[2], en};
-      double2 en1 = cdivr(rmul(-1.0, dot4(tmpte, bc.etanp1bc)), bc.etanp1bc[4]);
-      vw[t][0] = wm1; vw[t][1] = w0; vw[t][2] = wn; vw[t][3] = wn1;
-      ew[t][0] = em1; ew[t][1] = e0; ew[t][2] = en; ew[t][3] = en1;
-      V[vidx(d, 1, -1, mm[t])] = wm1;
-      V[vidx(d, 1, 0, mm[t])] = w0;
-      V[vidx(d, 1, ny, mm[t])] = wn;
-      V[vidx(d, 1, ny + 1, mm[t])] = wn1;
-      V[vidx(d, 0, -1, mm[t])] = em1;
-      V[vidx(d, 0, 0, mm[t])] = e0;
-      V[vidx(d, 0, ny, mm[t])] = en;
-      V[vidx(d, 0, ny + 1, mm[t])] = en1;
-    }
-  }
-
-  if (is00) {  // mean flow (linsolve_blocking.inc:62-97)
-    const int m = mm[0];
-    double2 c0 = cdivr(rmul(-1.0, dot3(&cc[0], bc.eta0bc + 2)), bc.eta0bc[1]);
-    double2 tmp[4] = {c0, cc[0], cc[1], cc[2]};
-    double2 cm1 = cdivr(rmul(-1.0, dot4(tmp, bc.eta0m1bc + 1)), bc.eta0m1bc[0]);
-    double2 cn = cdivr(rmul(-1.0, dot3(&cc[3], bc.etanbc)), bc.etanbc[3]);
-    double2 tmpt[4] = {cc[3], cc[4], cc[5], cn};
-    double2 cn1 = cdivr(rmul(-1.0, dot4(tmpt, bc.etanp1bc)), bc.etanp1bc[4]);
-    V[vidx(d, 2, -1, m)] = cm1;
-    V[vidx(d, 2, 0, m)] = c0;
-    V[vidx(d, 2, ny, m)] = cn;
-    V[vidx(d, 2, ny + 1, m)] = cn1;
-    // flow rates by the non-uniform Simpson rule (dnsdata.f90:312-324)
-    double fu = 0.0, fw = 0.0, fc = 0.0;
-    for (int iy = 1, k = 0; iy <= ny - 1; iy += 2, ++k) {
-      const double a1 = yint[3 * k], a2 = yint[3 * k + 1], a3 = yint[3 * k + 2];
-      const double2 e0 = V[vidx(d, 0, iy - 1, m)], e1 = V[vidx(d, 0, iy, m)], e2 = V[vidx(d, 0, iy + 1, m)];
-      const double2 u0 = V[vidx(d, 2, iy - 1, m)], u1 = V[vidx(d, 2, iy, m)], u2 = V[vidx(d, 2, iy + 1, m)];
-      fu = fu + a1 * e0.x + a2 * e1.x + a3 * e2.x;
-      fw = fw + a1 * e0.y + a2 * e1.y + a3 * e2.y;
-      fc = fc + a1 * u0.x + a2 * u1.x + a3 * u2.x;
-    }
-    double corrpx = sc->corrpx, corrpz = sc->corrpz;
-    const bool cx = fabs(d.meanflowx) > 1.0e-7 && !d.cpi;
-    const bool cz_ = fabs(d.meanflowz) > 1.0e-7 && !d.cpi;
-    if (cx) corrpx = (d.meanflowx - fu) / fc;
-    if (cz_) corrpz = (d.meanflowz - fw) / fc;
-    for (int iy = -1; iy <= ny + 1; ++iy) {
-      const double2 et = V[vidx(d, 0, iy, m)];
-      const double uc = V[vidx(d, 2, iy, m)].x;
-      double U = et.x, W = et.y;
-      if (cx) U = U + corrpx * uc;
-      if (cz_) W = W + corrpz * uc;
-      V[vidx(d, 0, iy, m)] = make_double2(U, 0.0);
-      V[vidx(d, 2, iy, m)] = make_double2(W, 0.0);
-    }
-    sc->fr[0] = fu; sc->fr[1] = fw; sc->fr[2] = fc;
-    sc->corrpx = corrpx; sc->corrpz = corrpz;
-    if (d.cpi) {
-      if (d.cpi_type == 0) sc->meanpx = (1 - d.gamma) * 6 * ni / fu;
-      else sc->meanpx = (1.5 / d.gamma) * fu * ni;
-    }
-    return;
-  }
-
-  // ---- pass C: bottom-up COMPLEXderiv + Step1(D0mat) into the w slot ----
-  double2 f0w[2], fm1w[2], fnw[2], fn1w[2];
-#pragma unroll
-  for (int t = 0; t < 2; ++t) {
-    if (t < nm) {
-      double2 lo[5] = {vw[t][0], vw[t][1], v[t][0], v[t][1], v[t][2]};
-      double2 hi[5] = {v[t][3], v[t][4], v[t][5], vw[t][2], vw[t][3]};
-      f0w[t] = dot5(lo, bc.d140);
-      fm1w[t] = dot5(lo, bc.d14m1);
-      fnw[t] = dot5(hi, bc.d14n);
-      fn1w[t] = dot5(hi, bc.d14np1);
-    }
-  }
-  {
-    double2 win[2][5];  // v(iy-2..iy+2) sliding downwards
+    // wall and ghost values (linsolve_blocking.inc:50-61)
 #pragma unroll
     for (int t = 0; t < 2; ++t) {
       if (t < nm) {
-        win[t][1] = V[vidx(d, 1, ny - 2, mm[t])];
-        win[t][2] = V[vidx(d, 1, ny - 1, mm[t])];
-        win[t][3] = vw[t][2];
-        win[t][4] = vw[t][3];
+        const double2 w0 = cdivr(make_double2(bval0, 0.0) - dot3(lo[t], bot + 2), bot[1]);
+        const double2 rb[4] = {w0, lo[t][0], lo[t][1], lo[t][2]};
+        const double2 wm1 = cdivr(cz() - dot4(rb, botm1 + 1), botm1[0]);
+        const double2 wn = cdivr(make_double2(bvaln, 0.0) - dot3(hi[t], top), top[3]);
+        const double2 rt[4] = {hi[t][0], hi[t][1], hi[t][2], wn};
+        const double2 wn1 = cdivr(cz() - dot4(rt, topp1), topp1[4]);
+        V[vidx(d, vc, -1, mm[t])] = wm1;
+        V[vidx(d, vc, 0, mm[t])] = w0;
+        V[vidx(d, vc, ny, mm[t])] = wn;
+        V[vidx(d, vc, ny + 1, mm[t])] = wn1;
       }
     }
-    double2 x1[2] = {cz(), cz()}, x2[2] = {cz(), cz()};
+    if (ucor) {  // mean flow (linsolve_blocking.inc:62-97)
+      const int m = mm[0];
+      const double2 c0 = cdivr(cz() - dot3(clo, bot + 2), bot[1]);
+      const double2 rb[4] = {c0, clo[0], clo[1], clo[2]};
+      const double2 cm1 = cdivr(cz() - dot4(rb, botm1 + 1), botm1[0]);
+      const double2 cn = cdivr(cz() - dot3(chi, top), top[3]);
+      const double2 rt[4] = {chi[0], chi[1], chi[2], cn};
+      const double2 cn1 = cdivr(cz() - dot4(rt, topp1), topp1[4]);
+      V[vidx(d, 2, -1, m)] = cm1;
+      V[vidx(d, 2, 0, m)] = c0;
+      V[vidx(d, 2, ny, m)] = cn;
+      V[vidx(d, 2, ny + 1, m)] = cn1;
+      // flow rates by the non-uniform Simpson rule (dnsdata.f90:312-324)
+      double fu = 0.0, fw = 0.0, fc = 0.0;
+      for (int iy = 1, k = 0; iy <= ny - 1; iy += 2, ++k) {
+        const double a1 = yint[3 * k], a2 = yint[3 * k + 1], a3 = yint[3 * k + 2];
+        const double2 e0 = V[vidx(d, 0, iy - 1, m)], e1 = V[vidx(d, 0, iy, m)], e2 = V[vidx(d, 0, iy + 1, m)];
+        const double2 u0 = V[vidx(d, 2, iy - 1, m)], u1 = V[vidx(d, 2, iy, m)], u2 = V[vidx(d, 2, iy + 1, m)];
+        fu = fu + a1 * e0.x + a2 * e1.x + a3 * e2.x;
+        fw = fw + a1 * e0.y + a2 * e1.y + a3 * e2.y;
+        fc = fc + a1 * u0.x + a2 * u1.x + a3 * u2.x;
+      }
+      double corrpx = sc->corrpx, corrpz = sc->corrpz;
+      const bool cx = fabs(d.meanflowx) > 1.0e-7 && !d.cpi;
+      const bool cz_ = fabs(d.meanflowz) > 1.0e-7 && !d.cpi;
+      if (cx) corrpx = (d.meanflowx - fu) / fc;
+      if (cz_) corrpz = (d.meanflowz - fw) / fc;
+      for (int iy = -1; iy <= ny + 1; ++iy) {
+        const double2 et = V[vidx(d, 0, iy, m)];
+        const double uc = V[vidx(d, 2, iy, m)].x;
+        double U = et.x, W = et.y;
+        if (cx) U = U + corrpx * uc;
+        if (cz_) W = W + corrpz * uc;
+        V[vidx(d, 0, iy, m)] = make_double2(U, 0.0);
+        V[vidx(d, 2, iy, m)] = make_double2(W, 0.0);
+      }
+      sc->fr[0] = fu; sc->fr[1] = fw; sc->fr[2] = fc;
+      sc->corrpx = corrpx; sc->corrpz = corrpz;
+      if (d.cpi) {
+        if (d.cpi_type == 0) sc->meanpx = (1 - d.gamma) * 6 * ni / fu;
+        else sc->meanpx = (1.5 / d.gamma) * fu * ni;
+      }
+    }
+  }
+  __syncthreads();  // v and eta of this block's pairs are in V
+  if (!active || is00 || role >= nm) return;
+
+  // ---- one mode per thread: COMPLEXderiv + Step1(D0mat) bottom-up, then
+  //      Step2(D0mat) and u, w top-down (dnsdata.f90:339-373, linsolve_blocking.inc:99-103) ----
+  const int m = mm[role];
+  const double kz = (role == 0 ? 1.0 : -1.0) * kb;
+  const double rk2 = 1.0 / k2;
+  const double au = ka * rk2, bu = kz * rk2;
+  double2 vlo[5], vhi[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    vlo[j] = V[vidx(d, 1, -1 + j, m)];
+    vhi[j] = V[vidx(d, 1, ny - 3 + j, m)];
+  }
+  const double2 f0 = dot5(vlo, bc.d140), fm1 = dot5(vlo, bc.d14m1);
+  const double2 fn = dot5(vhi, bc.d14n), fn1 = dot5(vhi, bc.d14np1);
+  {
+    double2 win[5];  // v(iy-2..iy+2) sliding downwards
+    win[1] = vhi[1];
+    win[2] = vhi[2];
+    win[3] = vhi[3];
+    win[4] = vhi[4];
+    double2 x1 = cz(), x2 = cz();
     for (int iy = ny - 1; iy >= 1; --iy) {
       const double* dr = der + (size_t)iy * 20;
-      double c1[5];
+      win[0] = V[vidx(d, 1, iy - 2, m)];
+      double2 f = rmul(__ldg(dr + 5), win[0]);
 #pragma unroll
-      for (int j = 0; j < 5; ++j) c1[j] = __ldg(dr + 5 + j);
+      for (int j = 1; j < 5; ++j) f = f + rmul(__ldg(dr + 5 + j), win[j]);
+      if (iy == ny - 1) f = f - (rmul(__ldg(dr + 3), fn) + rmul(__ldg(dr + 4), fn1));
+      if (iy == ny - 2) f = f - rmul(__ldg(dr + 4), fn);
+      if (iy == 1) f = f - (rmul(__ldg(dr + 1), f0) + rmul(__ldg(dr + 0), fm1));
+      if (iy == 2) f = f - rmul(__ldg(dr + 0), f0);
       double A[5];
 #pragma unroll
       for (int j = 0; j < 5; ++j) A[j] = __ldg(d0lu + (size_t)(iy - 1) * 5 + j);
+      const double2 x = step1(f, A, x1, x2);
+      x2 = x1;
+      x1 = x;
+      V[vidx(d, 2, iy, m)] = x;
 #pragma unroll
-      for (int t = 0; t < 2; ++t) {
-        if (t < nm) {
-          win[t][0] = (iy - 2 >= 1) ? V[vidx(d, 1, iy - 2, mm[t])] : (iy - 2 == 0 ? vw[t][1] : vw[t][0]);
-          double2 f = dot5(win[t], c1);
-          if (iy == ny - 1) f = f - (rmul(__ldg(dr + 3), fnw[t]) + rmul(__ldg(dr + 4), fn1w[t]));
-          if (iy == ny - 2) f = f - rmul(__ldg(dr + 4), fnw[t]);
-          if (iy == 1) f = f - (rmul(__ldg(dr + 1), f0w[t]) + rmul(__ldg(dr + 0), fm1w[t]));
-          if (iy == 2) f = f - rmul(__ldg(dr + 0), f0w[t]);
-          const double2 x = step1(f, A, x1[t], x2[t]);
-          x2[t] = x1[t]; x1[t] = x;
-          V[vidx(d, 2, iy, mm[t])] = x;
-#pragma unroll
-          for (int j = 4; j > 0; --j) win[t][j] = win[t][j - 1];
-        }
-      }
+      for (int j = 4; j > 0; --j) win[j] = win[j - 1];
     }
   }
-  // ---- pass D: top-down Step2(D0mat) and u, w recovery ----
   {
-    double2 bm2[2], bm1[2];
+    double2 bm2 = cz(), bm1 = fm1;
     for (int iy = -1; iy <= ny + 1; ++iy) {
-      double l2 = 0, l1 = 0;
-      if (iy >= 1 && iy <= ny - 1) {
-        l2 = __ldg(d0lu + (size_t)(iy - 1) * 5 + 0);
-        l1 = __ldg(d0lu + (size_t)(iy - 1) * 5 + 1);
+      double2 vp;
+      if (iy == -1) vp = fm1;
+      else if (iy == 0) vp = f0;
+      else if (iy == ny) vp = fn;
+      else if (iy == ny + 1) vp = fn1;
+      else {
+        vp = step2(V[vidx(d, 2, iy, m)], __ldg(d0lu + (size_t)(iy - 1) * 5 + 0), __ldg(d0lu + (size_t)(iy - 1) * 5 + 1),
+                   bm2, bm1);
       }
-#pragma unroll
-      for (int t = 0; t < 2; ++t) {
-        if (t < nm) {
-          double2 vp;
-          if (iy == -1) vp = fm1w[t];
-          else if (iy == 0) vp = f0w[t];
-          else if (iy == ny) vp = fnw[t];
-          else if (iy == ny + 1) vp = fn1w[t];
-          else vp = step2(V[vidx(d, 2, iy, mm[t])], l2, l1, bm2[t], bm1[t]);
-          if (iy <= ny - 1) { bm2[t] = (iy == -1) ? cz() : bm1[t]; bm1[t] = vp; }
-          if (iy == -1) { bm2[t] = cz(); bm1[t] = vp; }
-          const double bz = (t == 0 ? 1.0 : -1.0) * kb;
-          const double2 et = V[vidx(d, 0, iy, mm[t])];
-          const double2 u = rmul(rk2, mul_ia<double2>(ka, vp) - mul_ia<double2>(bz, et));
-          const double2 w = rmul(rk2, mul_ia<double2>(bz, vp) + mul_ia<double2>(ka, et));
-          V[vidx(d, 0, iy, mm[t])] = u;
-          V[vidx(d, 2, iy, mm[t])] = w;
-        }
+      if (iy >= 0 && iy <= ny - 1) {
+        bm2 = bm1;
+        bm1 = vp;
       }
+      const double2 et = V[vidx(d, 0, iy, m)];
+      // u = (i kx v' - i kz eta)/k2, w = (i kz v' + i kx eta)/k2
+      V[vidx(d, 0, iy, m)] = make_double2(bu * et.y - au * vp.y, au * vp.x - bu * et.x);
+      V[vidx(d, 2, iy, m)] = make_double2(-(bu * vp.y) - au * et.y, bu * vp.x + au * et.x);
     }
   }
 }
 
 void launch_linsolve(const SolveLaunch& L, cudaStream_t s) {
-  dim3 grid((L.d.npairs + 63) / 64);
+  dim3 grid((L.d.npairs + 31) / 32);
   k_linsolve<<<grid, 64, 0, s>>>(L.V, L.rhs_src, L.rhs_cstride, L.rhs_plane_off, L.fac, L.der, L.d0lu, L.yint, L.bc, L.d, L.lambda, L.ode[0],
                                   L.lambda_from_dt, L.sc);
 }
