@@ -42,7 +42,7 @@ struct chgpu_handle {
   BcRows bc{};
   Tables tab;
   RadixDev rz{}, rx{};
-  int mixed = 0;
+  int prec = CHGPU_FP64;  // CHGPU_FP64, CHGPU_MIXED or CHGPU_FP64DD
   int zcols = 1, xrows = 1;
   cudaStream_t stream = nullptr;
   // device buffers
@@ -54,6 +54,7 @@ struct chgpu_handle {
   double2* rhs = nullptr;
   double* fac = nullptr;
   double* der = nullptr;
+  void* derT = nullptr;
   double* d0lu = nullptr;
   double* yint = nullptr;
   double* dy = nullptr;
@@ -93,17 +94,39 @@ int cuda_fail(chgpu_handle* h, cudaError_t e, const char* where) {
     if (e_ != cudaSuccess) return cuda_fail((h), e_, #call); \
   } while (0)
 
-size_t tsize(const chgpu_handle* h) { return h->mixed ? sizeof(float2) : sizeof(double2); }
+// element size of the transform buffers and spectra (and of the RK history)
+size_t tsize(const chgpu_handle* h) { return h->prec == CHGPU_MIXED ? sizeof(float2) : sizeof(double2); }
+
+// value of a long double in each arithmetic type (double-float: split in extended precision)
+template <typename T> T from_ld(long double v) { return (T)v; }
+template <> dd from_ld<dd>(long double v) {
+  const float hi = (float)v;
+  return dd(hi, (float)(v - (long double)hi));
+}
 
 template <typename V2>
 std::vector<V2> roots(int n) {  // forward roots exp(-2 pi i m/n), from the mathematics in extended precision
+  using T = decltype(V2::x);
   std::vector<V2> w(n);
   for (int m = 0; m < n; ++m) {
     long double ang = 2.0L * 3.14159265358979323846264338327950288L * (long double)m / (long double)n;
-    w[m].x = (decltype(w[m].x))cosl(ang);
-    w[m].y = (decltype(w[m].x))(-sinl(ang));
+    w[m].x = from_ld<T>(cosl(ang));
+    w[m].y = from_ld<T>(-sinl(ang));
   }
   return w;
+}
+
+// der and the wavenumber units in the nonlinear-term type: [(ny+1)*20] then alfa0, beta0
+template <typename T>
+int upload_derT(chgpu_handle* h) {
+  const std::vector<double>& der = h->tab.der;
+  std::vector<T> t(der.size() + 2);
+  for (size_t i = 0; i < der.size(); ++i) t[i] = from_ld<T>((long double)der[i]);
+  t[der.size()] = from_ld<T>((long double)h->p.alfa0);
+  t[der.size() + 1] = from_ld<T>((long double)h->p.beta0);
+  CK(h, cudaMalloc(&h->derT, sizeof(T) * t.size()));
+  CK(h, cudaMemcpy(h->derT, t.data(), sizeof(T) * t.size(), cudaMemcpyHostToDevice));
+  return 0;
 }
 
 template <typename V2>
@@ -172,6 +195,7 @@ SolveLaunch solve_launch(chgpu_handle* h, const double* ode) {
   L.rhs = h->rhs;
   L.fac = h->fac;
   L.der = h->der;
+  L.derT = h->derT;
   L.d0lu = h->d0lu;
   L.yint = h->yint;
   L.sc = h->sc;
@@ -188,7 +212,8 @@ void run_convolutions(chgpu_handle* h, int compute_cfl, int products, int plane0
   const int nst = products ? 3 : 2;
   for (int stage = 0; stage < nst; ++stage)
     timed(h, stage, [&] {
-      if (h->mixed) launch_convolutions<float>(L, h->stream, stage);
+      if (h->prec == CHGPU_MIXED) launch_convolutions<float>(L, h->stream, stage);
+      else if (h->prec == CHGPU_FP64DD) launch_convolutions<dd>(L, h->stream, stage);
       else launch_convolutions<double>(L, h->stream, stage);
     });
   h->launches += nst;
@@ -197,7 +222,8 @@ void run_convolutions(chgpu_handle* h, int compute_cfl, int products, int plane0
 void run_rhs(chgpu_handle* h, const double* ode) {
   SolveLaunch L = solve_launch(h, ode);
   timed(h, 3, [&] {
-    if (h->mixed) launch_rhs<float>(L, h->stream);
+    if (h->prec == CHGPU_MIXED) launch_rhs<float>(L, h->stream);
+    else if (h->prec == CHGPU_FP64DD) launch_rhs<dd>(L, h->stream);
     else launch_rhs<double>(L, h->stream);
   });
   h->launches += 1;
@@ -269,7 +295,7 @@ void release(chgpu_handle* h) {
     cudaEventDestroy(pe.second.second);
   }
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
-  void* bufs[] = {h->V, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->d0lu, h->yint, h->dy,
+  void* bufs[] = {h->V, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->derT, h->d0lu, h->yint, h->dy,
                   h->twz, h->twx, h->twh, h->sc};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -290,14 +316,14 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
     return fail(nullptr, CHGPU_E_PARAM, "chgpu_create: need nx>=1, nz>=1, ny>=8");
   if (!(p->ymax > p->ymin) || !(p->a > 0) || !(p->alfa0 > 0) || !(p->beta0 > 0) || !(p->ni > 0))
     return fail(nullptr, CHGPU_E_PARAM, "chgpu_create: need ymax>ymin, a>0, alfa0>0, beta0>0, ni>0");
-  if (p->precision != CHGPU_FP64 && p->precision != CHGPU_MIXED)
-    return fail(nullptr, CHGPU_E_PARAM, "chgpu_create: precision must be CHGPU_FP64 or CHGPU_MIXED");
+  if (p->precision != CHGPU_FP64 && p->precision != CHGPU_MIXED && p->precision != CHGPU_FP64DD)
+    return fail(nullptr, CHGPU_E_PARAM, "chgpu_create: precision must be CHGPU_FP64, CHGPU_MIXED or CHGPU_FP64DD");
   if (p->cpi && p->cpi_type != 0 && p->cpi_type != 1)
     return fail(nullptr, CHGPU_E_PARAM, "Wrong selection of CPI_Type");  // linsolve_blocking.inc:93-95
   chgpu_handle* h = new (std::nothrow) chgpu_handle();
   if (!h) return fail(nullptr, CHGPU_E_NOMEM, "chgpu_create: host allocation failed");
   h->p = *p;
-  h->mixed = p->precision == CHGPU_MIXED;
+  h->prec = p->precision;
   int nxd, nzd;
   padded_sizes(p->nx, p->nz, &nxd, &nzd);
   Dims& d = h->d;
@@ -366,14 +392,21 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
     if ((rc = dev_alloc((void**)&h->sc, sizeof(DevScalars), "scalars"))) break;
     e = cudaMallocHost((void**)&h->sc_host, sizeof(DevScalars));
     if (e != cudaSuccess) { rc = cuda_fail(h, e, "cudaMallocHost"); break; }
-    if (h->mixed) {
+    if (h->prec == CHGPU_MIXED) {
       if ((rc = upload_roots<float2>(h, &h->twz, nzd))) break;
       if ((rc = upload_roots<float2>(h, &h->twx, nxd))) break;
       if ((rc = upload_roots<float2>(h, &h->twh, 2 * nxd))) break;
+      if ((rc = upload_derT<float>(h))) break;
+    } else if (h->prec == CHGPU_FP64DD) {
+      if ((rc = upload_roots<cdd>(h, &h->twz, nzd))) break;
+      if ((rc = upload_roots<cdd>(h, &h->twx, nxd))) break;
+      if ((rc = upload_roots<cdd>(h, &h->twh, 2 * nxd))) break;
+      if ((rc = upload_derT<dd>(h))) break;
     } else {
       if ((rc = upload_roots<double2>(h, &h->twz, nzd))) break;
       if ((rc = upload_roots<double2>(h, &h->twx, nxd))) break;
       if ((rc = upload_roots<double2>(h, &h->twh, 2 * nxd))) break;
+      if ((rc = upload_derT<double>(h))) break;
     }
     cudaMemcpy(h->der, t.der.data(), sizeof(double) * t.der.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(h->d0lu, t.d0lu.data(), sizeof(double) * t.d0lu.size(), cudaMemcpyHostToDevice);

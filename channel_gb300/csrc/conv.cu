@@ -42,13 +42,13 @@ __global__ void __launch_bounds__(256) k_zinv(const double2* __restrict__ V, typ
   for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) {
     const int b = idx / nzd;
     const int jz = idx - b * nzd;
-    V2 val = mk<V2>((T)0, (T)0);
+    V2 val = czero<V2>();
     int izp = -1;
     if (jz <= nz) izp = nz + jz;
     else if (jz >= nzd - nz) izp = jz - nzd + nz;
     if (izp >= 0) {
       double2 x = V[(colbase + ix0 + b) * d.nzt + izp];
-      val = mk<V2>((T)x.x, (T)x.y);
+      val = mk<V2>(Num<T>::from_double(x.x), Num<T>::from_double(x.y));
     }
     bufA[idx] = val;
   }
@@ -61,9 +61,8 @@ __global__ void __launch_bounds__(256) k_zinv(const double2* __restrict__ V, typ
   }
 }
 
-template <typename T>
-__device__ __forceinline__ void block_max_atomic(T v, double* target) {
-  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+__device__ __forceinline__ void block_max_atomic(double v, double* target) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
   __shared__ double wmax[32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0) wmax[wid] = (double)v;
@@ -97,7 +96,7 @@ __global__ void __launch_bounds__(256) k_xrow(const typename C2<T>::t* __restric
     const int ck = idx / nrows;
     const int k = ck % M;
     const int c = ck / M;
-    V2 val = mk<V2>((T)0, (T)0);
+    V2 val = czero<V2>();
     if (k <= nx) val = Zb[(((size_t)c * d.nplanes + plane) * nxp + k) * nzd + jz0 + r];
     Cb[((size_t)c * nrows + r) * M + k] = val;
   }
@@ -108,8 +107,8 @@ __global__ void __launch_bounds__(256) k_xrow(const typename C2<T>::t* __restric
     const int cr = idx / M;
     const V2* X = Cb + (size_t)cr * M;
     V2 xk = X[k];
-    V2 xm = mk<V2>((T)0, (T)0);
-    if (k == 0) xk.y = (T)0;  // the c2r reads only Re of the kx=0 entry
+    V2 xm = czero<V2>();
+    if (k == 0) xk.y = T();  // the c2r reads only Re of the kx=0 entry
     else xm = conjg(X[M - k]);
     V2 e = xk + xm, o = cmul(xk - xm, conjg(twh[k]));
     A[idx] = e + mul_i(o, +1);
@@ -118,29 +117,30 @@ __global__ void __launch_bounds__(256) k_xrow(const typename C2<T>::t* __restric
   V2* U = fft_block<V2>(A, B, 3 * nrows, rx, +1, twx);
   V2* freeb = (U == A) ? B : A;
   // CFL (dnsdata.f90:552-556) and products uu,vv,ww (:584)
-  const T f = (T)d.factor;
-  T cfl = (T)0;
+  const T f = Num<T>::from_double(d.factor);
+  T cfl = T();
   bool bad = false;
   const bool do_cfl = compute_cfl && plane >= 2 && plane <= d.ny;
-  const T rdx = (T)d.rdx, rdz = (T)d.rdz;
-  const T rdy = do_cfl ? (T)(1.0 / dy[plane - 1]) : (T)0;
+  const T rdx = Num<T>::from_double(d.rdx), rdz = Num<T>::from_double(d.rdz);
+  const T rdy = do_cfl ? Num<T>::from_double(1.0 / dy[plane - 1]) : T();
   for (int idx = threadIdx.x; idx < nrows * M; idx += blockDim.x) {
     const int m = idx % M, r = idx / M;
     V2 u = U[((size_t)0 * nrows + r) * M + m];
     V2 v = U[((size_t)1 * nrows + r) * M + m];
     V2 w = U[((size_t)2 * nrows + r) * M + m];
     if (do_cfl) {
-      T c0 = fabs(u.x) * rdx + fabs(v.x) * rdy + fabs(w.x) * rdz;
-      T c1 = fabs(u.y) * rdx + fabs(v.y) * rdy + fabs(w.y) * rdz;
-      cfl = max(cfl, max(c0, c1));
-      bad = bad || !isfinite(c0) || !isfinite(c1);
+      using N = Num<T>;
+      T c0 = N::abs(u.x) * rdx + N::abs(v.x) * rdy + N::abs(w.x) * rdz;
+      T c1 = N::abs(u.y) * rdx + N::abs(v.y) * rdy + N::abs(w.y) * rdz;
+      cfl = N::max(cfl, N::max(c0, c1));
+      bad = bad || !N::finite(c0) || !N::finite(c1);
     }
     Cb[((size_t)0 * nrows + r) * M + m] = mk<V2>(u.x * u.x * f, u.y * u.y * f);
     Cb[((size_t)1 * nrows + r) * M + m] = mk<V2>(v.x * v.x * f, v.y * v.y * f);
     Cb[((size_t)2 * nrows + r) * M + m] = mk<V2>(w.x * w.x * f, w.y * w.y * f);
   }
-  if (bad) cfl = (T)INFINITY;  // a non-finite velocity shows up as an infinite CFL
-  if (compute_cfl) block_max_atomic<T>(cfl, &sc->cfl);
+  if (bad) cfl = T((float)INFINITY);  // a non-finite velocity shows up as an infinite CFL
+  if (compute_cfl) block_max_atomic(Num<T>::to_double(cfl), &sc->cfl);
   __syncthreads();
   for (int half = 0; half < 2; ++half) {
     if (half == 1) {  // products uv, vw, uw (dnsdata.f90:581-583)
@@ -165,9 +165,9 @@ __global__ void __launch_bounds__(256) k_xrow(const typename C2<T>::t* __restric
       const V2* Z = P + ((size_t)p * nrows + r) * M;
       V2 zk = Z[k];
       V2 zm = conjg(Z[k == 0 ? 0 : M - k]);
-      V2 e = scale(zk + zm, (T)0.5);
-      V2 dd = zk - zm;
-      V2 o = mk<V2>(dd.y * (T)0.5, -dd.x * (T)0.5);
+      V2 e = scale(zk + zm, T(0.5f));
+      V2 df = zk - zm;
+      V2 o = mk<V2>(df.y * T(0.5f), -df.x * T(0.5f));
       V2 X = e + cmul(twh[k], o);
       Pb[(((size_t)(3 * half + p) * d.nplanes + plane) * nxp + k) * nzd + jz0 + r] = X;
     }
@@ -231,6 +231,7 @@ void launch_convolutions(const ConvLaunch& L, cudaStream_t s, int stage) {
 
 template void launch_convolutions<double>(const ConvLaunch&, cudaStream_t, int);
 template void launch_convolutions<float>(const ConvLaunch&, cudaStream_t, int);
+template void launch_convolutions<dd>(const ConvLaunch&, cudaStream_t, int);
 
 namespace {
 template <typename K>
@@ -253,7 +254,10 @@ cudaError_t conv_set_smem_limits() {
   if ((e = allow_max_smem(k_xrow<double>, optin))) return e;
   if ((e = allow_max_smem(k_xrow<float>, optin))) return e;
   if ((e = allow_max_smem(k_zfwd<double>, optin))) return e;
-  return allow_max_smem(k_zfwd<float>, optin);
+  if ((e = allow_max_smem(k_zfwd<float>, optin))) return e;
+  if ((e = allow_max_smem(k_zinv<dd>, optin))) return e;
+  if ((e = allow_max_smem(k_xrow<dd>, optin))) return e;
+  return allow_max_smem(k_zfwd<dd>, optin);
 }
 
 }  // namespace chgpu

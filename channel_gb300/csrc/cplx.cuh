@@ -4,11 +4,14 @@
 
 #include <cuda_runtime.h>
 
+#include "dd.cuh"
+
 namespace chgpu {
 
 template <typename T> struct C2;
 template <> struct C2<double> { using t = double2; };
 template <> struct C2<float> { using t = float2; };
+template <> struct C2<dd> { using t = cdd; };
 
 template <typename V> __device__ __forceinline__ V mk(decltype(V::x) a, decltype(V::x) b) { V r; r.x = a; r.y = b; return r; }
 __device__ __forceinline__ double2 operator+(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
@@ -19,6 +22,7 @@ template <typename V> __device__ __forceinline__ V cmul(V a, V b) {
   return mk<V>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 template <typename V> __device__ __forceinline__ V conjg(V a) { return mk<V>(a.x, -a.y); }
+template <typename V> __device__ __forceinline__ V czero() { return mk<V>(decltype(V::x)(), decltype(V::x)()); }
 template <typename V> __device__ __forceinline__ V scale(V a, decltype(V::x) s) { return mk<V>(a.x * s, a.y * s); }
 // a * (sign * i)
 template <typename V> __device__ __forceinline__ V mul_i(V a, int sign) {
@@ -41,7 +45,7 @@ __device__ V* fft_block(V* a, V* b, int B, const RadixDev& rad, int sign, const 
   using T = decltype(V::x);
   const int n = rad.n;
   int Ns = 1;
-  const T h3 = (T)0.86602540378443864676372317075294;  // sqrt(3)/2
+  const T h3 = Num<T>::sqrt3_2();
   for (int st = 0; st < rad.nst; ++st) {
     const int R = rad.r[st];
     const int nb = n / R;
@@ -83,7 +87,7 @@ __device__ V* fft_block(V* a, V* b, int B, const RadixDev& rad, int sign, const 
         dst[idxD + 3 * Ns] = t1 - t3;
       } else {
         V t1 = v1 + v2;
-        V t2 = v0 - scale(t1, (T)0.5);
+        V t2 = v0 - scale(t1, T(0.5f));
         V t3 = mul_i(scale(v1 - v2, h3), sign);
         dst[idxD] = v0 + t1;
         dst[idxD + Ns] = t2 + t3;

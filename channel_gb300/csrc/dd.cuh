@@ -19,8 +19,9 @@ struct dd {
   float hi, lo;
   __host__ __device__ constexpr dd() : hi(0.f), lo(0.f) {}
   __host__ __device__ constexpr dd(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ constexpr explicit dd(float h) : hi(h), lo(0.f) {}
   // split of a double: exact when the double's exponent fits FP32's range
-  __host__ __device__ dd(double v) : hi((float)v), lo((float)(v - (double)(float)v)) {}
+  __host__ __device__ explicit dd(double v) : hi((float)v), lo((float)(v - (double)(float)v)) {}
   __host__ __device__ explicit operator double() const { return (double)hi + (double)lo; }
 };
 
@@ -55,13 +56,70 @@ __device__ __forceinline__ dd operator*(dd a, dd b) {
 __device__ __forceinline__ bool operator<(dd a, dd b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 __device__ __forceinline__ bool operator>(dd a, dd b) { return b < a; }
 __device__ __forceinline__ bool operator==(dd a, dd b) { return a.hi == b.hi && a.lo == b.lo; }
-__device__ __forceinline__ dd fabs(dd a) { return a.hi < 0.f ? -a : a; }
-__device__ __forceinline__ dd max(dd a, dd b) { return (a < b) ? b : a; }
-__device__ __forceinline__ bool isfinite(dd a) { return ::isfinite(a.hi) && ::isfinite(a.lo); }
+__device__ __forceinline__ dd dd_abs(dd a) { return a.hi < 0.f ? -a : a; }
+__device__ __forceinline__ dd dd_max(dd a, dd b) { return (a < b) ? b : a; }
+__device__ __forceinline__ bool dd_isfinite(dd a) { return isfinite(a.hi) && isfinite(a.lo); }
 
 // complex double-float: 16 bytes, like double2
 struct __align__(16) cdd {
   dd x, y;
+};
+__device__ __forceinline__ cdd operator+(cdd a, cdd b) { return cdd{a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ cdd operator-(cdd a, cdd b) { return cdd{a.x - b.x, a.y - b.y}; }
+
+// FP64 -> double-float with integer operations only: conversions between
+// FP64 and FP32 run at the FP64 rate on GB300 (measured ~580 G/s against
+// 38.9 T FFMA/s), which would cost as much as the transform itself.  hi takes
+// the sign, exponent and top 23 fraction bits (truncated); lo is the
+// remaining 29 fraction bits rounded to 24 and scaled by 2^(e-1075); then the
+// pair is renormalised.  |v| below 2^-126 is flushed to zero (absolute error
+// under 1.2e-38); Inf and NaN stay Inf and NaN.
+__device__ __forceinline__ dd dd_from_double(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7ff);
+  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+  if (e == 0x7ff) return dd(m ? __int_as_float(0x7fc00000) : __uint_as_float(sign | 0x7f800000u), 0.f);
+  const int ef = e - 1023 + 127;
+  if (ef < 1) return dd(__uint_as_float(sign), 0.f);
+  if (ef > 254) return dd(__uint_as_float(sign | 0x7f800000u), 0.f);
+  const float hi = __uint_as_float(sign | ((unsigned)ef << 23) | (unsigned)(m >> 29));
+  const unsigned r = (unsigned)(m & 0x1FFFFFFFull);
+  float lo = 0.f;
+  if (r) {
+    const unsigned fb = __float_as_uint(__uint2float_rn(r));  // exact to 24 bits, exponent field <= 127+28
+    const int elo = (int)((fb >> 23) & 0xff) + (e - 1075);
+    if (elo >= 1) lo = __uint_as_float(sign | ((unsigned)elo << 23) | (fb & 0x7fffffu));
+  }
+  return fast_two_sum(hi, lo);
+}
+__device__ __forceinline__ double dd_to_double(dd a) { return (double)a.hi + (double)a.lo; }
+
+// Conversions and constants per arithmetic type T (double, float, dd).
+template <typename T> struct Num;
+template <> struct Num<double> {
+  __device__ static double from_double(double v) { return v; }
+  __device__ static double to_double(double v) { return v; }
+  __device__ static double abs(double v) { return fabs(v); }
+  __device__ static double max(double a, double b) { return fmax(a, b); }
+  __device__ static bool finite(double v) { return isfinite(v); }
+  __device__ static constexpr double sqrt3_2() { return 0.86602540378443864676372317075294; }
+};
+template <> struct Num<float> {
+  __device__ static float from_double(double v) { return (float)v; }
+  __device__ static double to_double(float v) { return (double)v; }
+  __device__ static float abs(float v) { return fabsf(v); }
+  __device__ static float max(float a, float b) { return fmaxf(a, b); }
+  __device__ static bool finite(float v) { return isfinite(v); }
+  __device__ static constexpr float sqrt3_2() { return 0.866025404f; }
+};
+template <> struct Num<dd> {
+  __device__ static dd from_double(double v) { return dd_from_double(v); }
+  __device__ static double to_double(dd v) { return dd_to_double(v); }
+  __device__ static dd abs(dd v) { return dd_abs(v); }
+  __device__ static dd max(dd a, dd b) { return dd_max(a, b); }
+  __device__ static bool finite(dd v) { return dd_isfinite(v); }
+  __device__ static constexpr dd sqrt3_2() { return dd(0.866025388f, 1.55436251e-08f); }
 };
 
 }  // namespace chgpu

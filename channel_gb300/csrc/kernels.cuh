@@ -61,6 +61,7 @@ struct SolveLaunch {
   int rhs_plane_off;       // row iy lives at plane iy+rhs_plane_off
   double* fac;
   const double* der;
+  const void* derT;  // der in the nonlinear-term type, then alfa0, beta0
   const double* d0lu;
   const double* yint;
   DevScalars* sc;

@@ -44,49 +44,70 @@ __device__ __forceinline__ size_t vidx(const Dims& d, int c, int iy, int m) {
 // ---------------------------------------------------------------------------
 // buildrhs rows
 // ---------------------------------------------------------------------------
+// History entry from the explicit term in T (x) and the same term in FP64 (e).
+template <typename O2, typename V2> __device__ __forceinline__ O2 hist_store(V2 x, double2 e) { return x; }
+template <> __device__ __forceinline__ double2 hist_store<double2, cdd>(cdd, double2 e) { return e; }
+
+// Storage type of the RK history (the explicit term of the previous
+// substep): FP32 in the mixed path, FP64 otherwise.
+template <typename T> struct HistT { using t = typename C2<T>::t; };
+template <> struct HistT<dd> { using t = double2; };
+
 template <typename T>
 __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, const typename C2<T>::t* __restrict__ VV,
-                                             typename C2<T>::t* __restrict__ old, double2* __restrict__ rhs,
-                                             const double* __restrict__ der, Dims d, double ode1, double ode2,
-                                             double ode3, const DevScalars* __restrict__ sc) {
+                                             typename HistT<T>::t* __restrict__ old, double2* __restrict__ rhs,
+                                             const double* __restrict__ der, const T* __restrict__ derT, Dims d,
+                                             double ode1, double ode2, double ode3,
+                                             const DevScalars* __restrict__ sc) {
   using V2 = typename C2<T>::t;
+  using O2 = typename HistT<T>::t;
+  using OT = decltype(O2::x);
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   const int iy = blockIdx.y + 1;
   if (m >= d.nmodes) return;
   const int ix = m / d.nzt;
   const int iz = m - ix * d.nzt - d.nz;
-  const double* dr = der + (size_t)iy * 20;
-  double c0[5], c1[5], c2[5], c4[5];
+  // wavenumbers and stencil coefficients in T (derT holds der in T, then alfa0, beta0)
+  const T* drT = derT + (size_t)iy * 20;
+  const size_t tail = (size_t)(d.ny + 1) * 20;
+  const T ta = T((float)ix) * derT[tail], tb = T((float)iz) * derT[tail + 1];
+  T e0[5], e1[5], e2[5];
 #pragma unroll
   for (int j = 0; j < 5; ++j) {
-    c0[j] = __ldg(dr + j);
-    c1[j] = __ldg(dr + 5 + j);
-    c2[j] = __ldg(dr + 10 + j);
-    c4[j] = __ldg(dr + 15 + j);
+    e0[j] = drT[j];
+    e1[j] = drT[5 + j];
+    e2[j] = drT[10 + j];
   }
-  const T ta = (T)(ix * d.alfa0), tb = (T)(iz * d.beta0);
   // DD(f,k) (dnsdata.f90:609-610) on product k (0-based) at rows iy-2..iy+2
   V2 vv[6][5];
 #pragma unroll
   for (int k = 0; k < 6; ++k)
 #pragma unroll
     for (int j = 0; j < 5; ++j) vv[k][j] = VV[((size_t)k * d.nplanes + (iy - 1 + j)) * d.nmodes + m];
-  auto DD = [&](const double* c, int k) -> V2 {
-    V2 s = mk<V2>((T)c[0] * vv[k][0].x, (T)c[0] * vv[k][0].y);
+  auto DD = [&](const T* c, int k) -> V2 {
+    V2 s = mk<V2>(c[0] * vv[k][0].x, c[0] * vv[k][0].y);
 #pragma unroll
-    for (int j = 1; j < 5; ++j) s = s + mk<V2>((T)c[j] * vv[k][j].x, (T)c[j] * vv[k][j].y);
+    for (int j = 1; j < 5; ++j) s = s + mk<V2>(c[j] * vv[k][j].x, c[j] * vv[k][j].y);
     return s;
   };
-  const V2 DD0_6 = DD(c0, 5), DD1_6 = DD(c1, 5);
-  const V2 rhsu = mk<V2>((T)0, (T)0) - mul_ia<V2>(ta, DD(c0, 0)) - DD(c1, 3) - mul_ia<V2>(tb, DD0_6);
-  const V2 rhsv = mk<V2>((T)0, (T)0) - mul_ia<V2>(ta, DD(c0, 3)) - DD(c1, 1) - mul_ia<V2>(tb, DD(c0, 4));
-  const V2 rhsw = mk<V2>((T)0, (T)0) - mul_ia<V2>(ta, DD0_6) - DD(c1, 4) - mul_ia<V2>(tb, DD(c0, 2));
+  const V2 DD0_6 = DD(e0, 5), DD1_6 = DD(e1, 5);
+  const V2 rhsu = czero<V2>() - mul_ia<V2>(ta, DD(e0, 0)) - DD(e1, 3) - mul_ia<V2>(tb, DD0_6);
+  const V2 rhsv = czero<V2>() - mul_ia<V2>(ta, DD(e0, 3)) - DD(e1, 1) - mul_ia<V2>(tb, DD(e0, 4));
+  const V2 rhsw = czero<V2>() - mul_ia<V2>(ta, DD0_6) - DD(e1, 4) - mul_ia<V2>(tb, DD(e0, 2));
+  const T tk2 = ta * ta + tb * tb;
+  V2 explv = mul_ia<V2>(ta, mul_ia<V2>(ta, DD(e1, 0)) + DD(e2, 3) + mul_ia<V2>(tb, DD1_6)) +
+             mul_ia<V2>(tb, mul_ia<V2>(ta, DD1_6) + DD(e2, 4) + mul_ia<V2>(tb, DD(e1, 2)));
+  explv = explv - mk<V2>(tk2 * rhsv.x, tk2 * rhsv.y);
   const double a = ix * d.alfa0, b = iz * d.beta0;
   const double k2 = a * a + b * b;
-  const T tk2 = (T)k2;
-  V2 explv = mul_ia<V2>(ta, mul_ia<V2>(ta, DD(c1, 0)) + DD(c2, 3) + mul_ia<V2>(tb, DD1_6)) +
-             mul_ia<V2>(tb, mul_ia<V2>(ta, DD1_6) + DD(c2, 4) + mul_ia<V2>(tb, DD(c1, 2)));
-  explv = explv - mk<V2>(tk2 * rhsv.x, tk2 * rhsv.y);
+  const double* dr = der + (size_t)iy * 20;
+  double c0[5], c2[5], c4[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    c0[j] = __ldg(dr + j);
+    c2[j] = __ldg(dr + 10 + j);
+    c4[j] = __ldg(dr + 15 + j);
+  }
   double2 v1[5], v2[5], v3[5];
 #pragma unroll
   for (int j = 0; j < 5; ++j) {
@@ -111,16 +132,16 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
     }
     const double2 unkn = s2 - rmul(k2, s0);
     const double2 impl = rmul(ni, s4 - rmul(2.0 * k2, s2) + rmul(k2 * k2, s0));
-    const V2 o = old[r1];
-    const double2 e = make_double2((double)explv.x, (double)explv.y);
+    const O2 o = old[r1];
+    const double2 e = make_double2(Num<T>::to_double(explv.x), Num<T>::to_double(explv.y));
     double2 r = rmul(odt, unkn) + impl;
     r = r + rmul(ode2, e);
     r = r - rmul(ode3, make_double2((double)o.x, (double)o.y));
-    old[r1] = explv;
+    old[r1] = hist_store<O2>(explv, e);
     rhs[r1] = r;
   }
   if (ix == 0 && iz == 0) {  // mean flow U + iW (:648-654)
-    const double2 e = make_double2((double)rhsu.x + sc->meanpx, (double)rhsw.x + sc->meanpz);
+    const double2 e = make_double2(Num<T>::to_double(rhsu.x) + sc->meanpx, Num<T>::to_double(rhsw.x) + sc->meanpz);
     double su = c0[0] * v1[0].x, sw = c0[0] * v3[0].x, tu = c2[0] * v1[0].x, tw = c2[0] * v3[0].x;
 #pragma unroll
     for (int j = 1; j < 5; ++j) {
@@ -131,11 +152,11 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
     }
     const double2 unkn = make_double2(su, sw);
     const double2 impl = make_double2(ni * tu, ni * tw);
-    const V2 o = old[r0];
+    const O2 o = old[r0];
     double2 r = rmul(odt, unkn) + impl;
     r = r + rmul(ode2, e);
     r = r - rmul(ode3, make_double2((double)o.x, (double)o.y));
-    old[r0] = mk<V2>((T)e.x, (T)e.y);
+    old[r0] = mk<O2>((OT)e.x, (OT)e.y);
     rhs[r0] = r;
   } else {  // eta (:656-661): with w = i kz V1 - i kx V3, unkn = D0(w), impl = ni (D2(w) - k2 D0(w))
     const V2 ee = mul_ia<V2>(tb, rhsu) - mul_ia<V2>(ta, rhsw);
@@ -148,12 +169,12 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
       s2 = s2 + rmul(c2[j], w);
     }
     const double2 impl = rmul(ni, s2 - rmul(k2, s0));
-    const V2 o = old[r0];
-    const double2 e = make_double2((double)ee.x, (double)ee.y);
+    const O2 o = old[r0];
+    const double2 e = make_double2(Num<T>::to_double(ee.x), Num<T>::to_double(ee.y));
     double2 r = rmul(odt, s0) + impl;
     r = r + rmul(ode2, e);
     r = r - rmul(ode3, make_double2((double)o.x, (double)o.y));
-    old[r0] = ee;
+    old[r0] = hist_store<O2>(ee, e);
     rhs[r0] = r;
   }
 }
@@ -161,12 +182,14 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
 template <typename T>
 void launch_rhs(const SolveLaunch& L, cudaStream_t s) {
   using V2 = typename C2<T>::t;
+  using O2 = typename HistT<T>::t;
   dim3 grid((L.d.nmodes + 127) / 128, L.d.ny - 1);
-  k_rhs<T><<<grid, 128, 0, s>>>(L.V, (const V2*)L.VV, (V2*)L.old, L.rhs, L.der, L.d, L.ode[0], L.ode[1], L.ode[2],
-                                L.sc);
+  k_rhs<T><<<grid, 128, 0, s>>>(L.V, (const V2*)L.VV, (O2*)L.old, L.rhs, L.der, (const T*)L.derT, L.d, L.ode[0],
+                                L.ode[1], L.ode[2], L.sc);
 }
 template void launch_rhs<double>(const SolveLaunch&, cudaStream_t);
 template void launch_rhs<float>(const SolveLaunch&, cudaStream_t);
+template void launch_rhs<dd>(const SolveLaunch&, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // linsolve

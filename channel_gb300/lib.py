@@ -20,7 +20,7 @@ from .dnsin import DnsIn
 
 PKG = Path(__file__).resolve().parent
 RK = [(120.0 / 32.0, 2.0, 0.0), (120.0 / 8.0, 50.0 / 8.0, 34.0 / 8.0), (120.0 / 20.0, 90.0 / 20.0, 50.0 / 20.0)]
-FP64, MIXED = 0, 1
+FP64, MIXED, FP64DD = 0, 1, 2
 
 
 class ChannelError(RuntimeError):
@@ -119,7 +119,7 @@ class Channel:
     def __init__(self, p: DnsIn, precision: str | int = "fp64"):
         self.lib = load_library()
         self.p = p
-        prec = {"fp64": FP64, "mixed": MIXED}.get(precision, precision) if isinstance(precision, str) else precision
+        prec = {"fp64": FP64, "mixed": MIXED, "fp64dd": FP64DD}.get(precision, precision) if isinstance(precision, str) else precision
         self.precision = prec
         self._params = params_struct(p, prec)
         h = C.c_void_p()

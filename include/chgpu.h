@@ -33,6 +33,8 @@ extern "C" {
 
 #define CHGPU_FP64 0  /* every stage in FP64 */
 #define CHGPU_MIXED 1 /* FFTs, products, nonlinear stencils in FP32; solves FP64 */
+#define CHGPU_FP64DD 2 /* FFTs, products, nonlinear stencils in double-float (two FP32
+                        * numbers, ~48 bits) on the FP32 pipes; everything else FP64 */
 
 /* dns.in after read_dnsin (dnsdata.f90:98-125). `ni` holds 1/Re, the value
  * read_dnsin leaves in `ni`. Logical flags are 0/1. */
@@ -51,7 +53,7 @@ typedef struct chgpu_params {
   int time_from_restart;
   long long nstep;
   int npy;
-  int precision; /* CHGPU_FP64 or CHGPU_MIXED */
+  int precision; /* CHGPU_FP64, CHGPU_MIXED or CHGPU_FP64DD */
 } chgpu_params;
 
 /* The numbers outstats prints (dnsdata.f90:876-879), plus the scalars the

@@ -53,8 +53,11 @@ def test_start_line_small(gpu_lib):
     g.close()
 
 
-def test_one_and_ten_steps_small(gpu_lib):
-    _, _, o, g = make("small", 0.01, 0)
+@pytest.mark.parametrize("prec", ["fp64", "fp64dd"])
+def test_one_and_ten_steps_small(gpu_lib, prec):
+    """Both FP64-class paths (native FP64, and double-float transforms) hold
+    the FP64 bars."""
+    _, _, o, g = make("small", 0.01, 0, prec)
     o.start()
     g.start()
     lo, lg = o.step(), g.step()
@@ -111,9 +114,10 @@ def test_wall_velocity_and_cpi(gpu_lib):
         g.close()
 
 
-def test_adaptive_dt_retau180(gpu_lib):
+@pytest.mark.parametrize("prec", ["fp64", "fp64dd"])
+def test_adaptive_dt_retau180(gpu_lib, prec):
     """127x192x127 with cflmax=1 (adaptive dt): one step against the oracle."""
-    _, _, o, g = make("retau180", 0.05, 0)
+    _, _, o, g = make("retau180", 0.05, 0, prec)
     lo0, lg0 = o.start(), g.start()
     ok, err = line_close(lg0, lo0, 1e-12)
     assert ok, (err, lg0, lo0)
