@@ -22,7 +22,7 @@ DRIVER = OUT / "channel_gb300"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", str(ROOT / "include")]
-SOURCES = ["capi.cu", "conv.cu", "solve.cu", "setup.cpp", "noalloc.cu"]
+SOURCES = ["capi.cu", "conv.cu", "solve.cu", "setup.cpp", "noalloc.cu", "stats.cu"]
 
 
 def nvcc() -> str:
@@ -70,7 +70,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
         _run([nv, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"])
     drv_src = CSRC / "driver.cpp"
     if drv_src.exists() and (force or _stale(DRIVER, [drv_src, LIB, ROOT / "include" / "chgpu.h"])):
-        _run(["g++", "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(drv_src), "-o", str(DRIVER),
+        _run(["g++", "-O2", "-std=c++17", "-pthread", "-I", str(ROOT / "include"), str(drv_src), "-o", str(DRIVER),
               f"-L{OUT}", "-lchgpu", f"-Wl,-rpath,{OUT}"])
     return LIB
 

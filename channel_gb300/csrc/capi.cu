@@ -65,6 +65,15 @@ struct chgpu_handle {
   DevScalars* sc_host = nullptr;  // pinned
   cudaGraphExec_t graph = nullptr;
   bool field_set = false;
+  // on-device statistics: [S1, comp S1, S2, comp S2][3][nplanes]
+  double* stats_acc = nullptr;
+  long long stats_n = 0;
+  // asynchronous snapshots: device staging, pinned host copy, side stream
+  double2* snap_stage = nullptr;
+  double* snap_host = nullptr;
+  cudaStream_t snap_stream = nullptr;
+  cudaEvent_t snap_read = nullptr, snap_done = nullptr;
+  bool snap_pending = false;
   // per-kernel timing
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -300,6 +309,12 @@ void release(chgpu_handle* h) {
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (h->sc_host) cudaFreeHost(h->sc_host);
+  if (h->stats_acc) cudaFree(h->stats_acc);
+  if (h->snap_stage) cudaFree(h->snap_stage);
+  if (h->snap_host) cudaFreeHost(h->snap_host);
+  if (h->snap_read) cudaEventDestroy(h->snap_read);
+  if (h->snap_done) cudaEventDestroy(h->snap_done);
+  if (h->snap_stream) cudaStreamDestroy(h->snap_stream);
   if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -618,6 +633,77 @@ int chgpu_kernel_times(chgpu_handle* h, double ms[CHGPU_NKINDS], long long launc
 const char* chgpu_kernel_kind_name(int kind) {
   static const char* names[CHGPU_NKINDS] = {"k_zinv", "k_xrow", "k_zfwd", "k_rhs", "k_linsolve", "scalars"};
   return (kind >= 0 && kind < CHGPU_NKINDS) ? names[kind] : "?";
+}
+
+int chgpu_stats_reset(chgpu_handle* h) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "null handle");
+  const size_t n = (size_t)4 * 3 * h->d.nplanes;
+  if (!h->stats_acc) CK(h, cudaMalloc((void**)&h->stats_acc, sizeof(double) * n));
+  CK(h, cudaMemsetAsync(h->stats_acc, 0, sizeof(double) * n, h->stream));
+  h->stats_n = 0;
+  return 0;
+}
+
+int chgpu_stats_accumulate(chgpu_handle* h) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "null handle");
+  if (!h->stats_acc) {
+    int rc = chgpu_stats_reset(h);
+    if (rc) return rc;
+  }
+  launch_stats_accumulate(h->V, h->d, h->stats_acc, h->stream);
+  h->launches += 1;
+  CK(h, cudaGetLastError());
+  h->stats_n += 1;
+  return 0;
+}
+
+int chgpu_profiles(chgpu_handle* h, double* mean, double* var, long long* nsamples) {
+  if (!h || !mean || !var) return fail(h, CHGPU_E_PARAM, "chgpu_profiles: null argument");
+  if (!h->stats_acc || h->stats_n == 0) return fail(h, CHGPU_E_STATE, "chgpu_profiles: no samples accumulated");
+  const size_t n = (size_t)3 * h->d.nplanes;
+  std::vector<double> acc(4 * n);
+  CK(h, cudaMemcpyAsync(acc.data(), h->stats_acc, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  const double N = (double)h->stats_n;
+  for (size_t k = 0; k < n; ++k) {
+    mean[k] = acc[k] / N;
+    var[k] = acc[2 * n + k] / N - mean[k] * mean[k];
+  }
+  if (nsamples) *nsamples = h->stats_n;
+  return 0;
+}
+
+int chgpu_snapshot_async(chgpu_handle* h) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "null handle");
+  if (h->snap_pending) return fail(h, CHGPU_E_STATE, "chgpu_snapshot_async: previous snapshot not collected");
+  const size_t n = (size_t)3 * h->d.nplanes * h->d.nmodes;
+  if (!h->snap_stage) {
+    CK(h, cudaMalloc((void**)&h->snap_stage, sizeof(double2) * n));
+    CK(h, cudaMallocHost((void**)&h->snap_host, sizeof(double2) * n));
+    CK(h, cudaStreamCreateWithFlags(&h->snap_stream, cudaStreamNonBlocking));
+    CK(h, cudaEventCreateWithFlags(&h->snap_read, cudaEventDisableTiming));
+    CK(h, cudaEventCreateWithFlags(&h->snap_done, cudaEventDisableTiming));
+  }
+  // the transpose reads V in stream order; later steps wait only for it, the
+  // device-to-host copy runs on the side stream while they compute
+  launch_transpose(h->V, h->snap_stage, h->d.nplanes, h->d.nmodes, 3, h->stream);
+  h->launches += 1;
+  CK(h, cudaGetLastError());
+  CK(h, cudaEventRecord(h->snap_read, h->stream));
+  CK(h, cudaStreamWaitEvent(h->snap_stream, h->snap_read, 0));
+  CK(h, cudaMemcpyAsync(h->snap_host, h->snap_stage, sizeof(double2) * n, cudaMemcpyDeviceToHost, h->snap_stream));
+  CK(h, cudaEventRecord(h->snap_done, h->snap_stream));
+  h->snap_pending = true;
+  return 0;
+}
+
+int chgpu_snapshot_wait(chgpu_handle* h, const double** V) {
+  if (!h || !V) return fail(h, CHGPU_E_PARAM, "chgpu_snapshot_wait: null argument");
+  if (!h->snap_pending) return fail(h, CHGPU_E_STATE, "chgpu_snapshot_wait: no snapshot in flight");
+  CK(h, cudaEventSynchronize(h->snap_done));
+  h->snap_pending = false;
+  *V = h->snap_host;
+  return 0;
 }
 
 void* chgpu_stream(chgpu_handle* h) { return h ? (void*)h->stream : nullptr; }

@@ -10,7 +10,7 @@
 //   Dati.cart.<n>.out  snapshots every dt_field (dnsdata.f90:895-918)
 //   Runtimedata   one line per step (dnsdata.f90:878), rewound to the restart
 //                 time when time_from_restart (get_record, dnsdata.f90:181-218)
-// Usage: channel_gb300 [--mixed] [--quiet]   (in the run directory)
+// Usage: channel_gb300 [--mixed | --fp64dd] [--quiet]   (in the run directory)
 #include <chgpu.h>
 
 #include <cmath>
@@ -22,6 +22,7 @@
 #include <iostream>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -97,11 +98,11 @@ static_assert(sizeof(Header) == 68, "restart header is 68 bytes");
 
 size_t field_count(const chgpu_params& p) { return (size_t)3 * (p.nx + 1) * (2 * p.nz + 1) * (p.ny + 3); }
 
-bool write_restart(const std::string& path, const chgpu_params& p, double time, const std::vector<double>& V) {
+bool write_restart(const std::string& path, const chgpu_params& p, double time, const double* V, size_t n) {
   std::FILE* f = std::fopen(path.c_str(), "wb");
   if (!f) return false;
   Header h{p.nx, p.ny, p.nz, p.alfa0, p.beta0, p.ni, p.a, p.ymin, p.ymax, time};
-  bool ok = std::fwrite(&h, sizeof h, 1, f) == 1 && std::fwrite(V.data(), sizeof(double), V.size(), f) == V.size();
+  bool ok = std::fwrite(&h, sizeof h, 1, f) == 1 && std::fwrite(V, sizeof(double), n, f) == n;
   return std::fclose(f) == 0 && ok;
 }
 
@@ -199,22 +200,25 @@ int check(int rc, chgpu_handle* h, const char* what) {
 }  // namespace
 
 int main(int argc, char** argv) {
-  bool mixed = false, quiet = false;
+  bool quiet = false;
+  int precision = CHGPU_FP64;
   for (int i = 1; i < argc; ++i) {
-    if (!std::strcmp(argv[i], "--mixed")) mixed = true;
+    if (!std::strcmp(argv[i], "--mixed")) precision = CHGPU_MIXED;
+    else if (!std::strcmp(argv[i], "--fp64dd")) precision = CHGPU_FP64DD;
     else if (!std::strcmp(argv[i], "--quiet")) quiet = true;
     else {
-      std::fprintf(stderr, "usage: %s [--mixed] [--quiet]\n", argv[0]);
+      std::fprintf(stderr, "usage: %s [--mixed | --fp64dd] [--quiet]\n", argv[0]);
       return 2;
     }
   }
+  const bool mixed = precision == CHGPU_MIXED;
   DnsIn d;
   if (!read_dnsin("dns.in", d)) {
     std::fprintf(stderr, "cannot read dns.in\n");
     return 1;
   }
   const double deltat_from_dnsin = d.p.deltat;
-  d.p.precision = mixed ? CHGPU_MIXED : CHGPU_FP64;
+  d.p.precision = precision;
   chgpu_handle* h = nullptr;
   check(chgpu_create(&d.p, &h), nullptr, "chgpu_create");
   chgpu_params& p = d.p;
@@ -266,7 +270,7 @@ int main(int argc, char** argv) {
     std::printf("   meanpx =%11.6f      meanpz =%11.6f\n", p.meanpx, p.meanpz);
     std::printf("   meanflowx =%11.6f   meanflowz =%11.6f\n", p.meanflowx, p.meanflowz);
     std::printf("   nsteps =%6lld   time_from_restart =%c   precision = %s\n\n", p.nstep,
-                p.time_from_restart ? 'T' : 'F', mixed ? "mixed" : "fp64");
+                p.time_from_restart ? 'T' : 'F', mixed ? "mixed" : (precision == CHGPU_FP64DD ? "fp64dd" : "fp64"));
   }
   check(chgpu_upload_field(h, V.data()), h, "upload");
   chgpu_stats st{};
@@ -279,8 +283,26 @@ int main(int argc, char** argv) {
   long long istep = 0;
   deltat = st.deltat;
   time = st.time;
+  // Snapshots leave the device while later steps run: the field is copied
+  // to a pinned buffer on a side stream (chgpu_snapshot_async), collected
+  // after the next step and written by a thread.
+  std::thread writer;
+  std::vector<std::string> pend_names;
+  double pend_time = 0.0;
+  bool pending = false;
+  auto collect = [&]() {
+    if (!pending) return;
+    const double* Vh = nullptr;
+    check(chgpu_snapshot_wait(h, &Vh), h, "snapshot");
+    if (writer.joinable()) writer.join();
+    writer = std::thread([&p, names = pend_names, pend_time, Vh, n = V.size()]() {
+      for (const auto& nm : names) write_restart(nm, p, pend_time, Vh, n);
+    });
+    pending = false;
+  };
   while (time < p.t_max - deltat / 2.0 && istep < p.nstep) {
     check(chgpu_step(h, &st), h, "step");
+    collect();  // the snapshot of the previous step has arrived by now
     istep = st.istep;
     time = st.time;
     deltat = st.deltat;
@@ -288,11 +310,11 @@ int main(int argc, char** argv) {
     rtd.flush();
     if (!quiet) echo_line(st.line);
     // restart and snapshot cadence (dnsdata.f90:882-918)
+    std::vector<std::string> names;
     if (p.dt_save > 0 && std::floor((time + 0.5 * deltat) / p.dt_save) > std::floor((time - 0.5 * deltat) / p.dt_save) &&
         istep > 1) {
       std::printf(" Writing Dati.cart.out at time %g\n", time);
-      check(chgpu_download_field(h, V.data()), h, "download");
-      write_restart("Dati.cart.out", p, time, V);
+      names.push_back("Dati.cart.out");
     }
     if (time + deltat >= (ifield + 1) * p.dt_field) {
       if (prev_was_close || (std::floor((time + 0.5 * deltat) / p.dt_field) >
@@ -301,17 +323,25 @@ int main(int argc, char** argv) {
         ++ifield;
         std::string name = "Dati.cart." + std::to_string(ifield) + ".out";
         std::printf(" Writing %s at time %g\n", name.c_str(), time);
-        check(chgpu_download_field(h, V.data()), h, "download");
-        write_restart(name, p, time, V);
+        names.push_back(name);
         prev_was_close = false;
       } else {
         prev_was_close = true;
       }
     }
+    if (!names.empty()) {
+      if (writer.joinable()) writer.join();  // the library's snapshot buffer is free again
+      check(chgpu_snapshot_async(h), h, "snapshot");
+      pend_names = names;
+      pend_time = time;
+      pending = true;
+    }
   }
+  collect();
+  if (writer.joinable()) writer.join();
   std::printf(" End of time/iterations loop: writing restart file at time %g\n", time);
   check(chgpu_download_field(h, V.data()), h, "download");
-  write_restart("Dati.cart.out", p, time, V);
+  write_restart("Dati.cart.out", p, time, V.data(), V.size());
   chgpu_destroy(h);
   return 0;
 }

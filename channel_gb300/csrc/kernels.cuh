@@ -76,5 +76,6 @@ void launch_advance_time(DevScalars* sc, double coef, int new_step, cudaStream_t
 void launch_outstats(const SolveLaunch& L, cudaStream_t s);
 void launch_flowrate(const SolveLaunch& L, cudaStream_t s);
 void launch_transpose(const double2* in, double2* out, int rows, int cols, int batch, cudaStream_t s);
+void launch_stats_accumulate(const double2* V, const Dims& d, double* acc, cudaStream_t s);
 
 }  // namespace chgpu

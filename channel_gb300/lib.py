@@ -74,6 +74,11 @@ SIGNATURES = {
     "chgpu_set_profiling": (C.c_int, [_P, C.c_int]),
     "chgpu_kernel_times": (C.c_int, [_P, _DP, C.POINTER(C.c_longlong)]),
     "chgpu_kernel_kind_name": (C.c_char_p, [C.c_int]),
+    "chgpu_stats_reset": (C.c_int, [_P]),
+    "chgpu_stats_accumulate": (C.c_int, [_P]),
+    "chgpu_profiles": (C.c_int, [_P, _DP, _DP, C.POINTER(C.c_longlong)]),
+    "chgpu_snapshot_async": (C.c_int, [_P]),
+    "chgpu_snapshot_wait": (C.c_int, [_P, C.POINTER(_DP)]),
     "chgpu_linsolve_noalloc": (C.c_int, [C.POINTER(Params), C.c_double, C.c_void_p, _DP, C.c_void_p,
                                          C.c_char_p, C.c_size_t]),
 }
@@ -208,6 +213,29 @@ class Channel:
         n = (C.c_longlong * NKINDS)()
         self._check(self.lib.chgpu_kernel_times(self.h, _dp(ms), n))
         return {self.lib.chgpu_kernel_kind_name(k).decode(): (float(ms[k]), int(n[k])) for k in range(NKINDS)}
+
+    def stats_reset(self):
+        self._check(self.lib.chgpu_stats_reset(self.h))
+
+    def stats_accumulate(self):
+        self._check(self.lib.chgpu_stats_accumulate(self.h))
+
+    def profiles(self):
+        """(mean, var, nsamples): mean and variance profiles, arrays (3, ny+3)."""
+        n = 3 * (self.p.ny + 3)
+        mean, var = np.empty(n), np.empty(n)
+        ns = C.c_longlong()
+        self._check(self.lib.chgpu_profiles(self.h, _dp(mean), _dp(var), C.byref(ns)))
+        return mean.reshape(3, -1), var.reshape(3, -1), int(ns.value)
+
+    def snapshot_async(self):
+        self._check(self.lib.chgpu_snapshot_async(self.h))
+
+    def snapshot_wait(self) -> np.ndarray:
+        ptr = _DP()
+        self._check(self.lib.chgpu_snapshot_wait(self.h, C.byref(ptr)))
+        n = int(np.prod(self.shape))
+        return np.ctypeslib.as_array(ptr, shape=(2 * n,)).view(np.complex128).reshape(self.shape).copy()
 
     @property
     def launches(self) -> int:

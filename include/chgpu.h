@@ -120,6 +120,28 @@ int chgpu_get_stats(chgpu_handle* h, chgpu_stats* st);
  * error flags (non-finite CFL) as CHGPU_E_NONFINITE. */
 int chgpu_synchronize(chgpu_handle* h);
 
+/* On-device statistics of the field, the mean and variance profiles of the
+ * reference's post-processing (postpro/history/var_history.f90:37-84).
+ * chgpu_stats_accumulate adds the current field to compensated running sums
+ * (one kernel, in stream order); chgpu_profiles returns for each component
+ * ic=1..3 and row iy=-1..ny+1 (arrays of 3*(ny+3), iy fastest)
+ *   mean = < Re V(iy,0,0,ic) >,
+ *   var  = < sum_{ix,iz} f_ix |V(iy,iz,ix,ic)|^2 > - mean^2, f_ix = 1 (ix=0), 2,
+ * over the samples since chgpu_stats_reset (the squared rms profile). */
+int chgpu_stats_reset(chgpu_handle* h);
+int chgpu_stats_accumulate(chgpu_handle* h);
+int chgpu_profiles(chgpu_handle* h, double* mean, double* var, long long* nsamples);
+
+/* Field snapshot for output without stalling the time loop (the dt_field /
+ * dt_save writes, dnsdata.f90:882-918).  chgpu_snapshot_async copies V to a
+ * device staging buffer in stream order and then, on a side stream while
+ * later steps run, to a pinned host buffer owned by the handle.
+ * chgpu_snapshot_wait blocks until that copy is complete and points *V at
+ * the field (restart-file layout), valid until the next chgpu_snapshot_async.
+ * One snapshot may be in flight at a time. */
+int chgpu_snapshot_async(chgpu_handle* h);
+int chgpu_snapshot_wait(chgpu_handle* h, const double** V);
+
 /* The handle's CUDA stream (cudaStream_t), for callers that order their own
  * work against the solver's. */
 void* chgpu_stream(chgpu_handle* h);

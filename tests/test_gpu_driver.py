@@ -35,6 +35,15 @@ def test_driver_run_and_restart(gpu_lib, tmp_path):
     assert max(per_field_rel(V, o.field())) <= 1e-11
     snaps = sorted(tmp_path.glob("Dati.cart.*.out"))
     assert len(snaps) >= 1  # Dati.cart.1.out, ... at t=0.012, ...
+    # the first snapshot (written while later steps ran) holds the field of its step
+    hs, Vs = fields.read_restart(tmp_path / "Dati.cart.1.out")
+    k = int(round(hs.time / 0.004))
+    o2 = pyoracle.Oracle(p)
+    o2.set_field(V0)
+    o2.start()
+    for _ in range(k):
+        o2.step()
+    assert max(per_field_rel(Vs, o2.field())) <= 1e-11
     # restart: time from the file, Runtimedata rewound to that record
     p.time_from_restart = True
     p.nstep = 3
