@@ -29,70 +29,152 @@ template <typename V> __device__ __forceinline__ V mul_i(V a, int sign) {
   return sign > 0 ? mk<V>(-a.y, a.x) : mk<V>(a.y, -a.x);
 }
 
-// Radix plan passed by value to kernels.
+// Radix plan passed by value to kernels: radices 16, then one of 8/4/2, then
+// 3 (lengths 2^a 3^b, b <= 1), so every stride before the last stage is a
+// power of two.
 struct RadixDev {
   int n, nst;
   int r[24];
 };
 
-// Batched in-shared-memory Stockham FFT (Govindaraju et al. 2008 formulation):
-// `B` transforms of length rad.n, contiguous, in `a`; `b` is scratch of the
-// same size. Unnormalised; sign -1: exp(-i...), +1: exp(+i...). `tw` holds
-// the forward roots exp(-2 pi i m / n), m<n. Returns the buffer holding the
-// result. Every thread of the block must call it.
+// In-register DFTs of length R (natural order in and out), sign -1: exp(-i),
+// +1: exp(+i).  Internal twiddles are constants of the type.
+template <typename V> __device__ __forceinline__ void dft4(V& a0, V& a1, V& a2, V& a3, int sign) {
+  const V t0 = a0 + a2, t1 = a0 - a2, t2 = a1 + a3, t3 = mul_i(a1 - a3, sign);
+  a0 = t0 + t2;
+  a1 = t1 + t3;
+  a2 = t0 - t2;
+  a3 = t1 - t3;
+}
+
+template <int R, typename V> struct Dft;
+template <typename V> struct Dft<2, V> {
+  __device__ static void run(V* a, int) {
+    const V t = a[0] - a[1];
+    a[0] = a[0] + a[1];
+    a[1] = t;
+  }
+};
+template <typename V> struct Dft<3, V> {
+  __device__ static void run(V* a, int sign) {
+    using T = decltype(V::x);
+    const V t1 = a[1] + a[2];
+    const V t2 = a[0] - scale(t1, T(0.5f));
+    const V t3 = mul_i(scale(a[1] - a[2], Num<T>::sqrt3_2()), sign);
+    a[0] = a[0] + t1;
+    a[1] = t2 + t3;
+    a[2] = t2 - t3;
+  }
+};
+template <typename V> struct Dft<4, V> {
+  __device__ static void run(V* a, int sign) { dft4(a[0], a[1], a[2], a[3], sign); }
+};
+template <typename V> struct Dft<8, V> {
+  // r = 2 r1 + r2, k = k1 + 4 k2: DFT4 over r1, twiddle w8^(r2 k1), DFT2 over r2
+  __device__ static void run(V* a, int sign) {
+    using T = decltype(V::x);
+    const T r2 = Num<T>::sqrt1_2();
+    const T sr2 = sign > 0 ? r2 : -r2;
+    dft4(a[0], a[2], a[4], a[6], sign);
+    dft4(a[1], a[3], a[5], a[7], sign);
+    a[3] = cmul(a[3], mk<V>(r2, sr2));   // w8^1
+    a[5] = mul_i(a[5], sign);            // w8^2
+    a[7] = cmul(a[7], mk<V>(-r2, sr2));  // w8^3
+    V y[8];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+      y[k1] = a[2 * k1] + a[2 * k1 + 1];
+      y[k1 + 4] = a[2 * k1] - a[2 * k1 + 1];
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = y[k];
+  }
+};
+template <typename V> struct Dft<16, V> {
+  // r = 4 r1 + r2, k = k1 + 4 k2: DFT4 over r1, twiddle w16^(r2 k1), DFT4 over r2
+  __device__ static void run(V* a, int sign) {
+    using T = decltype(V::x);
+    const T c = Num<T>::cos_pi8(), s = Num<T>::sin_pi8(), r2 = Num<T>::sqrt1_2();
+    const T ss = sign > 0 ? s : -s, sc = sign > 0 ? c : -c, sr2 = sign > 0 ? r2 : -r2;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) dft4(a[q], a[q + 4], a[q + 8], a[q + 12], sign);
+    // b[r2][k1] sits in a[r2 + 4 k1]
+    a[1 + 4] = cmul(a[1 + 4], mk<V>(c, ss));     // w^1
+    a[1 + 8] = cmul(a[1 + 8], mk<V>(r2, sr2));   // w^2
+    a[1 + 12] = cmul(a[1 + 12], mk<V>(s, sc));   // w^3
+    a[2 + 4] = cmul(a[2 + 4], mk<V>(r2, sr2));   // w^2
+    a[2 + 8] = mul_i(a[2 + 8], sign);            // w^4
+    a[2 + 12] = cmul(a[2 + 12], mk<V>(-r2, sr2));  // w^6
+    a[3 + 4] = cmul(a[3 + 4], mk<V>(s, sc));     // w^3
+    a[3 + 8] = cmul(a[3 + 8], mk<V>(-r2, sr2));  // w^6
+    a[3 + 12] = cmul(a[3 + 12], mk<V>(-c, -ss));  // w^9
+    V y[16];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+      V b0 = a[4 * k1], b1 = a[4 * k1 + 1], b2 = a[4 * k1 + 2], b3 = a[4 * k1 + 3];
+      dft4(b0, b1, b2, b3, sign);
+      y[k1] = b0;
+      y[k1 + 4] = b1;
+      y[k1 + 8] = b2;
+      y[k1 + 12] = b3;
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) a[k] = y[k];
+  }
+};
+
+// One Stockham stage (Govindaraju et al. 2008 formulation) with radix R over
+// B transforms of length n: item j of a transform reads R points at stride
+// n/R, twiddles them by w_{Ns R}^{r k} (k = j mod Ns), transforms them in
+// registers and writes them at stride Ns.  Ns is a power of two.
+template <int R, typename V>
+__device__ __forceinline__ void stockham_stage(const V* __restrict__ src, V* __restrict__ dst, int B, int n, int Ns,
+                                               int sign, const V* __restrict__ tw) {
+  const int nb = n / R;
+  const int total = B * nb;
+  const int twstep = n / (Ns * R);
+  const unsigned magic = 0xFFFFFFFFu / (unsigned)nb + 1u;  // item / nb by multiply-high
+  for (int item = threadIdx.x; item < total; item += blockDim.x) {
+    int t = (int)__umulhi((unsigned)item, magic);
+    if (t * nb > item) --t;
+    const int j = item - t * nb;
+    const int k = j & (Ns - 1);
+    const V* s = src + (size_t)t * n;
+    V* d = dst + (size_t)t * n;
+    V a[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) a[r] = s[j + r * nb];
+    if (k != 0) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        V w = tw[r * k * twstep];
+        if (sign > 0) w = conjg(w);
+        a[r] = cmul(a[r], w);
+      }
+    }
+    Dft<R, V>::run(a, sign);
+    const int idxD = (j - k) * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) d[idxD + r * Ns] = a[r];
+  }
+}
+
+// Batched in-shared-memory FFT: `B` transforms of length rad.n, contiguous,
+// in `a`; `b` is scratch of the same size. Unnormalised; sign -1: exp(-i...),
+// +1: exp(+i...). `tw` holds the forward roots exp(-2 pi i m / n), m<n.
+// Returns the buffer holding the result. Every thread of the block calls it.
 template <typename V>
 __device__ V* fft_block(V* a, V* b, int B, const RadixDev& rad, int sign, const V* __restrict__ tw) {
-  using T = decltype(V::x);
   const int n = rad.n;
   int Ns = 1;
-  const T h3 = Num<T>::sqrt3_2();
   for (int st = 0; st < rad.nst; ++st) {
     const int R = rad.r[st];
-    const int nb = n / R;
-    const int total = B * nb;
-    const int twstep = n / (Ns * R);
-    for (int item = threadIdx.x; item < total; item += blockDim.x) {
-      const int t = item / nb;
-      const int j = item - t * nb;
-      const V* src = a + (size_t)t * n;
-      V* dst = b + (size_t)t * n;
-      const int k = j % Ns;
-      V v0 = src[j], v1 = src[j + nb], v2, v3;
-      if (R >= 3) v2 = src[j + 2 * nb];
-      if (R == 4) v3 = src[j + 3 * nb];
-      if (k != 0) {
-        V w = tw[k * twstep];
-        if (sign > 0) w = conjg(w);
-        v1 = cmul(v1, w);
-        if (R >= 3) {
-          V w2 = tw[2 * k * twstep];
-          if (sign > 0) w2 = conjg(w2);
-          v2 = cmul(v2, w2);
-        }
-        if (R == 4) {
-          V w3 = tw[3 * k * twstep];
-          if (sign > 0) w3 = conjg(w3);
-          v3 = cmul(v3, w3);
-        }
-      }
-      const int idxD = (j - k) * R + k;
-      if (R == 2) {
-        dst[idxD] = v0 + v1;
-        dst[idxD + Ns] = v0 - v1;
-      } else if (R == 4) {
-        V t0 = v0 + v2, t1 = v0 - v2, t2 = v1 + v3, t3 = mul_i(v1 - v3, sign);
-        dst[idxD] = t0 + t2;
-        dst[idxD + Ns] = t1 + t3;
-        dst[idxD + 2 * Ns] = t0 - t2;
-        dst[idxD + 3 * Ns] = t1 - t3;
-      } else {
-        V t1 = v1 + v2;
-        V t2 = v0 - scale(t1, T(0.5f));
-        V t3 = mul_i(scale(v1 - v2, h3), sign);
-        dst[idxD] = v0 + t1;
-        dst[idxD + Ns] = t2 + t3;
-        dst[idxD + 2 * Ns] = t2 - t3;
-      }
+    switch (R) {
+      case 16: stockham_stage<16>(a, b, B, n, Ns, sign, tw); break;
+      case 8: stockham_stage<8>(a, b, B, n, Ns, sign, tw); break;
+      case 4: stockham_stage<4>(a, b, B, n, Ns, sign, tw); break;
+      case 2: stockham_stage<2>(a, b, B, n, Ns, sign, tw); break;
+      default: stockham_stage<3>(a, b, B, n, Ns, sign, tw); break;
     }
     __syncthreads();
     V* tmp = a;

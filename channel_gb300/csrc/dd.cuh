@@ -60,10 +60,28 @@ __device__ __forceinline__ dd dd_abs(dd a) { return a.hi < 0.f ? -a : a; }
 __device__ __forceinline__ dd dd_max(dd a, dd b) { return (a < b) ? b : a; }
 __device__ __forceinline__ bool dd_isfinite(dd a) { return isfinite(a.hi) && isfinite(a.lo); }
 
+// x1*y1 + x2*y2 with one renormalisation: both products exactly as
+// hi-product + FMA error + cross terms, one two-sum of the high parts.
+__device__ __forceinline__ dd dd_dot2(dd x1, dd y1, dd x2, dd y2) {
+  const float p1 = __fmul_rn(x1.hi, y1.hi);
+  float e1 = __fmaf_rn(x1.hi, y1.hi, -p1);
+  e1 = __fmaf_rn(x1.hi, y1.lo, e1);
+  e1 = __fmaf_rn(x1.lo, y1.hi, e1);
+  const float p2 = __fmul_rn(x2.hi, y2.hi);
+  float e2 = __fmaf_rn(x2.hi, y2.hi, -p2);
+  e2 = __fmaf_rn(x2.hi, y2.lo, e2);
+  e2 = __fmaf_rn(x2.lo, y2.hi, e2);
+  dd s = two_sum(p1, p2);
+  s.lo = __fadd_rn(s.lo, __fadd_rn(e1, e2));
+  return fast_two_sum(s.hi, s.lo);
+}
+
 // complex double-float: 16 bytes, like double2
 struct __align__(16) cdd {
   dd x, y;
 };
+// complex product in two fused dot products (38 FP32 operations instead of 68)
+__device__ __forceinline__ cdd cmul(cdd a, cdd b) { return cdd{dd_dot2(a.x, b.x, -a.y, b.y), dd_dot2(a.x, b.y, a.y, b.x)}; }
 __device__ __forceinline__ cdd operator+(cdd a, cdd b) { return cdd{a.x + b.x, a.y + b.y}; }
 __device__ __forceinline__ cdd operator-(cdd a, cdd b) { return cdd{a.x - b.x, a.y - b.y}; }
 
@@ -104,6 +122,9 @@ template <> struct Num<double> {
   __device__ static double max(double a, double b) { return fmax(a, b); }
   __device__ static bool finite(double v) { return isfinite(v); }
   __device__ static constexpr double sqrt3_2() { return 0.86602540378443864676372317075294; }
+  __device__ static constexpr double cos_pi8() { return 0.9238795325112867; }
+  __device__ static constexpr double sin_pi8() { return 0.3826834323650898; }
+  __device__ static constexpr double sqrt1_2() { return 0.7071067811865476; }
 };
 template <> struct Num<float> {
   __device__ static float from_double(double v) { return (float)v; }
@@ -112,6 +133,9 @@ template <> struct Num<float> {
   __device__ static float max(float a, float b) { return fmaxf(a, b); }
   __device__ static bool finite(float v) { return isfinite(v); }
   __device__ static constexpr float sqrt3_2() { return 0.866025404f; }
+  __device__ static constexpr float cos_pi8() { return 0.923879533f; }
+  __device__ static constexpr float sin_pi8() { return 0.382683432f; }
+  __device__ static constexpr float sqrt1_2() { return 0.707106781f; }
 };
 template <> struct Num<dd> {
   __device__ static dd from_double(double v) { return dd_from_double(v); }
@@ -120,6 +144,9 @@ template <> struct Num<dd> {
   __device__ static dd max(dd a, dd b) { return dd_max(a, b); }
   __device__ static bool finite(dd v) { return dd_isfinite(v); }
   __device__ static constexpr dd sqrt3_2() { return dd(0.866025388f, 1.55436251e-08f); }
+  __device__ static constexpr dd cos_pi8() { return dd(0.923879504f, 2.83074897e-08f); }
+  __device__ static constexpr dd sin_pi8() { return dd(0.382683426f, 6.22335072e-09f); }
+  __device__ static constexpr dd sqrt1_2() { return dd(0.707106769f, 1.21016175e-08f); }
 };
 
 }  // namespace chgpu

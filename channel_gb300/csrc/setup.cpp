@@ -31,8 +31,10 @@ Radix make_radix(int n) {
   Radix r;
   r.n = n;
   int m = n;
-  while (m % 4 == 0) { r.r[r.nst++] = 4; m /= 4; }
-  if (m % 2 == 0) { r.r[r.nst++] = 2; m /= 2; }
+  while (m % 16 == 0) { r.r[r.nst++] = 16; m /= 16; }
+  if (m % 8 == 0) { r.r[r.nst++] = 8; m /= 8; }
+  else if (m % 4 == 0) { r.r[r.nst++] = 4; m /= 4; }
+  else if (m % 2 == 0) { r.r[r.nst++] = 2; m /= 2; }
   if (m % 3 == 0) { r.r[r.nst++] = 3; m /= 3; }
   if (m != 1) r.nst = -1;
   return r;
