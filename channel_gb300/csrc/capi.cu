@@ -55,6 +55,7 @@ struct chgpu_handle {
   double* fac = nullptr;
   double* der = nullptr;
   void* derT = nullptr;
+  void* cst = nullptr;  // transform-type constants: factor, 1/dx, 1/dz, 1/dy per plane
   double* d0lu = nullptr;
   double* yint = nullptr;
   double* dy = nullptr;
@@ -135,6 +136,14 @@ int upload_derT(chgpu_handle* h) {
   t[der.size() + 1] = from_ld<T>((long double)h->p.beta0);
   CK(h, cudaMalloc(&h->derT, sizeof(T) * t.size()));
   CK(h, cudaMemcpy(h->derT, t.data(), sizeof(T) * t.size(), cudaMemcpyHostToDevice));
+  // constants of the x-row pass: factor, 1/dx, 1/dz (dnsdata.f90:124), 1/dy(iy) per plane (:155)
+  std::vector<T> c(3 + h->d.nplanes, T());
+  c[0] = from_ld<T>((long double)h->d.factor);
+  c[1] = from_ld<T>((long double)h->d.rdx);
+  c[2] = from_ld<T>((long double)h->d.rdz);
+  for (int iy = 1; iy <= h->p.ny - 1; ++iy) c[3 + iy + 1] = from_ld<T>(1.0L / (long double)h->tab.dy[iy]);
+  CK(h, cudaMalloc(&h->cst, sizeof(T) * c.size()));
+  CK(h, cudaMemcpy(h->cst, c.data(), sizeof(T) * c.size(), cudaMemcpyHostToDevice));
   return 0;
 }
 
@@ -184,6 +193,7 @@ ConvLaunch conv_launch(chgpu_handle* h, int compute_cfl, int products, int plane
   L.twx = h->twx;
   L.twh = h->twh;
   L.dy = h->dy;
+  L.cst = h->cst;
   L.sc = h->sc;
   L.zcols = h->zcols;
   L.xrows = h->xrows;
@@ -304,7 +314,7 @@ void release(chgpu_handle* h) {
     cudaEventDestroy(pe.second.second);
   }
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
-  void* bufs[] = {h->V, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->derT, h->d0lu, h->yint, h->dy,
+  void* bufs[] = {h->V, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->derT, h->cst, h->d0lu, h->yint, h->dy,
                   h->twz, h->twx, h->twh, h->sc};
   for (void* b : bufs)
     if (b) cudaFree(b);

@@ -39,8 +39,9 @@ __global__ void __launch_bounds__(256) k_zinv(const double2* __restrict__ V, typ
   const int ix0 = blockIdx.x * nb_cols;
   const int nb = min(nb_cols, nxp - ix0);
   const size_t colbase = ((size_t)c * d.nplanes + plane) * nxp;
+  const FastDiv by_nzd(nzd);
   for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) {
-    const int b = idx / nzd;
+    const int b = by_nzd.div(idx);
     const int jz = idx - b * nzd;
     V2 val = czero<V2>();
     int izp = -1;
@@ -55,7 +56,7 @@ __global__ void __launch_bounds__(256) k_zinv(const double2* __restrict__ V, typ
   __syncthreads();
   V2* res = fft_block<V2>(bufA, bufB, nb, rz, +1, twz);
   for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) {
-    const int b = idx / nzd;
+    const int b = by_nzd.div(idx);
     const int jz = idx - b * nzd;
     Zb[(colbase + ix0 + b) * nzd + jz] = res[idx];
   }
@@ -78,7 +79,7 @@ __device__ __forceinline__ void block_max_atomic(double v, double* target) {
 template <typename T>
 __global__ void __launch_bounds__(256) k_xrow(const typename C2<T>::t* __restrict__ Zb, typename C2<T>::t* __restrict__ Pb,
                                               const typename C2<T>::t* __restrict__ twx,
-                                              const typename C2<T>::t* __restrict__ twh, const double* __restrict__ dy,
+                                              const typename C2<T>::t* __restrict__ twh, const T* __restrict__ cst,
                                               Dims d, RadixDev rx, int nrows, int plane0, int compute_cfl,
                                               DevScalars* sc) {
   using V2 = typename C2<T>::t;
@@ -87,15 +88,17 @@ __global__ void __launch_bounds__(256) k_xrow(const typename C2<T>::t* __restric
   const int plane = plane0 + blockIdx.y;
   const int jz0 = blockIdx.x * nrows;
   const int S = 3 * nrows * M;  // one buffer group: [3][nrows][M]
+  const int lgr = __ffs(nrows) - 1;  // nrows is 1, 2 or 4
+  const FastDiv by_M(M), by_nxp(nxp);
   V2* A = reinterpret_cast<V2*>(smem_raw);
   V2* B = A + S;
   V2* Cb = B + S;
   // load the three spectra rows (zTOx, x zero band; dnsdata.f90:533-535)
   for (int idx = threadIdx.x; idx < 3 * M * nrows; idx += blockDim.x) {
-    const int r = idx % nrows;
-    const int ck = idx / nrows;
-    const int k = ck % M;
-    const int c = ck / M;
+    const int r = idx & (nrows - 1);
+    const int ck = idx >> lgr;
+    const int c = by_M.div(ck);
+    const int k = ck - c * M;
     V2 val = czero<V2>();
     if (k <= nx) val = Zb[(((size_t)c * d.nplanes + plane) * nxp + k) * nzd + jz0 + r];
     Cb[((size_t)c * nrows + r) * M + k] = val;
@@ -103,8 +106,8 @@ __global__ void __launch_bounds__(256) k_xrow(const typename C2<T>::t* __restric
   __syncthreads();
   // c2r packing: Z[k] = (X[k]+conj(X[M-k])) + i (X[k]-conj(X[M-k])) e^{+i pi k/M}
   for (int idx = threadIdx.x; idx < S; idx += blockDim.x) {
-    const int k = idx % M;
-    const int cr = idx / M;
+    const int cr = by_M.div(idx);
+    const int k = idx - cr * M;
     const V2* X = Cb + (size_t)cr * M;
     V2 xk = X[k];
     V2 xm = czero<V2>();
@@ -117,14 +120,14 @@ __global__ void __launch_bounds__(256) k_xrow(const typename C2<T>::t* __restric
   V2* U = fft_block<V2>(A, B, 3 * nrows, rx, +1, twx);
   V2* freeb = (U == A) ? B : A;
   // CFL (dnsdata.f90:552-556) and products uu,vv,ww (:584)
-  const T f = Num<T>::from_double(d.factor);
+  const T f = cst[0];
   T cfl = T();
   bool bad = false;
   const bool do_cfl = compute_cfl && plane >= 2 && plane <= d.ny;
-  const T rdx = Num<T>::from_double(d.rdx), rdz = Num<T>::from_double(d.rdz);
-  const T rdy = do_cfl ? Num<T>::from_double(1.0 / dy[plane - 1]) : T();
+  const T rdx = cst[1], rdz = cst[2];
+  const T rdy = do_cfl ? cst[3 + plane] : T();
   for (int idx = threadIdx.x; idx < nrows * M; idx += blockDim.x) {
-    const int m = idx % M, r = idx / M;
+    const int r = by_M.div(idx), m = idx - r * M;
     V2 u = U[((size_t)0 * nrows + r) * M + m];
     V2 v = U[((size_t)1 * nrows + r) * M + m];
     V2 w = U[((size_t)2 * nrows + r) * M + m];
@@ -145,7 +148,7 @@ __global__ void __launch_bounds__(256) k_xrow(const typename C2<T>::t* __restric
   for (int half = 0; half < 2; ++half) {
     if (half == 1) {  // products uv, vw, uw (dnsdata.f90:581-583)
       for (int idx = threadIdx.x; idx < nrows * M; idx += blockDim.x) {
-        const int m = idx % M, r = idx / M;
+        const int r = by_M.div(idx), m = idx - r * M;
         V2 u = U[((size_t)0 * nrows + r) * M + m];
         V2 v = U[((size_t)1 * nrows + r) * M + m];
         V2 w = U[((size_t)2 * nrows + r) * M + m];
@@ -158,10 +161,10 @@ __global__ void __launch_bounds__(256) k_xrow(const typename C2<T>::t* __restric
     V2* P = fft_block<V2>(Cb, freeb, 3 * nrows, rx, -1, twx);
     // r2c unpacking, kx = 0..nx (HFT + xTOz, dnsdata.f90:586-588)
     for (int idx = threadIdx.x; idx < 3 * nxp * nrows; idx += blockDim.x) {
-      const int r = idx % nrows;
-      const int pk = idx / nrows;
-      const int k = pk % nxp;
-      const int p = pk / nxp;
+      const int r = idx & (nrows - 1);
+      const int pk = idx >> lgr;
+      const int p = by_nxp.div(pk);
+      const int k = pk - p * nxp;
       const V2* Z = P + ((size_t)p * nrows + r) * M;
       V2 zk = Z[k];
       V2 zm = conjg(Z[k == 0 ? 0 : M - k]);
@@ -197,8 +200,9 @@ __global__ void __launch_bounds__(256) k_zfwd(const typename C2<T>::t* __restric
   for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) bufA[idx] = Pb[(colbase + ix0) * nzd + idx];
   __syncthreads();
   V2* res = fft_block<V2>(bufA, bufB, nb, rz, -1, twz);
+  const FastDiv by_nzt(nzt);
   for (int idx = threadIdx.x; idx < nb * nzt; idx += blockDim.x) {
-    const int b = idx / nzt;
+    const int b = by_nzt.div(idx);
     const int izp = idx - b * nzt;
     const int iz = izp - nz;
     const int jz = iz >= 0 ? iz : nzd + iz;
@@ -219,7 +223,7 @@ void launch_convolutions(const ConvLaunch& L, cudaStream_t s, int stage) {
   if (stage == 1) {
     dim3 grid(d.nzd / L.xrows, L.nplanes);
     size_t sm = 9 * (size_t)L.xrows * d.nxd * sizeof(V2);
-    k_xrow<T><<<grid, 256, sm, s>>>((const V2*)L.Zb, (V2*)L.Pb, (const V2*)L.twx, (const V2*)L.twh, L.dy, d, L.rx,
+    k_xrow<T><<<grid, 256, sm, s>>>((const V2*)L.Zb, (V2*)L.Pb, (const V2*)L.twx, (const V2*)L.twh, (const T*)L.cst, d, L.rx,
                                     L.xrows, L.plane0, L.compute_cfl, L.sc);
   }
   if (stage == 2) {

@@ -29,6 +29,18 @@ template <typename V> __device__ __forceinline__ V mul_i(V a, int sign) {
   return sign > 0 ? mk<V>(-a.y, a.x) : mk<V>(a.y, -a.x);
 }
 
+// x / d and x % d for 0 <= x, x*d < 2^32 by a multiply-high (integer
+// division by a value unknown at compile time costs tens of instructions).
+struct FastDiv {
+  int d;
+  unsigned magic;
+  __device__ __forceinline__ explicit FastDiv(int dv) : d(dv), magic(0xFFFFFFFFu / (unsigned)dv + 1u) {}
+  __device__ __forceinline__ int div(int x) const {
+    int q = (int)__umulhi((unsigned)x, magic);
+    return (q * d > x) ? q - 1 : q;
+  }
+};
+
 // Radix plan passed by value to kernels: radices 16, then one of 8/4/2, then
 // 3 (lengths 2^a 3^b, b <= 1), so every stride before the last stage is a
 // power of two.
@@ -133,10 +145,9 @@ __device__ __forceinline__ void stockham_stage(const V* __restrict__ src, V* __r
   const int nb = n / R;
   const int total = B * nb;
   const int twstep = n / (Ns * R);
-  const unsigned magic = 0xFFFFFFFFu / (unsigned)nb + 1u;  // item / nb by multiply-high
+  const FastDiv by_nb(nb);
   for (int item = threadIdx.x; item < total; item += blockDim.x) {
-    int t = (int)__umulhi((unsigned)item, magic);
-    if (t * nb > item) --t;
+    const int t = by_nb.div(item);
     const int j = item - t * nb;
     const int k = j & (Ns - 1);
     const V* s = src + (size_t)t * n;

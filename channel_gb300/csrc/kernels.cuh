@@ -38,6 +38,7 @@ struct ConvLaunch {
   const void* twx;
   const void* twh;
   const double* dy;
+  const void* cst;  // in the transform type: factor, 1/dx, 1/dz, then 1/dy(iy) at [3 + plane]
   DevScalars* sc;
   int zcols, xrows;
   int plane0, nplanes;
