@@ -55,6 +55,7 @@ struct chgpu_handle {
   double* fac = nullptr;
   double* der = nullptr;
   void* derT = nullptr;
+  void* derL = nullptr;
   void* cst = nullptr;  // transform-type constants: factor, 1/dx, 1/dz, 1/dy per plane
   double* d0lu = nullptr;
   double* yint = nullptr;
@@ -147,6 +148,21 @@ int upload_derT(chgpu_handle* h) {
   return 0;
 }
 
+// der in the linear-term type of buildrhs (double-float in the mixed path,
+// FP64 otherwise), then alfa0, beta0, ni
+template <typename L>
+int upload_derL(chgpu_handle* h) {
+  const std::vector<double>& der = h->tab.der;
+  std::vector<L> t(der.size() + 3);
+  for (size_t i = 0; i < der.size(); ++i) t[i] = from_ld<L>((long double)der[i]);
+  t[der.size()] = from_ld<L>((long double)h->p.alfa0);
+  t[der.size() + 1] = from_ld<L>((long double)h->p.beta0);
+  t[der.size() + 2] = from_ld<L>((long double)h->p.ni);
+  CK(h, cudaMalloc(&h->derL, sizeof(L) * t.size()));
+  CK(h, cudaMemcpy(h->derL, t.data(), sizeof(L) * t.size(), cudaMemcpyHostToDevice));
+  return 0;
+}
+
 template <typename V2>
 int upload_roots(chgpu_handle* h, void** dst, int n) {
   std::vector<V2> w = roots<V2>(n);
@@ -215,6 +231,7 @@ SolveLaunch solve_launch(chgpu_handle* h, const double* ode) {
   L.fac = h->fac;
   L.der = h->der;
   L.derT = h->derT;
+  L.derL = h->derL;
   L.d0lu = h->d0lu;
   L.yint = h->yint;
   L.sc = h->sc;
@@ -314,7 +331,7 @@ void release(chgpu_handle* h) {
     cudaEventDestroy(pe.second.second);
   }
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
-  void* bufs[] = {h->V, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->derT, h->cst, h->d0lu, h->yint, h->dy,
+  void* bufs[] = {h->V, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->derT, h->derL, h->cst, h->d0lu, h->yint, h->dy,
                   h->twz, h->twx, h->twh, h->sc};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -422,16 +439,19 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
       if ((rc = upload_roots<float2>(h, &h->twx, nxd))) break;
       if ((rc = upload_roots<float2>(h, &h->twh, 2 * nxd))) break;
       if ((rc = upload_derT<float>(h))) break;
+      if ((rc = upload_derL<dd>(h))) break;
     } else if (h->prec == CHGPU_FP64DD) {
       if ((rc = upload_roots<cdd>(h, &h->twz, nzd))) break;
       if ((rc = upload_roots<cdd>(h, &h->twx, nxd))) break;
       if ((rc = upload_roots<cdd>(h, &h->twh, 2 * nxd))) break;
       if ((rc = upload_derT<dd>(h))) break;
+      if ((rc = upload_derL<double>(h))) break;
     } else {
       if ((rc = upload_roots<double2>(h, &h->twz, nzd))) break;
       if ((rc = upload_roots<double2>(h, &h->twx, nxd))) break;
       if ((rc = upload_roots<double2>(h, &h->twh, 2 * nxd))) break;
       if ((rc = upload_derT<double>(h))) break;
+      if ((rc = upload_derL<double>(h))) break;
     }
     cudaMemcpy(h->der, t.der.data(), sizeof(double) * t.der.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(h->d0lu, t.d0lu.data(), sizeof(double) * t.d0lu.size(), cudaMemcpyHostToDevice);
@@ -441,6 +461,7 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
     cudaMemset(h->old, 0, ts * 2 * (p->ny - 1) * nmodes);  // oldrhs starts at zero (RK1 has ODE(3)=0)
     DevScalars s{};
     s.deltat = p->deltat;
+    s.rdt = 1.0 / p->deltat;
     s.time = p->time;
     s.meanpx = p->meanpx;
     s.meanpz = p->meanpz;
@@ -508,6 +529,7 @@ int chgpu_start(chgpu_handle* h, double time, double deltat, chgpu_stats* st) {
   s = *h->sc_host;
   s.time = time;
   s.deltat = deltat;
+  s.rdt = 1.0 / deltat;
   s.cfl = 0.0;
   s.istep = 0;
   *h->sc_host = s;

@@ -56,6 +56,7 @@ Radix make_radix(int n);
 // that whole steps (including the CFL-driven time step) run without the host.
 struct DevScalars {
   double deltat;
+  double rdt;  // 1/deltat
   double time;
   double cfl;  // running max over planes (non-negative: ordered as u64 bits)
   double fr[3];

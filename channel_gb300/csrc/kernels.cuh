@@ -63,6 +63,7 @@ struct SolveLaunch {
   double* fac;
   const double* der;
   const void* derT;  // der in the nonlinear-term type, then alfa0, beta0
+  const void* derL;  // der in the linear-term type, then alfa0, beta0, ni
   const double* d0lu;
   const double* yint;
   DevScalars* sc;

@@ -44,9 +44,35 @@ __device__ __forceinline__ size_t vidx(const Dims& d, int c, int iy, int m) {
 // ---------------------------------------------------------------------------
 // buildrhs rows
 // ---------------------------------------------------------------------------
-// History entry from the explicit term in T (x) and the same term in FP64 (e).
-template <typename O2, typename V2> __device__ __forceinline__ O2 hist_store(V2 x, double2 e) { return x; }
-template <> __device__ __forceinline__ double2 hist_store<double2, cdd>(cdd, double2 e) { return e; }
+// Type of the linear terms of the field in buildrhs: FP64, except in the
+// mixed path, where double-float keeps them FP64-accurate (~1e-14) on the
+// FP32 pipes.
+template <typename T> struct LinT { using t = double; };
+template <> struct LinT<float> { using t = dd; };
+
+// real * complex in the linear-term type
+__device__ __forceinline__ double2 lmul(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+__device__ __forceinline__ cdd lmul(dd s, cdd a) { return cdd{s * a.x, s * a.y}; }
+// FP64 field value in the linear-term type
+template <typename LV> __device__ __forceinline__ LV cvt2(double2 v);
+template <> __device__ __forceinline__ double2 cvt2<double2>(double2 v) { return v; }
+template <> __device__ __forceinline__ cdd cvt2<cdd>(double2 v) { return cdd{dd_from_double(v.x), dd_from_double(v.y)}; }
+// explicit-term or history value in the linear-term type
+template <typename L> __device__ __forceinline__ L conv(double x);
+template <typename L> __device__ __forceinline__ L conv(float x);
+template <typename L> __device__ __forceinline__ L conv(dd x);
+template <> __device__ __forceinline__ double conv<double>(double x) { return x; }
+template <> __device__ __forceinline__ double conv<double>(dd x) { return dd_to_double(x); }
+template <> __device__ __forceinline__ dd conv<dd>(float x) { return dd(x); }
+// linear-term value stored in the history type
+template <typename OT> __device__ __forceinline__ OT store_as(double x) { return (OT)x; }
+template <typename OT> __device__ __forceinline__ OT store_as(dd x);
+template <> __device__ __forceinline__ float store_as<float>(dd x) { return __fadd_rn(x.hi, x.lo); }
+
+// History entry from the explicit term in T (x) and the same term in the
+// linear-term type (e).
+template <typename O2, typename V2, typename LV> __device__ __forceinline__ O2 hist_store(V2 x, LV) { return x; }
+template <> __device__ __forceinline__ double2 hist_store<double2, cdd, double2>(cdd, double2 e) { return e; }
 
 // Storage type of the RK history (the explicit term of the previous
 // substep): FP32 in the mixed path, FP64 otherwise.
@@ -56,12 +82,14 @@ template <> struct HistT<dd> { using t = double2; };
 template <typename T>
 __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, const typename C2<T>::t* __restrict__ VV,
                                              typename HistT<T>::t* __restrict__ old, double2* __restrict__ rhs,
-                                             const double* __restrict__ der, const T* __restrict__ derT, Dims d,
-                                             double ode1, double ode2, double ode3,
+                                             const typename LinT<T>::t* __restrict__ derL, const T* __restrict__ derT,
+                                             Dims d, double ode1, double ode2, double ode3,
                                              const DevScalars* __restrict__ sc) {
   using V2 = typename C2<T>::t;
   using O2 = typename HistT<T>::t;
   using OT = decltype(O2::x);
+  using L = typename LinT<T>::t;
+  using LV = typename C2<L>::t;
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   const int iy = blockIdx.y + 1;
   if (m >= d.nmodes) return;
@@ -98,51 +126,55 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
   V2 explv = mul_ia<V2>(ta, mul_ia<V2>(ta, DD(e1, 0)) + DD(e2, 3) + mul_ia<V2>(tb, DD1_6)) +
              mul_ia<V2>(tb, mul_ia<V2>(ta, DD1_6) + DD(e2, 4) + mul_ia<V2>(tb, DD(e1, 2)));
   explv = explv - mk<V2>(tk2 * rhsv.x, tk2 * rhsv.y);
-  const double a = ix * d.alfa0, b = iz * d.beta0;
-  const double k2 = a * a + b * b;
-  const double* dr = der + (size_t)iy * 20;
-  double c0[5], c2[5], c4[5];
+  // ---- linear terms of the field and the RK combination, in L (FP64, or
+  //      double-float in the mixed path: the FP64 pipe is 1/62 of FP32 here) ----
+  const L* drL = derL + (size_t)iy * 20;
+  const size_t tailL = (size_t)(d.ny + 1) * 20;  // then alfa0, beta0, ni
+  const L a = L((float)ix) * derL[tailL], b = L((float)iz) * derL[tailL + 1];
+  const L k2 = a * a + b * b;
+  const L ni = derL[tailL + 2];
+  L c0[5], c2[5], c4[5];
 #pragma unroll
   for (int j = 0; j < 5; ++j) {
-    c0[j] = __ldg(dr + j);
-    c2[j] = __ldg(dr + 10 + j);
-    c4[j] = __ldg(dr + 15 + j);
+    c0[j] = drL[j];
+    c2[j] = drL[10 + j];
+    c4[j] = drL[15 + j];
   }
-  double2 v1[5], v2[5], v3[5];
+  LV v1[5], v2[5], v3[5];
 #pragma unroll
   for (int j = 0; j < 5; ++j) {
-    v1[j] = V[vidx(d, 0, iy - 2 + j, m)];
-    v2[j] = V[vidx(d, 1, iy - 2 + j, m)];
-    v3[j] = V[vidx(d, 2, iy - 2 + j, m)];
+    v1[j] = cvt2<LV>(V[vidx(d, 0, iy - 2 + j, m)]);
+    v2[j] = cvt2<LV>(V[vidx(d, 1, iy - 2 + j, m)]);
+    v3[j] = cvt2<LV>(V[vidx(d, 2, iy - 2 + j, m)]);
   }
-  const double dt = sc->deltat;
-  const double ni = d.ni;
+  const L odt = Num<L>::from_double(ode1 * sc->rdt);  // ODE(1)/deltat
+  const L lode2 = Num<L>::from_double(ode2), lode3 = Num<L>::from_double(ode3);
   const size_t r0 = ((size_t)0 * (d.ny - 1) + (iy - 1)) * d.nmodes + m;  // eta
   const size_t r1 = ((size_t)1 * (d.ny - 1) + (iy - 1)) * d.nmodes + m;  // d2v
   // timescheme (dnsdata.f90:486) for D2v (:647): with S_k = Dk(V2),
   //   unkn = S2 - k2 S0,  impl = sum OS V2 = ni (S4 - 2 k2 S2 + k2^2 S0)
-  const double odt = ode1 * (1.0 / dt);
   {
-    double2 s0 = rmul(c0[0], v2[0]), s2 = rmul(c2[0], v2[0]), s4 = rmul(c4[0], v2[0]);
+    LV s0 = lmul(c0[0], v2[0]), s2 = lmul(c2[0], v2[0]), s4 = lmul(c4[0], v2[0]);
 #pragma unroll
     for (int j = 1; j < 5; ++j) {
-      s0 = s0 + rmul(c0[j], v2[j]);
-      s2 = s2 + rmul(c2[j], v2[j]);
-      s4 = s4 + rmul(c4[j], v2[j]);
+      s0 = s0 + lmul(c0[j], v2[j]);
+      s2 = s2 + lmul(c2[j], v2[j]);
+      s4 = s4 + lmul(c4[j], v2[j]);
     }
-    const double2 unkn = s2 - rmul(k2, s0);
-    const double2 impl = rmul(ni, s4 - rmul(2.0 * k2, s2) + rmul(k2 * k2, s0));
+    const LV unkn = s2 - lmul(k2, s0);
+    const LV impl = lmul(ni, s4 - lmul(k2 + k2, s2) + lmul(k2 * k2, s0));
     const O2 o = old[r1];
-    const double2 e = make_double2(Num<T>::to_double(explv.x), Num<T>::to_double(explv.y));
-    double2 r = rmul(odt, unkn) + impl;
-    r = r + rmul(ode2, e);
-    r = r - rmul(ode3, make_double2((double)o.x, (double)o.y));
+    const LV e = mk<LV>(conv<L>(explv.x), conv<L>(explv.y));
+    LV r = lmul(odt, unkn) + impl;
+    r = r + lmul(lode2, e);
+    r = r - lmul(lode3, mk<LV>(conv<L>(o.x), conv<L>(o.y)));
     old[r1] = hist_store<O2>(explv, e);
-    rhs[r1] = r;
+    rhs[r1] = make_double2(Num<L>::to_double(r.x), Num<L>::to_double(r.y));
   }
   if (ix == 0 && iz == 0) {  // mean flow U + iW (:648-654)
-    const double2 e = make_double2(Num<T>::to_double(rhsu.x) + sc->meanpx, Num<T>::to_double(rhsw.x) + sc->meanpz);
-    double su = c0[0] * v1[0].x, sw = c0[0] * v3[0].x, tu = c2[0] * v1[0].x, tw = c2[0] * v3[0].x;
+    const LV e = mk<LV>(conv<L>(rhsu.x) + Num<L>::from_double(sc->meanpx),
+                        conv<L>(rhsw.x) + Num<L>::from_double(sc->meanpz));
+    L su = c0[0] * v1[0].x, sw = c0[0] * v3[0].x, tu = c2[0] * v1[0].x, tw = c2[0] * v3[0].x;
 #pragma unroll
     for (int j = 1; j < 5; ++j) {
       su = su + c0[j] * v1[j].x;
@@ -150,32 +182,32 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
       tu = tu + c2[j] * v1[j].x;
       tw = tw + c2[j] * v3[j].x;
     }
-    const double2 unkn = make_double2(su, sw);
-    const double2 impl = make_double2(ni * tu, ni * tw);
+    const LV unkn = mk<LV>(su, sw);
+    const LV impl = mk<LV>(ni * tu, ni * tw);
     const O2 o = old[r0];
-    double2 r = rmul(odt, unkn) + impl;
-    r = r + rmul(ode2, e);
-    r = r - rmul(ode3, make_double2((double)o.x, (double)o.y));
-    old[r0] = mk<O2>((OT)e.x, (OT)e.y);
-    rhs[r0] = r;
+    LV r = lmul(odt, unkn) + impl;
+    r = r + lmul(lode2, e);
+    r = r - lmul(lode3, mk<LV>(conv<L>(o.x), conv<L>(o.y)));
+    old[r0] = mk<O2>(store_as<OT>(e.x), store_as<OT>(e.y));
+    rhs[r0] = make_double2(Num<L>::to_double(r.x), Num<L>::to_double(r.y));
   } else {  // eta (:656-661): with w = i kz V1 - i kx V3, unkn = D0(w), impl = ni (D2(w) - k2 D0(w))
     const V2 ee = mul_ia<V2>(tb, rhsu) - mul_ia<V2>(ta, rhsw);
-    double2 w = mul_ia<double2>(b, v1[0]) - mul_ia<double2>(a, v3[0]);
-    double2 s0 = rmul(c0[0], w), s2 = rmul(c2[0], w);
+    LV w = mul_ia<LV>(b, v1[0]) - mul_ia<LV>(a, v3[0]);
+    LV s0 = lmul(c0[0], w), s2 = lmul(c2[0], w);
 #pragma unroll
     for (int j = 1; j < 5; ++j) {
-      w = mul_ia<double2>(b, v1[j]) - mul_ia<double2>(a, v3[j]);
-      s0 = s0 + rmul(c0[j], w);
-      s2 = s2 + rmul(c2[j], w);
+      w = mul_ia<LV>(b, v1[j]) - mul_ia<LV>(a, v3[j]);
+      s0 = s0 + lmul(c0[j], w);
+      s2 = s2 + lmul(c2[j], w);
     }
-    const double2 impl = rmul(ni, s2 - rmul(k2, s0));
+    const LV impl = lmul(ni, s2 - lmul(k2, s0));
     const O2 o = old[r0];
-    const double2 e = make_double2(Num<T>::to_double(ee.x), Num<T>::to_double(ee.y));
-    double2 r = rmul(odt, s0) + impl;
-    r = r + rmul(ode2, e);
-    r = r - rmul(ode3, make_double2((double)o.x, (double)o.y));
+    const LV e = mk<LV>(conv<L>(ee.x), conv<L>(ee.y));
+    LV r = lmul(odt, s0) + impl;
+    r = r + lmul(lode2, e);
+    r = r - lmul(lode3, mk<LV>(conv<L>(o.x), conv<L>(o.y)));
     old[r0] = hist_store<O2>(ee, e);
-    rhs[r0] = r;
+    rhs[r0] = make_double2(Num<L>::to_double(r.x), Num<L>::to_double(r.y));
   }
 }
 
@@ -184,8 +216,9 @@ void launch_rhs(const SolveLaunch& L, cudaStream_t s) {
   using V2 = typename C2<T>::t;
   using O2 = typename HistT<T>::t;
   dim3 grid((L.d.nmodes + 127) / 128, L.d.ny - 1);
-  k_rhs<T><<<grid, 128, 0, s>>>(L.V, (const V2*)L.VV, (O2*)L.old, L.rhs, L.der, (const T*)L.derT, L.d, L.ode[0],
-                                L.ode[1], L.ode[2], L.sc);
+  using LT = typename LinT<T>::t;
+  k_rhs<T><<<grid, 128, 0, s>>>(L.V, (const V2*)L.VV, (O2*)L.old, L.rhs, (const LT*)L.derL, (const T*)L.derT, L.d,
+                                L.ode[0], L.ode[1], L.ode[2], L.sc);
 }
 template void launch_rhs<double>(const SolveLaunch&, cudaStream_t);
 template void launch_rhs<float>(const SolveLaunch&, cudaStream_t);
@@ -580,7 +613,10 @@ void launch_advance_time(DevScalars* sc, double coef, int new_step, cudaStream_t
 __global__ void k_outstats(const double2* __restrict__ V, Dims d, BcRows bc, DevScalars* sc) {
   const double rg = sc->cfl;
   sc->cfl = 0.0;
-  if (d.cflmax > 0) sc->deltat = d.cflmax / rg;
+  if (d.cflmax > 0) {
+    sc->deltat = d.cflmax / rg;
+    sc->rdt = 1.0 / sc->deltat;
+  }
   const int m = d.nz;  // ix=0, iz=0
   const int ny = d.ny;
   double lo1[5], lo3[5], hi1[5], hi3[5];
