@@ -52,6 +52,8 @@ struct chgpu_handle {
   void* Zb = nullptr;
   void* Pb = nullptr;
   double2* rhs = nullptr;
+  double2* F = nullptr;  // body force, plane-major like V
+  bool use_F = false;
   double* fac = nullptr;
   double* der = nullptr;
   void* derT = nullptr;
@@ -228,6 +230,7 @@ SolveLaunch solve_launch(chgpu_handle* h, const double* ode) {
   L.VV = h->VV;
   L.old = h->old;
   L.rhs = h->rhs;
+  L.F = h->use_F ? h->F : nullptr;
   L.fac = h->fac;
   L.der = h->der;
   L.derT = h->derT;
@@ -331,7 +334,7 @@ void release(chgpu_handle* h) {
     cudaEventDestroy(pe.second.second);
   }
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
-  void* bufs[] = {h->V, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->derT, h->derL, h->cst, h->d0lu, h->yint, h->dy,
+  void* bufs[] = {h->V, h->F, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->derT, h->derL, h->cst, h->d0lu, h->yint, h->dy,
                   h->twz, h->twx, h->twh, h->sc};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -665,6 +668,30 @@ int chgpu_kernel_times(chgpu_handle* h, double ms[CHGPU_NKINDS], long long launc
 const char* chgpu_kernel_kind_name(int kind) {
   static const char* names[CHGPU_NKINDS] = {"k_zinv", "k_xrow", "k_zfwd", "k_rhs", "k_linsolve", "scalars"};
   return (kind >= 0 && kind < CHGPU_NKINDS) ? names[kind] : "?";
+}
+
+int chgpu_set_body_force(chgpu_handle* h, const double* F) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "null handle");
+  const bool was = h->use_F;
+  if (!F) {
+    h->use_F = false;
+  } else {
+    const size_t n = (size_t)3 * h->d.nplanes * h->d.nmodes;
+    if (!h->F) CK(h, cudaMalloc((void**)&h->F, sizeof(double2) * n));
+    double2* stage = reinterpret_cast<double2*>(h->Pb);
+    CK(h, cudaMemcpyAsync(stage, F, sizeof(double2) * n, cudaMemcpyHostToDevice, h->stream));
+    launch_transpose(stage, h->F, h->d.nmodes, h->d.nplanes, 3, h->stream);
+    launch_force_ghosts(h->F, h->der, h->d, h->stream);
+    h->launches += 2;
+    CK(h, cudaGetLastError());
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->use_F = true;
+  }
+  if (was != h->use_F && h->graph) {  // the captured step holds the old launch parameters
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  return 0;
 }
 
 int chgpu_stats_reset(chgpu_handle* h) {

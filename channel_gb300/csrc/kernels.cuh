@@ -57,6 +57,7 @@ struct SolveLaunch {
   const void* VV;
   void* old;
   double2* rhs;
+  const double2* F;        // body force (plane-major like V) or null
   const double2* rhs_src;  // where k_linsolve reads its right-hand sides
   size_t rhs_cstride;      // component stride of rhs_src
   int rhs_plane_off;       // row iy lives at plane iy+rhs_plane_off
@@ -78,6 +79,7 @@ void launch_advance_time(DevScalars* sc, double coef, int new_step, cudaStream_t
 void launch_outstats(const SolveLaunch& L, cudaStream_t s);
 void launch_flowrate(const SolveLaunch& L, cudaStream_t s);
 void launch_transpose(const double2* in, double2* out, int rows, int cols, int batch, cudaStream_t s);
+void launch_force_ghosts(double2* F, const double* der, const Dims& d, cudaStream_t s);
 void launch_stats_accumulate(const double2* V, const Dims& d, double* acc, cudaStream_t s);
 
 }  // namespace chgpu

@@ -69,10 +69,6 @@ template <typename OT> __device__ __forceinline__ OT store_as(double x) { return
 template <typename OT> __device__ __forceinline__ OT store_as(dd x);
 template <> __device__ __forceinline__ float store_as<float>(dd x) { return __fadd_rn(x.hi, x.lo); }
 
-// History entry from the explicit term in T (x) and the same term in the
-// linear-term type (e).
-template <typename O2, typename V2, typename LV> __device__ __forceinline__ O2 hist_store(V2 x, LV) { return x; }
-template <> __device__ __forceinline__ double2 hist_store<double2, cdd, double2>(cdd, double2 e) { return e; }
 
 // Storage type of the RK history (the explicit term of the previous
 // substep): FP32 in the mixed path, FP64 otherwise.
@@ -84,7 +80,7 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
                                              typename HistT<T>::t* __restrict__ old, double2* __restrict__ rhs,
                                              const typename LinT<T>::t* __restrict__ derL, const T* __restrict__ derT,
                                              Dims d, double ode1, double ode2, double ode3,
-                                             const DevScalars* __restrict__ sc) {
+                                             const DevScalars* __restrict__ sc, const double2* __restrict__ F) {
   using V2 = typename C2<T>::t;
   using O2 = typename HistT<T>::t;
   using OT = decltype(O2::x);
@@ -140,6 +136,29 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
     c2[j] = drL[10 + j];
     c4[j] = drL[15 + j];
   }
+  // body-force terms (dnsdata.f90:644, 651, 658): fv for the v equation,
+  // fe for eta (or the mean mode's D0 of Re F1, Re F3)
+  LV fv = czero<LV>(), fe = czero<LV>();
+  if (F) {
+    LV D0f1 = czero<LV>(), D0f2 = czero<LV>(), D0f3 = czero<LV>(), D1f1 = czero<LV>(), D1f3 = czero<LV>();
+    L r1 = L(), r3 = L();
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      const L c1 = drL[5 + j];
+      const LV f1 = cvt2<LV>(F[vidx(d, 0, iy - 2 + j, m)]);
+      const LV f2 = cvt2<LV>(F[vidx(d, 1, iy - 2 + j, m)]);
+      const LV f3 = cvt2<LV>(F[vidx(d, 2, iy - 2 + j, m)]);
+      D0f1 = D0f1 + lmul(c0[j], f1);
+      D0f2 = D0f2 + lmul(c0[j], f2);
+      D0f3 = D0f3 + lmul(c0[j], f3);
+      D1f1 = D1f1 + lmul(c1, f1);
+      D1f3 = D1f3 + lmul(c1, f3);
+      r1 = r1 + c0[j] * f1.x;
+      r3 = r3 + c0[j] * f3.x;
+    }
+    fv = czero<LV>() - lmul(k2, D0f2) - mul_ia<LV>(a, D1f1) - mul_ia<LV>(b, D1f3);
+    fe = (ix == 0 && iz == 0) ? mk<LV>(r1, r3) : mul_ia<LV>(b, D0f1) - mul_ia<LV>(a, D0f3);
+  }
   LV v1[5], v2[5], v3[5];
 #pragma unroll
   for (int j = 0; j < 5; ++j) {
@@ -164,16 +183,18 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
     const LV unkn = s2 - lmul(k2, s0);
     const LV impl = lmul(ni, s4 - lmul(k2 + k2, s2) + lmul(k2 * k2, s0));
     const O2 o = old[r1];
-    const LV e = mk<LV>(conv<L>(explv.x), conv<L>(explv.y));
+    LV e = mk<LV>(conv<L>(explv.x), conv<L>(explv.y));
+    if (F) e = e + fv;
     LV r = lmul(odt, unkn) + impl;
     r = r + lmul(lode2, e);
     r = r - lmul(lode3, mk<LV>(conv<L>(o.x), conv<L>(o.y)));
-    old[r1] = hist_store<O2>(explv, e);
+    old[r1] = mk<O2>(store_as<OT>(e.x), store_as<OT>(e.y));
     rhs[r1] = make_double2(Num<L>::to_double(r.x), Num<L>::to_double(r.y));
   }
   if (ix == 0 && iz == 0) {  // mean flow U + iW (:648-654)
-    const LV e = mk<LV>(conv<L>(rhsu.x) + Num<L>::from_double(sc->meanpx),
-                        conv<L>(rhsw.x) + Num<L>::from_double(sc->meanpz));
+    LV e = mk<LV>(conv<L>(rhsu.x) + Num<L>::from_double(sc->meanpx),
+                  conv<L>(rhsw.x) + Num<L>::from_double(sc->meanpz));
+    if (F) e = e + fe;
     L su = c0[0] * v1[0].x, sw = c0[0] * v3[0].x, tu = c2[0] * v1[0].x, tw = c2[0] * v3[0].x;
 #pragma unroll
     for (int j = 1; j < 5; ++j) {
@@ -202,11 +223,12 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
     }
     const LV impl = lmul(ni, s2 - lmul(k2, s0));
     const O2 o = old[r0];
-    const LV e = mk<LV>(conv<L>(ee.x), conv<L>(ee.y));
+    LV e = mk<LV>(conv<L>(ee.x), conv<L>(ee.y));
+    if (F) e = e + fe;
     LV r = lmul(odt, s0) + impl;
     r = r + lmul(lode2, e);
     r = r - lmul(lode3, mk<LV>(conv<L>(o.x), conv<L>(o.y)));
-    old[r0] = hist_store<O2>(ee, e);
+    old[r0] = mk<O2>(store_as<OT>(e.x), store_as<OT>(e.y));
     rhs[r0] = make_double2(Num<L>::to_double(r.x), Num<L>::to_double(r.y));
   }
 }
@@ -218,7 +240,7 @@ void launch_rhs(const SolveLaunch& L, cudaStream_t s) {
   dim3 grid((L.d.nmodes + 127) / 128, L.d.ny - 1);
   using LT = typename LinT<T>::t;
   k_rhs<T><<<grid, 128, 0, s>>>(L.V, (const V2*)L.VV, (O2*)L.old, L.rhs, (const LT*)L.derL, (const T*)L.derT, L.d,
-                                L.ode[0], L.ode[1], L.ode[2], L.sc);
+                                L.ode[0], L.ode[1], L.ode[2], L.sc, L.F);
 }
 template void launch_rhs<double>(const SolveLaunch&, cudaStream_t);
 template void launch_rhs<float>(const SolveLaunch&, cudaStream_t);
@@ -669,6 +691,35 @@ __global__ void k_flowrate(const double2* __restrict__ V, const double* __restri
 }
 
 void launch_flowrate(const SolveLaunch& L, cudaStream_t s) { k_flowrate<<<1, 1, 0, s>>>(L.V, L.yint, L.d, L.sc); }
+
+// ---------------------------------------------------------------------------
+// body-force ghost rows as buildrhs sets them (dnsdata.f90:617-628):
+// F(0)=F(ny)=0, F(-1) = -D4(F)/d4(-2) at iy=1, F(ny+1) = -D4(F)/d4(2) at iy=ny-1
+// ---------------------------------------------------------------------------
+__global__ void k_force_ghosts(double2* __restrict__ F, const double* __restrict__ der, Dims d) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (m >= d.nmodes) return;
+  const int ny = d.ny;
+  F[vidx(d, c, -1, m)] = cz();
+  F[vidx(d, c, 0, m)] = cz();
+  F[vidx(d, c, ny, m)] = cz();
+  F[vidx(d, c, ny + 1, m)] = cz();
+  const double* d4b = der + (size_t)1 * 20 + 15;
+  const double* d4t = der + (size_t)(ny - 1) * 20 + 15;
+  double2 lo[5], hi[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    lo[j] = F[vidx(d, c, -1 + j, m)];
+    hi[j] = F[vidx(d, c, ny - 3 + j, m)];
+  }
+  F[vidx(d, c, -1, m)] = cdivr(cz() - dot5(lo, d4b), d4b[0]);
+  F[vidx(d, c, ny + 1, m)] = cdivr(cz() - dot5(hi, d4t), d4t[4]);
+}
+
+void launch_force_ghosts(double2* F, const double* der, const Dims& d, cudaStream_t s) {
+  k_force_ghosts<<<dim3((d.nmodes + 127) / 128, 3), 128, 0, s>>>(F, der, d);
+}
 
 // ---------------------------------------------------------------------------
 // layout transposes between the restart-file order (y fastest) and the

@@ -74,6 +74,7 @@ SIGNATURES = {
     "chgpu_set_profiling": (C.c_int, [_P, C.c_int]),
     "chgpu_kernel_times": (C.c_int, [_P, _DP, C.POINTER(C.c_longlong)]),
     "chgpu_kernel_kind_name": (C.c_char_p, [C.c_int]),
+    "chgpu_set_body_force": (C.c_int, [_P, _DP]),
     "chgpu_stats_reset": (C.c_int, [_P]),
     "chgpu_stats_accumulate": (C.c_int, [_P]),
     "chgpu_profiles": (C.c_int, [_P, _DP, _DP, C.POINTER(C.c_longlong)]),
@@ -213,6 +214,16 @@ class Channel:
         n = (C.c_longlong * NKINDS)()
         self._check(self.lib.chgpu_kernel_times(self.h, _dp(ms), n))
         return {self.lib.chgpu_kernel_kind_name(k).decode(): (float(ms[k]), int(n[k])) for k in range(NKINDS)}
+
+    def set_body_force(self, F: np.ndarray | None):
+        """Body force in the restart-file layout (None switches it off)."""
+        if F is None:
+            self._check(self.lib.chgpu_set_body_force(self.h, None))
+            return
+        a = np.ascontiguousarray(F, dtype=np.complex128)
+        if a.shape != self.shape:
+            raise ValueError(f"force shape {a.shape} != {self.shape}")
+        self._check(self.lib.chgpu_set_body_force(self.h, _dp(a.view(np.float64))))
 
     def stats_reset(self):
         self._check(self.lib.chgpu_stats_reset(self.h))

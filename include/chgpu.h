@@ -120,6 +120,15 @@ int chgpu_get_stats(chgpu_handle* h, chgpu_stats* st);
  * error flags (non-finite CFL) as CHGPU_E_NONFINITE. */
 int chgpu_synchronize(chgpu_handle* h);
 
+/* Body force F(iy,iz,ix,ic) added to the explicit terms of buildrhs: the
+ * `bodyforce` hook of the reference (dnsdata.f90:617-659), which
+ * set_body_force fills before each buildrhs (channel.f90:129-131).  F has
+ * V's restart-file layout and stays in effect until the next call; NULL
+ * switches the forcing off.  Its ghost rows are rebuilt as buildrhs does
+ * (dnsdata.f90:617-628): F(0) = F(ny) = 0, F(-1) and F(ny+1) such that the
+ * compact fourth derivative of F vanishes at iy = 1 and iy = ny-1. */
+int chgpu_set_body_force(chgpu_handle* h, const double* F);
+
 /* On-device statistics of the field, the mean and variance profiles of the
  * reference's post-processing (postpro/history/var_history.f90:37-84).
  * chgpu_stats_accumulate adds the current field to compensated running sums

@@ -166,6 +166,7 @@ struct orc_state {
   cplx* VV;      /* per plane: [plane][6][ix][iz] truncated spectra */
   cplx* newrhs_eta;
   cplx* newrhs_d2v;
+  cplx* F;       /* body force, V's layout, or NULL */
   double* k2;    /* k2[ix*(2nz+1)+iz+nz] */
   fftplan pz_f, pz_b, px_f, px_b;
   /* module scalars */
@@ -384,13 +385,13 @@ orc_state* orc_create(const orc_params* p, int nthreads) {
   s->dx = PI / (p->alfa0 * s->nxd);
   s->dz = 2.0 * PI / (p->beta0 * s->nzd);
   s->factor = 1.0 / (2.0 * s->nxd * s->nzd);
-  const int ny = s->ny, nx = s->nx, nz = s->nz, nzt = s->nzt;
+  const int ny = p->ny, nx = p->nx, nz = p->nz, nzt = 2 * nz + 1;  /* ny >= 8 checked above */
   /* dnsdata.f90:153-158 */
   s->y = (double*)malloc(sizeof(double) * (size_t)(ny + 3));
   for (int iy = -1; iy <= ny + 1; ++iy)
     s->y[YI(iy)] = p->ymin + 0.5 * (p->ymax - p->ymin) *
                    (tanh(p->a * (2.0 * (double)(float)iy / (double)(float)ny - 1)) / tanh(p->a) + 1);
-  s->dy = (double*)calloc((size_t)(ny + 1), sizeof(double));
+  s->dy = (double*)calloc((size_t)ny + 1, sizeof(double));
   for (int iy = 1; iy <= ny - 1; ++iy) s->dy[iy] = 0.5 * (s->y[YI(iy + 1)] - s->y[YI(iy - 1)]);
   s->k2 = (double*)malloc(sizeof(double) * (size_t)(nx + 1) * nzt);
   for (int ix = 0; ix <= nx; ++ix)
@@ -422,6 +423,7 @@ void orc_destroy(orc_state* s) {
   free(s->y); free(s->dy); free(s->k2); free(s->der); free(s->D0mat);
   free(s->V); free(s->old_eta); free(s->old_d2v); free(s->newrhs_eta); free(s->newrhs_d2v);
   free(s->VV);
+  free(s->F);
   fftplan_free(&s->pz_f); fftplan_free(&s->pz_b); fftplan_free(&s->px_f); fftplan_free(&s->px_b);
   free(s);
 }
@@ -562,6 +564,46 @@ double orc_convolve_plane(orc_state* s, int iy, double* out) {
 /* ------------------------------------------------------------------ */
 /* buildrhs (dnsdata.f90:611-673)                                      */
 /* ------------------------------------------------------------------ */
+#define F_(s, iy, iz, ix, ic) ((s)->F[VIDX(s, iy, iz, ix, ic)])
+
+void orc_set_body_force(orc_state* s, const double* F) {
+  if (!F) {
+    free(s->F);
+    s->F = NULL;
+    return;
+  }
+  if (!s->F) s->F = (cplx*)malloc(sizeof(cplx) * (size_t)orc_field_len(s));
+  memcpy(s->F, F, sizeof(cplx) * (size_t)orc_field_len(s));
+}
+
+/* dnsdata.f90:617-628: F(-1:0)=0, then F(-1) = -D4(F)/d4(-2) at iy=1; same at the top */
+static void body_force_ghosts(orc_state* s) {
+  const int ny = s->ny, nx = s->nx, nz = s->nz;
+  for (int ic = 1; ic <= 3; ++ic)
+    for (int ix = 0; ix <= nx; ++ix)
+      for (int iz = -nz; iz <= nz; ++iz) {
+        F_(s, -1, iz, ix, ic) = 0;
+        F_(s, 0, iz, ix, ic) = 0;
+        F_(s, ny, iz, ix, ic) = 0;
+        F_(s, ny + 1, iz, ix, ic) = 0;
+      }
+  for (int ic = 1; ic <= 3; ++ic)
+    for (int ix = 0; ix <= nx; ++ix)
+      for (int iz = -nz; iz <= nz; ++iz) {
+        cplx f[5];
+        for (int j = 0; j < 5; ++j) f[j] = F_(s, 1 - 2 + j, iz, ix, ic);
+        F_(s, -1, iz, ix, ic) = -csum5(s->der[1].d4, f) / s->der[1].d4[0];
+        for (int j = 0; j < 5; ++j) f[j] = F_(s, ny - 1 - 2 + j, iz, ix, ic);
+        F_(s, ny + 1, iz, ix, ic) = -csum5(s->der[ny - 1].d4, f) / s->der[ny - 1].d4[4];
+      }
+}
+
+static cplx fstencil(const orc_state* s, const double* c, int iy, int iz, int ix, int ic) {
+  cplx f[5];
+  for (int j = 0; j < 5; ++j) f[j] = F_(s, iy - 2 + j, iz, ix, ic);
+  return csum5(c, f);
+}
+
 #define VVP(s, iy, k, ix, iz) \
   ((s)->VV[(((size_t)YI(iy) * 6 + (size_t)((k) - 1)) * ((s)->nx + 1) + (size_t)(ix)) * (s)->nzt + (size_t)((iz) + (s)->nz)])
 
@@ -589,6 +631,7 @@ void orc_buildrhs(orc_state* s, const double ode[3], int compute_cfl) {
     conv_ws_free(&w);
   }
   s->cfl = cflmax;
+  if (s->F) body_force_ghosts(s);
   const double dt = s->deltat, ni = s->p.ni;
   const double meanpx = s->meanpx, meanpz = s->meanpz;
 #pragma omp parallel for num_threads(nthr) schedule(static)
@@ -606,6 +649,9 @@ void orc_buildrhs(orc_state* s, const double ode[3], int compute_cfl) {
         const cplx rhsw = -(cmul(ialfa, DD0_6)) - DD(d1, 5) - cmul(ibeta, DD(d0, 3));
         cplx expl = cmul(ialfa, cmul(ialfa, DD(d1, 1)) + DD(d2, 4) + cmul(ibeta, DD1_6)) +
                     cmul(ibeta, cmul(ialfa, DD1_6) + DD(d2, 5) + cmul(ibeta, DD(d1, 3))) - k2 * rhsv;
+        if (s->F) /* dnsdata.f90:644 */
+          expl = expl - k2 * fstencil(s, d->d0, iy, iz, ix, 2) - cmul(ialfa, fstencil(s, d->d1, iy, iz, ix, 1)) -
+                 cmul(ibeta, fstencil(s, d->d1, iy, iz, ix, 3));
 #undef DD
         cplx v2[5], v1[5], v3[5];
         for (int j = 0; j < 5; ++j) {
@@ -632,6 +678,11 @@ void orc_buildrhs(orc_state* s, const double ode[3], int compute_cfl) {
         }
         if (ix == 0 && iz == 0) { /* dnsdata.f90:648-654 */
           expl = CMPLX(creal(rhsu) + meanpx, creal(rhsw) + meanpz);
+          if (s->F) { /* dnsdata.f90:651: rD0(F,1,3) */
+            double r1[5], r3[5];
+            for (int j = 0; j < 5; ++j) { r1[j] = creal(F_(s, iy - 2 + j, iz, ix, 1)); r3[j] = creal(F_(s, iy - 2 + j, iz, ix, 3)); }
+            expl = expl + CMPLX(sum5(d->d0, r1), sum5(d->d0, r3));
+          }
           double r1[5], r3[5];
           for (int j = 0; j < 5; ++j) { r1[j] = creal(v1[j]); r3[j] = creal(v3[j]); }
           cplx unkn = CMPLX(sum5(d->d0, r1), sum5(d->d0, r3));
@@ -641,6 +692,8 @@ void orc_buildrhs(orc_state* s, const double ode[3], int compute_cfl) {
           s->newrhs_eta[r] = rhs;
         } else { /* dnsdata.f90:655-661 */
           expl = cmul(ibeta, rhsu) - cmul(ialfa, rhsw);
+          if (s->F) /* dnsdata.f90:658 */
+            expl = expl + cmul(ibeta, fstencil(s, d->d0, iy, iz, ix, 1)) - cmul(ialfa, fstencil(s, d->d0, iy, iz, ix, 3));
           cplx unkn = cmul(ibeta, csum5(d->d0, v1)) - cmul(ialfa, csum5(d->d0, v3));
           cplx impl;
           {

@@ -102,6 +102,11 @@ void orc_step(orc_state* s, orc_line* line);
  * initial CFL pass, flow rate and CPI, first outstats line. */
 void orc_start(orc_state* s, orc_line* line);
 
+/* Body force F (bodyforce hook, dnsdata.f90:617-659): F has V's layout;
+ * NULL switches it off.  buildrhs first rebuilds F's ghost rows
+ * (dnsdata.f90:617-628) and adds F's terms to the explicit parts. */
+void orc_set_body_force(orc_state* s, const double* F);
+
 /* COMPLEXderiv followed by LeftLU5divStep2(D0mat) on one y-line
  * (dnsdata.f90:339-373): f0, f1 hold ny+3 complex values (iy=-1..ny+1). */
 void orc_deriv(const orc_state* s, const double* f0, double* f1);

@@ -82,6 +82,7 @@ def lib():
         L.orc_start.argtypes = [P, C.POINTER(Line)]
         L.orc_fft.argtypes = [C.c_int, C.c_int, C.c_int, D]
         L.orc_deriv.argtypes = [P, D, D]
+        L.orc_set_body_force.argtypes = [P, D]
         L.orc_fftfit.restype = C.c_int
         L.orc_fftfit.argtypes = [C.c_int]
         _lib = L
@@ -169,6 +170,14 @@ class Oracle:
         out = np.empty((6, self.p.nx + 1, 2 * self.p.nz + 1), dtype=np.complex128)
         c = lib().orc_convolve_plane(self.h, iy, _dp(out.view(np.float64)))
         return out, c
+
+    def set_body_force(self, F):
+        if F is None:
+            lib().orc_set_body_force(self.h, None)
+            return
+        a = np.ascontiguousarray(F, dtype=np.complex128)
+        assert a.shape == self.shape
+        lib().orc_set_body_force(self.h, _dp(a.view(np.float64)))
 
     def deriv(self, f: np.ndarray) -> np.ndarray:
         """Compact first y-derivative of a complex y-line (iy=-1..ny+1)."""

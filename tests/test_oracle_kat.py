@@ -200,3 +200,38 @@ def test_squire_mode_decay(oracle_mod):
     rate = math.log(amp1 / amp0) / (nsteps * p.deltat)
     sigma = -p.ni * (p.alfa0 ** 2 + (math.pi / 2) ** 2)
     assert abs(rate - sigma) <= 1e-5 * abs(sigma), (rate, sigma)
+
+
+def test_oracle_body_force_ghost_rows_are_rebuilt(oracle_mod):
+    """buildrhs overwrites the forcing's rows iy = -1, 0, ny, ny+1
+    (dnsdata.f90:617-628): values planted there change nothing, a zero force
+    changes nothing, and a force in the interior does."""
+    from channel_gb300 import dnsin, initial
+
+    p = dnsin.workload("small")
+    p.nx, p.ny, p.nz = 8, 20, 8
+    V0 = initial.perturbed_laminar(p, 0.01, 1)
+    ny = p.ny
+    G = np.zeros((3, p.nx + 1, 2 * p.nz + 1, ny + 3), dtype=np.complex128)
+    rng = np.random.default_rng(4)
+    for iy in (-1, 0, ny, ny + 1):
+        G[..., iy + 1] = rng.standard_normal(G.shape[:3]) + 1j * rng.standard_normal(G.shape[:3])
+    out = []
+    for F in (None, np.zeros_like(G), G):
+        o = oracle_mod.Oracle(p)
+        o.set_field(V0)
+        o.set_body_force(F)
+        o.start()
+        o.step()
+        out.append(o.field())
+        o.close()
+    assert np.array_equal(out[0], out[1]) and np.array_equal(out[0], out[2])
+    H = G.copy()
+    H[0, 0, p.nz, 5] = 0.5
+    o = oracle_mod.Oracle(p)
+    o.set_field(V0)
+    o.set_body_force(H)
+    o.start()
+    o.step()
+    assert not np.array_equal(o.field(), out[0])
+    o.close()
