@@ -374,7 +374,8 @@ static void setup_boundary_conditions(orc_state* s) {
 }
 
 orc_state* orc_create(const orc_params* p, int nthreads) {
-  if (p->ny < 8 || p->nx < 1 || p->nz < 1) return NULL;
+  const int ny = p->ny, nx = p->nx, nz = p->nz, nzt = 2 * nz + 1;
+  if (ny < 8 || nx < 1 || nz < 1) return NULL;
   orc_state* s = (orc_state*)calloc(1, sizeof(orc_state));
   s->p = *p;
   s->nx = p->nx; s->ny = p->ny; s->nz = p->nz;
@@ -385,7 +386,6 @@ orc_state* orc_create(const orc_params* p, int nthreads) {
   s->dx = PI / (p->alfa0 * s->nxd);
   s->dz = 2.0 * PI / (p->beta0 * s->nzd);
   s->factor = 1.0 / (2.0 * s->nxd * s->nzd);
-  const int ny = p->ny, nx = p->nx, nz = p->nz, nzt = 2 * nz + 1;  /* ny >= 8 checked above */
   /* dnsdata.f90:153-158 */
   s->y = (double*)malloc(sizeof(double) * (size_t)(ny + 3));
   for (int iy = -1; iy <= ny + 1; ++iy)
