@@ -19,10 +19,11 @@ CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libchgpu.so"
 DRIVER = OUT / "channel_gb300"
+OUT2BIN = OUT / "out2bin"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", str(ROOT / "include")]
-SOURCES = ["capi.cu", "conv.cu", "solve.cu", "setup.cpp", "noalloc.cu", "stats.cu"]
+SOURCES = ["capi.cu", "conv.cu", "solve.cu", "setup.cpp", "noalloc.cu", "stats.cu", "export.cu"]
 
 
 def nvcc() -> str:
@@ -68,10 +69,16 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
                     print(out, file=sys.stderr)
     if force or _stale(LIB, objs):
         _run([nv, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"])
-    drv_src = CSRC / "driver.cpp"
-    if drv_src.exists() and (force or _stale(DRIVER, [drv_src, LIB, ROOT / "include" / "chgpu.h"])):
-        _run(["g++", "-O2", "-std=c++17", "-pthread", "-I", str(ROOT / "include"), str(drv_src), "-o", str(DRIVER),
-              f"-L{OUT}", "-lchgpu", f"-Wl,-rpath,{OUT}"])
+    # host programs over the C ABI: the driver (channel.f90) and the exporter (out2bin.f90)
+    host_jobs = []
+    for src, exe in (("driver.cpp", DRIVER), ("out2bin.cpp", OUT2BIN)):
+        s = CSRC / src
+        if force or _stale(exe, [s, LIB, CSRC / "hostio.h", ROOT / "include" / "chgpu.h"]):
+            host_jobs.append(["g++", "-O2", "-std=c++17", "-pthread", "-I", str(ROOT / "include"), str(s), "-o",
+                              str(exe), f"-L{OUT}", "-lchgpu", f"-Wl,-rpath,{OUT}"])
+    if host_jobs:
+        with cf.ThreadPoolExecutor(max_workers=len(host_jobs)) as ex:
+            list(ex.map(_run, host_jobs))
     return LIB
 
 

@@ -78,6 +78,15 @@ struct chgpu_handle {
   cudaStream_t snap_stream = nullptr;
   cudaEvent_t snap_read = nullptr, snap_done = nullptr;
   bool snap_pending = false;
+  // physical-space export: per-chunk work buffers and root tables
+  double2* ex_W = nullptr;
+  double* ex_P = nullptr;
+  double* ex_out = nullptr;
+  double2* ex_twz = nullptr;
+  double2* ex_twx = nullptr;
+  size_t ex_out_cap = 0;  // doubles
+  int ex_chunk = 0, ex_zcols = 0, ex_xpairs = 0;
+  RadixDev ex_rz{}, ex_rx{};
   // per-kernel timing
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -335,7 +344,7 @@ void release(chgpu_handle* h) {
   }
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   void* bufs[] = {h->V, h->F, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->derT, h->derL, h->cst, h->d0lu, h->yint, h->dy,
-                  h->twz, h->twx, h->twh, h->sc};
+                  h->twz, h->twx, h->twh, h->sc, h->ex_W, h->ex_P, h->ex_out, h->ex_twz, h->ex_twx};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (h->sc_host) cudaFreeHost(h->sc_host);
@@ -668,6 +677,122 @@ int chgpu_kernel_times(chgpu_handle* h, double ms[CHGPU_NKINDS], long long launc
 const char* chgpu_kernel_kind_name(int kind) {
   static const char* names[CHGPU_NKINDS] = {"k_zinv", "k_xrow", "k_zfwd", "k_rhs", "k_linsolve", "scalars"};
   return (kind >= 0 && kind < CHGPU_NKINDS) ? names[kind] : "?";
+}
+
+// ---------------------------------------------------------------------------
+// physical-space export (out_exporter/out2bin.f90)
+// ---------------------------------------------------------------------------
+namespace {
+
+int fortran_nint(float x) { return x >= 0.f ? (int)std::floor(x + 0.5f) : -(int)std::floor(-x + 0.5f); }
+
+// out2bin.f90:76-78: nint(xcent_undersample * (2n+1)) with the product in real*4
+int export_len(int n, float undersample) {
+  volatile float prod = undersample * (float)(2 * n + 1);
+  return fortran_nint(prod);
+}
+
+RadixDev prime_radices(int n) {
+  RadixDev r{};
+  r.n = n;
+  int m = n;
+  for (int p = 2; m > 1; ++p) {
+    if ((long long)p * p > m) p = m;
+    while (m % p == 0) {
+      r.r[r.nst++] = p;
+      m /= p;
+    }
+  }
+  return r;
+}
+
+int export_setup(chgpu_handle* h) {
+  if (h->ex_W) return 0;
+  const int Nx = 2 * h->d.nx + 1, Nz = 2 * h->d.nz + 1;
+  const int lim = export_set_smem_limits();
+  if (lim <= 0) return fail(h, CHGPU_E_CUDA, "export: shared-memory limits");
+  h->ex_zcols = 8;
+  while (h->ex_zcols > 1 && export_z_smem(h->ex_zcols, Nz) > (size_t)lim) --h->ex_zcols;
+  h->ex_xpairs = 4;
+  while (h->ex_xpairs > 1 && export_x_smem(h->ex_xpairs, h->d.nx, Nx) > (size_t)lim) --h->ex_xpairs;
+  if (export_z_smem(h->ex_zcols, Nz) > (size_t)lim || export_x_smem(h->ex_xpairs, h->d.nx, Nx) > (size_t)lim)
+    return fail(h, CHGPU_E_PARAM, "export: 2nx+1 or 2nz+1 too long for one transform in shared memory");
+  h->ex_rz = prime_radices(Nz);
+  h->ex_rx = prime_radices(Nx);
+  // planes per chunk: W and P of a chunk within 256 MiB
+  const size_t per_plane = (size_t)3 * (h->d.nx + 1) * Nz * sizeof(double2) + (size_t)3 * Nz * Nx * sizeof(double);
+  h->ex_chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)h->d.ny + 1, (1ull << 28) / per_plane));
+  CK(h, cudaMalloc((void**)&h->ex_W, (size_t)3 * h->ex_chunk * (h->d.nx + 1) * Nz * sizeof(double2)));
+  CK(h, cudaMalloc((void**)&h->ex_P, (size_t)3 * h->ex_chunk * Nz * Nx * sizeof(double)));
+  const std::vector<double2> wz = roots<double2>(Nz), wx = roots<double2>(Nx);
+  CK(h, cudaMalloc((void**)&h->ex_twz, sizeof(double2) * Nz));
+  CK(h, cudaMalloc((void**)&h->ex_twx, sizeof(double2) * Nx));
+  CK(h, cudaMemcpy(h->ex_twz, wz.data(), sizeof(double2) * Nz, cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(h->ex_twx, wx.data(), sizeof(double2) * Nx, cudaMemcpyHostToDevice));
+  return 0;
+}
+
+}  // namespace
+
+int chgpu_export_dims(const chgpu_handle* h, float undersample, int dims[3]) {
+  if (!h || !dims || !(undersample > 0.f)) return CHGPU_E_PARAM;
+  dims[0] = export_len(h->d.nx, undersample);
+  dims[1] = h->d.ny + 1;
+  dims[2] = export_len(h->d.nz, undersample);
+  return (dims[0] >= 1 && dims[2] >= 1) ? 0 : CHGPU_E_PARAM;
+}
+
+int chgpu_export_physical(chgpu_handle* h, const chgpu_export_opts* o, double* out) {
+  if (!h || !out) return fail(h, CHGPU_E_PARAM, "chgpu_export_physical: null argument");
+  chgpu_export_opts opt{0, CHGPU_EXPORT_ALL, 0, 1.0f};
+  if (o) opt = *o;
+  int dims[3];
+  if (chgpu_export_dims(h, opt.undersample, dims) != 0)
+    return fail(h, CHGPU_E_PARAM, "chgpu_export_physical: undersample factor gives an empty grid");
+  if (opt.part < CHGPU_EXPORT_ALL || opt.part > CHGPU_EXPORT_SMALL)
+    return fail(h, CHGPU_E_PARAM, "chgpu_export_physical: part must be CHGPU_EXPORT_ALL, _LARGE or _SMALL");
+  if (!h->field_set) return fail(h, CHGPU_E_STATE, "chgpu_export_physical: no field uploaded");
+  if (int rc = export_setup(h)) return rc;
+  const int nxtot = dims[0], nytot = dims[1], nztot = dims[2];
+  const size_t need = (size_t)nztot * h->ex_chunk * nxtot * 3;
+  if (need > h->ex_out_cap) {
+    if (h->ex_out) CK(h, cudaFree(h->ex_out));
+    h->ex_out = nullptr;
+    h->ex_out_cap = 0;
+    CK(h, cudaMalloc((void**)&h->ex_out, need * sizeof(double)));
+    h->ex_out_cap = need;
+  }
+  ExportLaunch L{};
+  L.V = h->V;
+  L.d = h->d;
+  L.W = h->ex_W;
+  L.P = h->ex_P;
+  L.out = h->ex_out;
+  L.twz = h->ex_twz;
+  L.twx = h->ex_twx;
+  L.rz = h->ex_rz;
+  L.rx = h->ex_rx;
+  L.zcols = h->ex_zcols;
+  L.xpairs = h->ex_xpairs;
+  L.chunk = h->ex_chunk;
+  L.nxtot = nxtot;
+  L.nztot = nztot;
+  L.fluct_only = opt.fluct_only ? 1 : 0;
+  L.part = opt.part;
+  L.z_threshold = opt.z_threshold;
+  L.beta0 = h->p.beta0;
+  const size_t row = (size_t)nxtot * 3 * sizeof(double);
+  for (int iy0 = 0; iy0 < nytot; iy0 += h->ex_chunk) {
+    const int nc = std::min(h->ex_chunk, nytot - iy0);
+    launch_export_chunk(L, iy0, nc, h->stream);
+    h->launches += 3;
+    CK(h, cudaGetLastError());
+    // [zz][iy][xx][c]: the chunk's planes are one strided block per zz
+    CK(h, cudaMemcpy2DAsync(out + (size_t)iy0 * nxtot * 3, row * nytot, h->ex_out, row * nc, row * nc, nztot,
+                            cudaMemcpyDeviceToHost, h->stream));
+  }
+  CK(h, cudaStreamSynchronize(h->stream));
+  return 0;
 }
 
 int chgpu_set_body_force(chgpu_handle* h, const double* F) {

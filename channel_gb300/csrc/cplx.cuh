@@ -29,13 +29,16 @@ template <typename V> __device__ __forceinline__ V mul_i(V a, int sign) {
   return sign > 0 ? mk<V>(-a.y, a.x) : mk<V>(a.y, -a.x);
 }
 
-// x / d and x % d for 0 <= x, x*d < 2^32 by a multiply-high (integer
-// division by a value unknown at compile time costs tens of instructions).
+// x / d for 0 <= x, x*d < 2^32 by a multiply-high (integer division by a
+// value unknown at compile time costs tens of instructions).  magic =
+// floor((2^32-1)/d) + 1 over-estimates the quotient by at most one, which the
+// final compare removes; d = 1 (magic would be 2^32) is taken apart.
 struct FastDiv {
   int d;
   unsigned magic;
-  __device__ __forceinline__ explicit FastDiv(int dv) : d(dv), magic(0xFFFFFFFFu / (unsigned)dv + 1u) {}
+  __device__ __forceinline__ explicit FastDiv(int dv) : d(dv), magic(dv > 1 ? 0xFFFFFFFFu / (unsigned)dv + 1u : 0u) {}
   __device__ __forceinline__ int div(int x) const {
+    if (magic == 0u) return x;
     int q = (int)__umulhi((unsigned)x, magic);
     return (q * d > x) ? q - 1 : q;
   }

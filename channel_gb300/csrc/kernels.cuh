@@ -79,6 +79,25 @@ void launch_advance_time(DevScalars* sc, double coef, int new_step, cudaStream_t
 void launch_outstats(const SolveLaunch& L, cudaStream_t s);
 void launch_flowrate(const SolveLaunch& L, cudaStream_t s);
 void launch_transpose(const double2* in, double2* out, int rows, int cols, int batch, cudaStream_t s);
+// physical-space export (export.cu)
+struct ExportLaunch {
+  const double2* V;
+  Dims d;
+  double2* W;    // z-transformed planes of a chunk: [3][chunk][nx+1][Nz]
+  double* P;     // physical planes of a chunk: [3][chunk][Nz][Nx]
+  double* out;   // sampled output of a chunk: [nztot][planes of the chunk][nxtot][3]
+  const double2* twz;  // forward roots of Nz = 2nz+1
+  const double2* twx;  // forward roots of Nx = 2nx+1
+  RadixDev rz, rx;     // prime factors of Nz and Nx
+  int zcols, xpairs, chunk;
+  int nxtot, nztot;
+  int fluct_only, part, z_threshold;
+  double beta0;
+};
+size_t export_z_smem(int zcols, int Nz);
+size_t export_x_smem(int xpairs, int nx, int Nx);
+int export_set_smem_limits();  // dynamic shared memory allowed per block, or -1
+void launch_export_chunk(const ExportLaunch& L, int iy0, int nplanes_chunk, cudaStream_t s);
 void launch_force_ghosts(double2* F, const double* der, const Dims& d, cudaStream_t s);
 void launch_stats_accumulate(const double2* V, const Dims& d, double* acc, cudaStream_t s);
 

@@ -268,15 +268,6 @@ __device__ __forceinline__ AsmCoef asm_coef(double lambda, double k2, double ni)
   c.ce2 = -ni;
   return c;
 }
-__device__ __forceinline__ void assemble(const double* __restrict__ dr, const AsmCoef& c, double Dv[5], double De[5]) {
-#pragma unroll
-  for (int j = 0; j < 5; ++j) {
-    const double d0 = __ldg(dr + j), d2 = __ldg(dr + 10 + j), d4 = __ldg(dr + 15 + j);
-    Dv[j] = c.cv4 * d4 + c.cv2 * d2 + c.cv0 * d0;
-    De[j] = c.ce0 * d0 + c.ce2 * d2;
-  }
-}
-
 // applybc_n rows ny-1 / ny-2 and applybc_0 rows 1 / 2 (dnsdata.f90:458-472)
 __device__ __forceinline__ void bc_top1(double A[5], const double* bcn, const double* bcnp1) {
   double e = A[4];

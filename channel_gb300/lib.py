@@ -52,6 +52,12 @@ class Stats(C.Structure):
 
 
 # name -> (restype, argtypes), one per declaration in include/chgpu.h
+class ExportOpts(C.Structure):
+    _fields_ = [("fluct_only", C.c_int), ("part", C.c_int), ("z_threshold", C.c_int), ("undersample", C.c_float)]
+
+
+EXPORT_PART = {"all": 0, "large": 1, "small": 2}
+
 _P = C.c_void_p
 _DP = C.POINTER(C.c_double)
 SIGNATURES = {
@@ -75,6 +81,8 @@ SIGNATURES = {
     "chgpu_kernel_times": (C.c_int, [_P, _DP, C.POINTER(C.c_longlong)]),
     "chgpu_kernel_kind_name": (C.c_char_p, [C.c_int]),
     "chgpu_set_body_force": (C.c_int, [_P, _DP]),
+    "chgpu_export_dims": (C.c_int, [_P, C.c_float, C.POINTER(C.c_int)]),
+    "chgpu_export_physical": (C.c_int, [_P, C.POINTER(ExportOpts), _DP]),
     "chgpu_stats_reset": (C.c_int, [_P]),
     "chgpu_stats_accumulate": (C.c_int, [_P]),
     "chgpu_profiles": (C.c_int, [_P, _DP, _DP, C.POINTER(C.c_longlong)]),
@@ -214,6 +222,22 @@ class Channel:
         n = (C.c_longlong * NKINDS)()
         self._check(self.lib.chgpu_kernel_times(self.h, _dp(ms), n))
         return {self.lib.chgpu_kernel_kind_name(k).decode(): (float(ms[k]), int(n[k])) for k in range(NKINDS)}
+
+    def export_dims(self, undersample: float = 1.0) -> tuple[int, int, int]:
+        d = (C.c_int * 3)()
+        self._check(self.lib.chgpu_export_dims(self.h, undersample, d))
+        return d[0], d[1], d[2]
+
+    def export_physical(self, fluct_only: bool = False, part: str = "all", z_threshold: int = 0,
+                        undersample: float = 1.0) -> np.ndarray:
+        """The current field in physical space as the exporter writes it:
+        vec(3, nxtot, 0:ny, nztot) in Fortran order = an array
+        [nztot][ny+1][nxtot][3]."""
+        nxtot, nytot, nztot = self.export_dims(undersample)
+        out = np.empty((nztot, nytot, nxtot, 3))
+        o = ExportOpts(int(bool(fluct_only)), EXPORT_PART[part], int(z_threshold), undersample)
+        self._check(self.lib.chgpu_export_physical(self.h, C.byref(o), _dp(out)))
+        return out
 
     def set_body_force(self, F: np.ndarray | None):
         """Body force in the restart-file layout (None switches it off)."""

@@ -120,6 +120,31 @@ int chgpu_get_stats(chgpu_handle* h, chgpu_stats* st);
  * error flags (non-finite CFL) as CHGPU_E_NONFINITE. */
 int chgpu_synchronize(chgpu_handle* h);
 
+/* Physical-space export of the field: the reference's exporter
+ * out_exporter/out2bin.f90 (convert_outfile :141-203, xz_interpolation
+ * :236-275, undersampled_to_fullindex :279-299, filter_vfield :338-347) on
+ * the handle's current field.  Planes iy = 0..ny go through the
+ * un-dealiased inverse transform on the (2nx+1) x (2nz+1) grid and are
+ * sampled on nxtot x nztot points (nint(undersample * (2n+1)), :76-78).
+ * `out` (host) receives vec(3, nxtot, 0:ny, nztot) in Fortran order, i.e.
+ * the C array out[nztot][ny+1][nxtot][3] -- the body of the .bin file that
+ * write_brutal_bin writes (:207-232).  Sample indices past the last grid
+ * point (undersample factors whose grid does not divide the period) wrap
+ * to the first point of the periodic domain. */
+#define CHGPU_EXPORT_ALL 0
+#define CHGPU_EXPORT_LARGE 1 /* -l: large scales, modes with |beta0 kz| <= z_threshold kept */
+#define CHGPU_EXPORT_SMALL 2 /* -s: small scales, modes with |beta0 kz| > z_threshold kept */
+typedef struct chgpu_export_opts {
+  int fluct_only;    /* -f: the mean mode (kx, kz) = (0, 0) removed */
+  int part;          /* CHGPU_EXPORT_ALL, _LARGE or _SMALL */
+  int z_threshold;   /* largesmall_settings.in (an integer, as read there) */
+  float undersample; /* -u factor (real*4 in the reference); 1 = full grid */
+} chgpu_export_opts;
+/* dims = {nxtot, ny+1, nztot} for this factor; CHGPU_E_PARAM when empty. */
+int chgpu_export_dims(const chgpu_handle* h, float undersample, int dims[3]);
+/* opts NULL = defaults (full field, full grid). */
+int chgpu_export_physical(chgpu_handle* h, const chgpu_export_opts* opts, double* out);
+
 /* Body force F(iy,iz,ix,ic) added to the explicit terms of buildrhs: the
  * `bodyforce` hook of the reference (dnsdata.f90:617-659), which
  * set_body_force fills before each buildrhs (channel.f90:129-131).  F has
