@@ -8,7 +8,8 @@ MODULE chgpu_interface
   USE, INTRINSIC :: iso_c_binding
   IMPLICIT NONE
 
-  INTEGER(C_INT), PARAMETER :: CHGPU_FP64 = 0, CHGPU_MIXED = 1
+  INTEGER(C_INT), PARAMETER :: CHGPU_FP64 = 0, CHGPU_MIXED = 1, CHGPU_FP64DD = 2
+  INTEGER(C_INT), PARAMETER :: CHGPU_EXPORT_ALL = 0, CHGPU_EXPORT_LARGE = 1, CHGPU_EXPORT_SMALL = 2
 
   ! Mirrors chgpu_params field by field (C layout).
   TYPE, BIND(C) :: chgpu_params
@@ -37,6 +38,12 @@ MODULE chgpu_interface
     REAL(C_DOUBLE)       :: cfl, deltat, time
     INTEGER(C_LONG_LONG) :: istep
   END TYPE chgpu_stats
+
+  ! Mirrors chgpu_export_opts (out2bin's -f, -l/-s, z_threshold, -u).
+  TYPE, BIND(C) :: chgpu_export_opts
+    INTEGER(C_INT)       :: fluct_only, part, z_threshold
+    REAL(C_FLOAT)        :: undersample
+  END TYPE chgpu_export_opts
 
   INTERFACE
     INTEGER(C_INT) FUNCTION chgpu_create(p, h) BIND(C, name="chgpu_create")
@@ -90,6 +97,55 @@ MODULE chgpu_interface
       IMPORT :: C_INT, C_PTR, chgpu_stats
       TYPE(C_PTR), VALUE :: h
       TYPE(chgpu_stats), INTENT(OUT) :: st
+    END FUNCTION
+    ! bodyforce hook: F(-1:ny+1,-nz:nz,0:nx,1:3) like V; pass C_NULL_PTR via
+    ! chgpu_clear_body_force below to switch it off
+    INTEGER(C_INT) FUNCTION chgpu_set_body_force(h, F) BIND(C, name="chgpu_set_body_force")
+      IMPORT :: C_INT, C_PTR, C_DOUBLE_COMPLEX
+      TYPE(C_PTR), VALUE :: h
+      COMPLEX(C_DOUBLE_COMPLEX), INTENT(IN) :: F(*)
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION chgpu_clear_body_force(h, nullF) BIND(C, name="chgpu_set_body_force")
+      IMPORT :: C_INT, C_PTR
+      TYPE(C_PTR), VALUE :: h, nullF
+    END FUNCTION
+    ! asynchronous snapshot: start the copy, later get a pointer to the host copy
+    INTEGER(C_INT) FUNCTION chgpu_snapshot_async(h) BIND(C, name="chgpu_snapshot_async")
+      IMPORT :: C_INT, C_PTR
+      TYPE(C_PTR), VALUE :: h
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION chgpu_snapshot_wait(h, V) BIND(C, name="chgpu_snapshot_wait")
+      IMPORT :: C_INT, C_PTR
+      TYPE(C_PTR), VALUE :: h
+      TYPE(C_PTR), INTENT(OUT) :: V
+    END FUNCTION
+    ! mean and variance profiles (var_history.f90) accumulated on the device
+    INTEGER(C_INT) FUNCTION chgpu_stats_reset(h) BIND(C, name="chgpu_stats_reset")
+      IMPORT :: C_INT, C_PTR
+      TYPE(C_PTR), VALUE :: h
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION chgpu_stats_accumulate(h) BIND(C, name="chgpu_stats_accumulate")
+      IMPORT :: C_INT, C_PTR
+      TYPE(C_PTR), VALUE :: h
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION chgpu_profiles(h, mean, var, nsamples) BIND(C, name="chgpu_profiles")
+      IMPORT :: C_INT, C_PTR, C_DOUBLE, C_LONG_LONG
+      TYPE(C_PTR), VALUE :: h
+      REAL(C_DOUBLE), INTENT(OUT) :: mean(*), var(*)
+      INTEGER(C_LONG_LONG), INTENT(OUT) :: nsamples
+    END FUNCTION
+    ! out2bin: vec(3,nxtot,0:ny,nztot) of the current field
+    INTEGER(C_INT) FUNCTION chgpu_export_dims(h, undersample, dims) BIND(C, name="chgpu_export_dims")
+      IMPORT :: C_INT, C_PTR, C_FLOAT
+      TYPE(C_PTR), VALUE :: h
+      REAL(C_FLOAT), VALUE :: undersample
+      INTEGER(C_INT), INTENT(OUT) :: dims(3)
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION chgpu_export_physical(h, opts, vec) BIND(C, name="chgpu_export_physical")
+      IMPORT :: C_INT, C_PTR, C_DOUBLE, chgpu_export_opts
+      TYPE(C_PTR), VALUE :: h
+      TYPE(chgpu_export_opts), INTENT(IN) :: opts
+      REAL(C_DOUBLE), INTENT(OUT) :: vec(*)
     END FUNCTION
     TYPE(C_PTR) FUNCTION chgpu_last_error(h) BIND(C, name="chgpu_last_error")
       IMPORT :: C_PTR
