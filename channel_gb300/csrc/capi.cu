@@ -44,6 +44,8 @@ struct chgpu_handle {
   RadixDev rz{}, rx{};
   int prec = CHGPU_FP64;  // CHGPU_FP64, CHGPU_MIXED or CHGPU_FP64DD
   int zcols = 1, xrows = 1;
+  int xminb = 2;  // register-cap variant of the x-row kernel
+  bool tuned = false;
   cudaStream_t stream = nullptr;
   // device buffers
   double2* V = nullptr;
@@ -174,6 +176,39 @@ int upload_derL(chgpu_handle* h) {
   return 0;
 }
 
+// per-stage twiddles of a radix plan (the layout stockham_stage reads):
+// stage st at twoff[st], R-1 values w_{Ns R}^{r k} (r = 1..R-1) per k < Ns
+void set_twiddle_offsets(RadixDev& r) {
+  int Ns = 1, off = 0;
+  for (int st = 0; st < r.nst; ++st) {
+    r.twoff[st] = off;
+    off += Ns * (r.r[st] - 1);
+    Ns *= r.r[st];
+  }
+}
+
+template <typename V2>
+int upload_stage_twiddles(chgpu_handle* h, void** dst, const RadixDev& rad) {
+  using T = decltype(V2::x);
+  std::vector<V2> w(std::max(1, rad.n));
+  int Ns = 1;
+  for (int st = 0; st < rad.nst; ++st) {
+    const int R = rad.r[st];
+    for (int k = 0; k < Ns; ++k)
+      for (int r = 1; r < R; ++r) {
+        const long double ang = 2.0L * 3.14159265358979323846264338327950288L * (long double)(r * k) /
+                                (long double)(Ns * R);
+        V2& e = w[rad.twoff[st] + k * (R - 1) + r - 1];
+        e.x = from_ld<T>(cosl(ang));
+        e.y = from_ld<T>(-sinl(ang));
+      }
+    Ns *= R;
+  }
+  CK(h, cudaMalloc(dst, sizeof(V2) * w.size()));
+  CK(h, cudaMemcpy(*dst, w.data(), sizeof(V2) * w.size(), cudaMemcpyHostToDevice));
+  return 0;
+}
+
 template <typename V2>
 int upload_roots(chgpu_handle* h, void** dst, int n) {
   std::vector<V2> w = roots<V2>(n);
@@ -224,6 +259,7 @@ ConvLaunch conv_launch(chgpu_handle* h, int compute_cfl, int products, int plane
   L.sc = h->sc;
   L.zcols = h->zcols;
   L.xrows = h->xrows;
+  L.xminb = h->xminb;
   L.plane0 = plane0;
   L.nplanes = nplanes;
   L.compute_cfl = compute_cfl;
@@ -408,14 +444,21 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
   if (rz.nst < 0 || rx.nst < 0) { delete h; return fail(nullptr, CHGPU_E_PARAM, "unsupported FFT length"); }
   h->rz.n = rz.n; h->rz.nst = rz.nst; std::memcpy(h->rz.r, rz.r, sizeof rz.r);
   h->rx.n = rx.n; h->rx.nst = rx.nst; std::memcpy(h->rx.r, rx.r, sizeof rx.r);
+  set_twiddle_offsets(h->rz);
+  set_twiddle_offsets(h->rx);
   // tiles: columns per z-transform block and rows per x block, from the
   // shared-memory budget (two ping-pong buffers; nine row buffers)
   const size_t ts = tsize(h);
-  h->zcols = (int)std::max<size_t>(1, std::min<size_t>(8, (100 * 1024) / (2 * (size_t)nzd * ts)));
+  h->zcols = 8;
+  while (h->zcols > 1 && conv_z_smem(h->zcols, nzd, ts) > 100 * 1024) --h->zcols;
+  // rows per x block: the most that keep two resident blocks per SM (228 KB
+  // of shared memory per SM, 1 KB reserved per block); chgpu_autotune may
+  // choose otherwise by timing
+  const size_t xbudget = 233472 / 2 - 1024 - 512;
   h->xrows = 1;
-  while (h->xrows < 4 && 9 * (size_t)(2 * h->xrows) * nxd * ts <= 200 * 1024 && nzd % (2 * h->xrows) == 0)
+  while (h->xrows < 4 && conv_x_smem(2 * h->xrows, nxd, ts) <= xbudget && nzd % (2 * h->xrows) == 0)
     h->xrows *= 2;
-  if (9 * (size_t)h->xrows * nxd * ts > 227 * 1024 || 2 * (size_t)nzd * ts > 227 * 1024) {
+  if (conv_x_smem(h->xrows, nxd, ts) > 227 * 1024 || conv_z_smem(1, nzd, ts) > 227 * 1024) {
     delete h;
     return fail(nullptr, CHGPU_E_PARAM, "transform length too large for one thread block");
   }
@@ -447,20 +490,20 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
     e = cudaMallocHost((void**)&h->sc_host, sizeof(DevScalars));
     if (e != cudaSuccess) { rc = cuda_fail(h, e, "cudaMallocHost"); break; }
     if (h->prec == CHGPU_MIXED) {
-      if ((rc = upload_roots<float2>(h, &h->twz, nzd))) break;
-      if ((rc = upload_roots<float2>(h, &h->twx, nxd))) break;
+      if ((rc = upload_stage_twiddles<float2>(h, &h->twz, h->rz))) break;
+      if ((rc = upload_stage_twiddles<float2>(h, &h->twx, h->rx))) break;
       if ((rc = upload_roots<float2>(h, &h->twh, 2 * nxd))) break;
       if ((rc = upload_derT<float>(h))) break;
       if ((rc = upload_derL<dd>(h))) break;
     } else if (h->prec == CHGPU_FP64DD) {
-      if ((rc = upload_roots<cdd>(h, &h->twz, nzd))) break;
-      if ((rc = upload_roots<cdd>(h, &h->twx, nxd))) break;
+      if ((rc = upload_stage_twiddles<cdd>(h, &h->twz, h->rz))) break;
+      if ((rc = upload_stage_twiddles<cdd>(h, &h->twx, h->rx))) break;
       if ((rc = upload_roots<cdd>(h, &h->twh, 2 * nxd))) break;
       if ((rc = upload_derT<dd>(h))) break;
       if ((rc = upload_derL<double>(h))) break;
     } else {
-      if ((rc = upload_roots<double2>(h, &h->twz, nzd))) break;
-      if ((rc = upload_roots<double2>(h, &h->twx, nxd))) break;
+      if ((rc = upload_stage_twiddles<double2>(h, &h->twz, h->rz))) break;
+      if ((rc = upload_stage_twiddles<double2>(h, &h->twx, h->rx))) break;
       if ((rc = upload_roots<double2>(h, &h->twh, 2 * nxd))) break;
       if ((rc = upload_derT<double>(h))) break;
       if ((rc = upload_derL<double>(h))) break;
@@ -677,6 +720,117 @@ int chgpu_kernel_times(chgpu_handle* h, double ms[CHGPU_NKINDS], long long launc
 const char* chgpu_kernel_kind_name(int kind) {
   static const char* names[CHGPU_NKINDS] = {"k_zinv", "k_xrow", "k_zfwd", "k_rhs", "k_linsolve", "scalars"};
   return (kind >= 0 && kind < CHGPU_NKINDS) ? names[kind] : "?";
+}
+
+// ---------------------------------------------------------------------------
+// autotuner of the transform tiles
+// ---------------------------------------------------------------------------
+namespace {
+
+// average device time of `reps` launches of one convolution stage over all
+// planes with the handle's current tiles (after one untimed launch)
+int time_conv_stage(chgpu_handle* h, int stage, int reps, float* ms) {
+  ConvLaunch L = conv_launch(h, 0, 1, 0, h->d.nplanes);
+  auto launch = [&] {
+    if (h->prec == CHGPU_MIXED) launch_convolutions<float>(L, h->stream, stage);
+    else if (h->prec == CHGPU_FP64DD) launch_convolutions<dd>(L, h->stream, stage);
+    else launch_convolutions<double>(L, h->stream, stage);
+  };
+  cudaEvent_t a = take_event(h), b = take_event(h);
+  launch();
+  CK(h, cudaEventRecord(a, h->stream));
+  for (int i = 0; i < reps; ++i) launch();
+  CK(h, cudaEventRecord(b, h->stream));
+  CK(h, cudaGetLastError());
+  CK(h, cudaEventSynchronize(b));
+  CK(h, cudaEventElapsedTime(ms, a, b));
+  *ms /= (float)reps;
+  h->ev_pool.push_back(a);
+  h->ev_pool.push_back(b);
+  h->launches += reps + 1;
+  return 0;
+}
+
+}  // namespace
+
+int chgpu_autotune(chgpu_handle* h) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "null handle");
+  int dev = 0, optin = 0;
+  CK(h, cudaGetDevice(&dev));
+  CK(h, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const size_t ts = tsize(h), lim = (size_t)optin - 1024;
+  const int nzd = h->d.nzd, nxd = h->d.nxd;
+  const int reps = 2;
+  float ms = 0;
+  // valid spectra in the work buffers before timing the later stages
+  if (int rc = time_conv_stage(h, 0, 1, &ms)) return rc;
+  if (int rc = time_conv_stage(h, 1, 1, &ms)) return rc;
+  // columns per block of the two z-transform kernels
+  int best_z = h->zcols;
+  float best = 1e30f;
+  for (int zc = 1; zc <= 8; zc *= 2) {
+    if (conv_z_smem(zc, nzd, ts) > lim) break;
+    h->zcols = zc;
+    float m0 = 0, m2 = 0;
+    if (int rc = time_conv_stage(h, 0, reps, &m0)) return rc;
+    if (int rc = time_conv_stage(h, 2, reps, &m2)) return rc;
+    if (m0 + m2 < best) {
+      best = m0 + m2;
+      best_z = zc;
+    }
+  }
+  h->zcols = best_z;
+  // rows per block and register-cap variant of the x-row kernel
+  int best_r = h->xrows, best_b = h->xminb;
+  best = 1e30f;
+  for (int xb = 1; xb <= 3; ++xb)
+    for (int xr = 1; xr <= 4; xr *= 2) {
+      if (nzd % xr != 0 || conv_x_smem(xr, nxd, ts) > lim) continue;
+      h->xrows = xr;
+      h->xminb = xb;
+      if (int rc = time_conv_stage(h, 1, reps, &ms)) return rc;
+      if (ms < best) {
+        best = ms;
+        best_r = xr;
+        best_b = xb;
+      }
+    }
+  h->xrows = best_r;
+  h->xminb = best_b;
+  h->tuned = true;
+  if (h->graph) {  // the captured step holds the old launch shapes
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  return 0;
+}
+
+int chgpu_set_tiles(chgpu_handle* h, const int tiles[3]) {
+  if (!h || !tiles) return fail(h, CHGPU_E_PARAM, "chgpu_set_tiles: null argument");
+  int dev = 0, optin = 0;
+  CK(h, cudaGetDevice(&dev));
+  CK(h, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const size_t ts = tsize(h), lim = (size_t)optin - 1024;
+  const int zc = tiles[0], xr = tiles[1], xb = tiles[2];
+  if (zc < 1 || zc > 8 || conv_z_smem(zc, h->d.nzd, ts) > lim || (xr != 1 && xr != 2 && xr != 4) ||
+      h->d.nzd % xr != 0 || conv_x_smem(xr, h->d.nxd, ts) > lim || xb < 1 || xb > 3)
+    return fail(h, CHGPU_E_PARAM, "chgpu_set_tiles: tiles outside what this handle's sizes allow");
+  h->zcols = zc;
+  h->xrows = xr;
+  h->xminb = xb;
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  return 0;
+}
+
+int chgpu_tiles(const chgpu_handle* h, int tiles[3]) {
+  if (!h || !tiles) return CHGPU_E_PARAM;
+  tiles[0] = h->zcols;
+  tiles[1] = h->xrows;
+  tiles[2] = h->xminb;
+  return 0;
 }
 
 // ---------------------------------------------------------------------------

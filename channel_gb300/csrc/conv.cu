@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(256) k_zinv(const double2* __restrict__ V, typ
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nzd = d.nzd, nz = d.nz, nxp = d.nx + 1;
   V2* bufA = reinterpret_cast<V2*>(smem_raw);
-  V2* bufB = bufA + (size_t)nb_cols * nzd;
+  V2* bufB = bufA + pad32_size(nb_cols * nzd);
   const int c = blockIdx.z;
   const int plane = plane0 + blockIdx.y;
   const int ix0 = blockIdx.x * nb_cols;
@@ -51,15 +51,12 @@ __global__ void __launch_bounds__(256) k_zinv(const double2* __restrict__ V, typ
       double2 x = V[(colbase + ix0 + b) * d.nzt + izp];
       val = mk<V2>(Num<T>::from_double(x.x), Num<T>::from_double(x.y));
     }
-    bufA[idx] = val;
+    bufA[pad32(idx)] = val;
   }
   __syncthreads();
-  V2* res = fft_block<V2>(bufA, bufB, nb, rz, +1, twz);
-  for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) {
-    const int b = by_nzd.div(idx);
-    const int jz = idx - b * nzd;
-    Zb[(colbase + ix0 + b) * nzd + jz] = res[idx];
-  }
+  V2* res = fft_block<+1>(bufA, bufB, nb, rz, twz);
+  V2* out = Zb + (colbase + ix0) * nzd;
+  for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) out[idx] = res[pad32(idx)];
 }
 
 __device__ __forceinline__ void block_max_atomic(double v, double* target) {
@@ -76,8 +73,10 @@ __device__ __forceinline__ void block_max_atomic(double v, double* target) {
   }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) k_xrow(const typename C2<T>::t* __restrict__ Zb, typename C2<T>::t* __restrict__ Pb,
+// MINB: resident 256-thread blocks per SM the register allocation is capped
+// for (the autotuner picks the variant and the rows per block together)
+template <typename T, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_xrow(const typename C2<T>::t* __restrict__ Zb, typename C2<T>::t* __restrict__ Pb,
                                               const typename C2<T>::t* __restrict__ twx,
                                               const typename C2<T>::t* __restrict__ twh, const T* __restrict__ cst,
                                               Dims d, RadixDev rx, int nrows, int plane0, int compute_cfl,
@@ -91,8 +90,8 @@ __global__ void __launch_bounds__(256) k_xrow(const typename C2<T>::t* __restric
   const int lgr = __ffs(nrows) - 1;  // nrows is 1, 2 or 4
   const FastDiv by_M(M), by_nxp(nxp);
   V2* A = reinterpret_cast<V2*>(smem_raw);
-  V2* B = A + S;
-  V2* Cb = B + S;
+  V2* B = A + pad32_size(S);
+  V2* Cb = B + pad32_size(S);
   // load the three spectra rows (zTOx, x zero band; dnsdata.f90:533-535)
   for (int idx = threadIdx.x; idx < 3 * M * nrows; idx += blockDim.x) {
     const int r = idx & (nrows - 1);
@@ -101,23 +100,22 @@ __global__ void __launch_bounds__(256) k_xrow(const typename C2<T>::t* __restric
     const int k = ck - c * M;
     V2 val = czero<V2>();
     if (k <= nx) val = Zb[(((size_t)c * d.nplanes + plane) * nxp + k) * nzd + jz0 + r];
-    Cb[((size_t)c * nrows + r) * M + k] = val;
+    Cb[pad32((c * nrows + r) * M + k)] = val;
   }
   __syncthreads();
   // c2r packing: Z[k] = (X[k]+conj(X[M-k])) + i (X[k]-conj(X[M-k])) e^{+i pi k/M}
   for (int idx = threadIdx.x; idx < S; idx += blockDim.x) {
     const int cr = by_M.div(idx);
     const int k = idx - cr * M;
-    const V2* X = Cb + (size_t)cr * M;
-    V2 xk = X[k];
+    V2 xk = Cb[pad32(cr * M + k)];
     V2 xm = czero<V2>();
     if (k == 0) xk.y = T();  // the c2r reads only Re of the kx=0 entry
-    else xm = conjg(X[M - k]);
-    V2 e = xk + xm, o = cmul(xk - xm, conjg(twh[k]));
-    A[idx] = e + mul_i(o, +1);
+    else xm = conjg(Cb[pad32(cr * M + M - k)]);
+    V2 e = xk + xm, o = cmul_s<+1>(xk - xm, twh[k]);
+    A[pad32(idx)] = e + mul_is<+1>(o);
   }
   __syncthreads();
-  V2* U = fft_block<V2>(A, B, 3 * nrows, rx, +1, twx);
+  V2* U = fft_block<+1>(A, B, 3 * nrows, rx, twx);
   V2* freeb = (U == A) ? B : A;
   // CFL (dnsdata.f90:552-556) and products uu,vv,ww (:584)
   const T f = cst[0];
@@ -128,9 +126,9 @@ __global__ void __launch_bounds__(256) k_xrow(const typename C2<T>::t* __restric
   const T rdy = do_cfl ? cst[3 + plane] : T();
   for (int idx = threadIdx.x; idx < nrows * M; idx += blockDim.x) {
     const int r = by_M.div(idx), m = idx - r * M;
-    V2 u = U[((size_t)0 * nrows + r) * M + m];
-    V2 v = U[((size_t)1 * nrows + r) * M + m];
-    V2 w = U[((size_t)2 * nrows + r) * M + m];
+    V2 u = U[pad32((0 * nrows + r) * M + m)];
+    V2 v = U[pad32((1 * nrows + r) * M + m)];
+    V2 w = U[pad32((2 * nrows + r) * M + m)];
     if (do_cfl) {
       using N = Num<T>;
       T c0 = N::abs(u.x) * rdx + N::abs(v.x) * rdy + N::abs(w.x) * rdz;
@@ -138,9 +136,9 @@ __global__ void __launch_bounds__(256) k_xrow(const typename C2<T>::t* __restric
       cfl = N::max(cfl, N::max(c0, c1));
       bad = bad || !N::finite(c0) || !N::finite(c1);
     }
-    Cb[((size_t)0 * nrows + r) * M + m] = mk<V2>(u.x * u.x * f, u.y * u.y * f);
-    Cb[((size_t)1 * nrows + r) * M + m] = mk<V2>(v.x * v.x * f, v.y * v.y * f);
-    Cb[((size_t)2 * nrows + r) * M + m] = mk<V2>(w.x * w.x * f, w.y * w.y * f);
+    Cb[pad32((0 * nrows + r) * M + m)] = mk<V2>(u.x * u.x * f, u.y * u.y * f);
+    Cb[pad32((1 * nrows + r) * M + m)] = mk<V2>(v.x * v.x * f, v.y * v.y * f);
+    Cb[pad32((2 * nrows + r) * M + m)] = mk<V2>(w.x * w.x * f, w.y * w.y * f);
   }
   if (bad) cfl = T((float)INFINITY);  // a non-finite velocity shows up as an infinite CFL
   if (compute_cfl) block_max_atomic(Num<T>::to_double(cfl), &sc->cfl);
@@ -149,25 +147,25 @@ __global__ void __launch_bounds__(256) k_xrow(const typename C2<T>::t* __restric
     if (half == 1) {  // products uv, vw, uw (dnsdata.f90:581-583)
       for (int idx = threadIdx.x; idx < nrows * M; idx += blockDim.x) {
         const int r = by_M.div(idx), m = idx - r * M;
-        V2 u = U[((size_t)0 * nrows + r) * M + m];
-        V2 v = U[((size_t)1 * nrows + r) * M + m];
-        V2 w = U[((size_t)2 * nrows + r) * M + m];
-        Cb[((size_t)0 * nrows + r) * M + m] = mk<V2>(u.x * v.x * f, u.y * v.y * f);
-        Cb[((size_t)1 * nrows + r) * M + m] = mk<V2>(v.x * w.x * f, v.y * w.y * f);
-        Cb[((size_t)2 * nrows + r) * M + m] = mk<V2>(u.x * w.x * f, u.y * w.y * f);
+        V2 u = U[pad32((0 * nrows + r) * M + m)];
+        V2 v = U[pad32((1 * nrows + r) * M + m)];
+        V2 w = U[pad32((2 * nrows + r) * M + m)];
+        Cb[pad32((0 * nrows + r) * M + m)] = mk<V2>(u.x * v.x * f, u.y * v.y * f);
+        Cb[pad32((1 * nrows + r) * M + m)] = mk<V2>(v.x * w.x * f, v.y * w.y * f);
+        Cb[pad32((2 * nrows + r) * M + m)] = mk<V2>(u.x * w.x * f, u.y * w.y * f);
       }
       __syncthreads();
     }
-    V2* P = fft_block<V2>(Cb, freeb, 3 * nrows, rx, -1, twx);
+    V2* P = fft_block<-1>(Cb, freeb, 3 * nrows, rx, twx);
     // r2c unpacking, kx = 0..nx (HFT + xTOz, dnsdata.f90:586-588)
     for (int idx = threadIdx.x; idx < 3 * nxp * nrows; idx += blockDim.x) {
       const int r = idx & (nrows - 1);
       const int pk = idx >> lgr;
       const int p = by_nxp.div(pk);
       const int k = pk - p * nxp;
-      const V2* Z = P + ((size_t)p * nrows + r) * M;
-      V2 zk = Z[k];
-      V2 zm = conjg(Z[k == 0 ? 0 : M - k]);
+      const int zb = (p * nrows + r) * M;
+      V2 zk = P[pad32(zb + k)];
+      V2 zm = conjg(P[pad32(zb + (k == 0 ? 0 : M - k))]);
       V2 e = scale(zk + zm, T(0.5f));
       V2 df = zk - zm;
       V2 o = mk<V2>(df.y * T(0.5f), -df.x * T(0.5f));
@@ -191,24 +189,28 @@ __global__ void __launch_bounds__(256) k_zfwd(const typename C2<T>::t* __restric
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nzd = d.nzd, nz = d.nz, nxp = d.nx + 1, nzt = d.nzt;
   V2* bufA = reinterpret_cast<V2*>(smem_raw);
-  V2* bufB = bufA + (size_t)nb_cols * nzd;
+  V2* bufB = bufA + pad32_size(nb_cols * nzd);
   const int p = blockIdx.z;
   const int plane = plane0 + blockIdx.y;
   const int ix0 = blockIdx.x * nb_cols;
   const int nb = min(nb_cols, nxp - ix0);
   const size_t colbase = ((size_t)p * d.nplanes + plane) * nxp;
-  for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) bufA[idx] = Pb[(colbase + ix0) * nzd + idx];
+  const V2* in = Pb + (colbase + ix0) * nzd;
+  for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) bufA[pad32(idx)] = in[idx];
   __syncthreads();
-  V2* res = fft_block<V2>(bufA, bufB, nb, rz, -1, twz);
+  V2* res = fft_block<-1>(bufA, bufB, nb, rz, twz);
   const FastDiv by_nzt(nzt);
   for (int idx = threadIdx.x; idx < nb * nzt; idx += blockDim.x) {
     const int b = by_nzt.div(idx);
     const int izp = idx - b * nzt;
     const int iz = izp - nz;
     const int jz = iz >= 0 ? iz : nzd + iz;
-    VV[(colbase + ix0 + b) * nzt + izp] = res[(size_t)b * nzd + jz];
+    VV[(colbase + ix0 + b) * nzt + izp] = res[pad32(b * nzd + jz)];
   }
 }
+
+size_t conv_z_smem(int zcols, int nzd, size_t ts) { return 2 * (size_t)pad32_size(zcols * nzd) * ts; }
+size_t conv_x_smem(int xrows, int nxd, size_t ts) { return 3 * (size_t)pad32_size(3 * xrows * nxd) * ts; }
 
 template <typename T>
 void launch_convolutions(const ConvLaunch& L, cudaStream_t s, int stage) {
@@ -217,18 +219,19 @@ void launch_convolutions(const ConvLaunch& L, cudaStream_t s, int stage) {
   const int nxp = d.nx + 1;
   if (stage == 0) {
     dim3 grid((nxp + L.zcols - 1) / L.zcols, L.nplanes, 3);
-    size_t sm = 2 * (size_t)L.zcols * d.nzd * sizeof(V2);
+    size_t sm = conv_z_smem(L.zcols, d.nzd, sizeof(V2));
     k_zinv<T><<<grid, 256, sm, s>>>(L.V, (V2*)L.Zb, (const V2*)L.twz, d, L.rz, L.zcols, L.plane0);
   }
   if (stage == 1) {
     dim3 grid(d.nzd / L.xrows, L.nplanes);
-    size_t sm = 9 * (size_t)L.xrows * d.nxd * sizeof(V2);
-    k_xrow<T><<<grid, 256, sm, s>>>((const V2*)L.Zb, (V2*)L.Pb, (const V2*)L.twx, (const V2*)L.twh, (const T*)L.cst, d, L.rx,
-                                    L.xrows, L.plane0, L.compute_cfl, L.sc);
+    size_t sm = conv_x_smem(L.xrows, d.nxd, sizeof(V2));
+    auto kern = L.xminb == 1 ? k_xrow<T, 1> : L.xminb == 3 ? k_xrow<T, 3> : k_xrow<T, 2>;
+    kern<<<grid, 256, sm, s>>>((const V2*)L.Zb, (V2*)L.Pb, (const V2*)L.twx, (const V2*)L.twh, (const T*)L.cst, d, L.rx,
+                               L.xrows, L.plane0, L.compute_cfl, L.sc);
   }
   if (stage == 2) {
     dim3 grid((nxp + L.zcols - 1) / L.zcols, L.nplanes, 6);
-    size_t sm = 2 * (size_t)L.zcols * d.nzd * sizeof(V2);
+    size_t sm = conv_z_smem(L.zcols, d.nzd, sizeof(V2));
     k_zfwd<T><<<grid, 256, sm, s>>>((const V2*)L.Pb, (V2*)L.VV, (const V2*)L.twz, d, L.rz, L.zcols, L.plane0);
   }
 }
@@ -255,13 +258,19 @@ cudaError_t conv_set_smem_limits() {
   if (e != cudaSuccess) return e;
   if ((e = allow_max_smem(k_zinv<double>, optin))) return e;
   if ((e = allow_max_smem(k_zinv<float>, optin))) return e;
-  if ((e = allow_max_smem(k_xrow<double>, optin))) return e;
-  if ((e = allow_max_smem(k_xrow<float>, optin))) return e;
+  if ((e = allow_max_smem(k_zinv<dd>, optin))) return e;
   if ((e = allow_max_smem(k_zfwd<double>, optin))) return e;
   if ((e = allow_max_smem(k_zfwd<float>, optin))) return e;
-  if ((e = allow_max_smem(k_zinv<dd>, optin))) return e;
-  if ((e = allow_max_smem(k_xrow<dd>, optin))) return e;
-  return allow_max_smem(k_zfwd<dd>, optin);
+  if ((e = allow_max_smem(k_zfwd<dd>, optin))) return e;
+  if ((e = allow_max_smem(k_xrow<double, 1>, optin))) return e;
+  if ((e = allow_max_smem(k_xrow<double, 2>, optin))) return e;
+  if ((e = allow_max_smem(k_xrow<double, 3>, optin))) return e;
+  if ((e = allow_max_smem(k_xrow<float, 1>, optin))) return e;
+  if ((e = allow_max_smem(k_xrow<float, 2>, optin))) return e;
+  if ((e = allow_max_smem(k_xrow<float, 3>, optin))) return e;
+  if ((e = allow_max_smem(k_xrow<dd, 1>, optin))) return e;
+  if ((e = allow_max_smem(k_xrow<dd, 2>, optin))) return e;
+  return allow_max_smem(k_xrow<dd, 3>, optin);
 }
 
 }  // namespace chgpu

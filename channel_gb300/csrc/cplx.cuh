@@ -24,10 +24,6 @@ template <typename V> __device__ __forceinline__ V cmul(V a, V b) {
 template <typename V> __device__ __forceinline__ V conjg(V a) { return mk<V>(a.x, -a.y); }
 template <typename V> __device__ __forceinline__ V czero() { return mk<V>(decltype(V::x)(), decltype(V::x)()); }
 template <typename V> __device__ __forceinline__ V scale(V a, decltype(V::x) s) { return mk<V>(a.x * s, a.y * s); }
-// a * (sign * i)
-template <typename V> __device__ __forceinline__ V mul_i(V a, int sign) {
-  return sign > 0 ? mk<V>(-a.y, a.x) : mk<V>(a.y, -a.x);
-}
 
 // x / d for 0 <= x, x*d < 2^32 by a multiply-high (integer division by a
 // value unknown at compile time costs tens of instructions).  magic =
@@ -46,16 +42,37 @@ struct FastDiv {
 
 // Radix plan passed by value to kernels: radices 16, then one of 8/4/2, then
 // 3 (lengths 2^a 3^b, b <= 1), so every stride before the last stage is a
-// power of two.
+// power of two.  twoff[st] is the offset of stage st's twiddles in the
+// per-length table (see stockham_stage).
 struct RadixDev {
   int n, nst;
   int r[24];
+  int twoff[24];
 };
 
-// In-register DFTs of length R (natural order in and out), sign -1: exp(-i),
+// Shared-memory index with one pad slot per 32 elements: the stores of a
+// Stockham stage with small Ns run at stride R, which without padding puts a
+// whole warp on one bank; with it every warp access needs only the minimum
+// number of wavefronts for 8- and 16-byte elements.
+__device__ __forceinline__ int pad32(int i) { return i + (i >> 5); }
+__host__ __device__ constexpr int pad32_size(int n) { return n + (n >> 5) + 1; }
+
+// a * (SIGN * i)
+template <int SIGN, typename V> __device__ __forceinline__ V mul_is(V a) {
+  return SIGN > 0 ? mk<V>(-a.y, a.x) : mk<V>(a.y, -a.x);
+}
+// a * w (SIGN < 0) or a * conj(w) (SIGN > 0): the tables hold forward roots
+template <int SIGN, typename V> __device__ __forceinline__ V cmul_s(V a, V w) {
+  return SIGN < 0 ? cmul(a, w) : mk<V>(a.x * w.x + a.y * w.y, a.y * w.x - a.x * w.y);
+}
+template <int SIGN> __device__ __forceinline__ cdd cmul_s(cdd a, cdd w) {
+  return SIGN < 0 ? cmul(a, w) : cdd{dd_dot2(a.x, w.x, a.y, w.y), dd_dot2(a.y, w.x, -a.x, w.y)};
+}
+
+// In-register DFTs of length R (natural order in and out), SIGN -1: exp(-i),
 // +1: exp(+i).  Internal twiddles are constants of the type.
-template <typename V> __device__ __forceinline__ void dft4(V& a0, V& a1, V& a2, V& a3, int sign) {
-  const V t0 = a0 + a2, t1 = a0 - a2, t2 = a1 + a3, t3 = mul_i(a1 - a3, sign);
+template <int SIGN, typename V> __device__ __forceinline__ void dft4(V& a0, V& a1, V& a2, V& a3) {
+  const V t0 = a0 + a2, t1 = a0 - a2, t2 = a1 + a3, t3 = mul_is<SIGN>(a1 - a3);
   a0 = t0 + t2;
   a1 = t1 + t3;
   a2 = t0 - t2;
@@ -64,36 +81,36 @@ template <typename V> __device__ __forceinline__ void dft4(V& a0, V& a1, V& a2, 
 
 template <int R, typename V> struct Dft;
 template <typename V> struct Dft<2, V> {
-  __device__ static void run(V* a, int) {
+  template <int SIGN> __device__ static void run(V* a) {
     const V t = a[0] - a[1];
     a[0] = a[0] + a[1];
     a[1] = t;
   }
 };
 template <typename V> struct Dft<3, V> {
-  __device__ static void run(V* a, int sign) {
+  template <int SIGN> __device__ static void run(V* a) {
     using T = decltype(V::x);
     const V t1 = a[1] + a[2];
     const V t2 = a[0] - scale(t1, T(0.5f));
-    const V t3 = mul_i(scale(a[1] - a[2], Num<T>::sqrt3_2()), sign);
+    const V t3 = mul_is<SIGN>(scale(a[1] - a[2], Num<T>::sqrt3_2()));
     a[0] = a[0] + t1;
     a[1] = t2 + t3;
     a[2] = t2 - t3;
   }
 };
 template <typename V> struct Dft<4, V> {
-  __device__ static void run(V* a, int sign) { dft4(a[0], a[1], a[2], a[3], sign); }
+  template <int SIGN> __device__ static void run(V* a) { dft4<SIGN>(a[0], a[1], a[2], a[3]); }
 };
 template <typename V> struct Dft<8, V> {
   // r = 2 r1 + r2, k = k1 + 4 k2: DFT4 over r1, twiddle w8^(r2 k1), DFT2 over r2
-  __device__ static void run(V* a, int sign) {
+  template <int SIGN> __device__ static void run(V* a) {
     using T = decltype(V::x);
     const T r2 = Num<T>::sqrt1_2();
-    const T sr2 = sign > 0 ? r2 : -r2;
-    dft4(a[0], a[2], a[4], a[6], sign);
-    dft4(a[1], a[3], a[5], a[7], sign);
+    const T sr2 = SIGN > 0 ? r2 : -r2;
+    dft4<SIGN>(a[0], a[2], a[4], a[6]);
+    dft4<SIGN>(a[1], a[3], a[5], a[7]);
     a[3] = cmul(a[3], mk<V>(r2, sr2));   // w8^1
-    a[5] = mul_i(a[5], sign);            // w8^2
+    a[5] = mul_is<SIGN>(a[5]);           // w8^2
     a[7] = cmul(a[7], mk<V>(-r2, sr2));  // w8^3
     V y[8];
 #pragma unroll
@@ -107,27 +124,27 @@ template <typename V> struct Dft<8, V> {
 };
 template <typename V> struct Dft<16, V> {
   // r = 4 r1 + r2, k = k1 + 4 k2: DFT4 over r1, twiddle w16^(r2 k1), DFT4 over r2
-  __device__ static void run(V* a, int sign) {
+  template <int SIGN> __device__ static void run(V* a) {
     using T = decltype(V::x);
     const T c = Num<T>::cos_pi8(), s = Num<T>::sin_pi8(), r2 = Num<T>::sqrt1_2();
-    const T ss = sign > 0 ? s : -s, sc = sign > 0 ? c : -c, sr2 = sign > 0 ? r2 : -r2;
+    const T ss = SIGN > 0 ? s : -s, sc = SIGN > 0 ? c : -c, sr2 = SIGN > 0 ? r2 : -r2;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) dft4(a[q], a[q + 4], a[q + 8], a[q + 12], sign);
+    for (int q = 0; q < 4; ++q) dft4<SIGN>(a[q], a[q + 4], a[q + 8], a[q + 12]);
     // b[r2][k1] sits in a[r2 + 4 k1]
-    a[1 + 4] = cmul(a[1 + 4], mk<V>(c, ss));     // w^1
-    a[1 + 8] = cmul(a[1 + 8], mk<V>(r2, sr2));   // w^2
-    a[1 + 12] = cmul(a[1 + 12], mk<V>(s, sc));   // w^3
-    a[2 + 4] = cmul(a[2 + 4], mk<V>(r2, sr2));   // w^2
-    a[2 + 8] = mul_i(a[2 + 8], sign);            // w^4
+    a[1 + 4] = cmul(a[1 + 4], mk<V>(c, ss));      // w^1
+    a[1 + 8] = cmul(a[1 + 8], mk<V>(r2, sr2));    // w^2
+    a[1 + 12] = cmul(a[1 + 12], mk<V>(s, sc));    // w^3
+    a[2 + 4] = cmul(a[2 + 4], mk<V>(r2, sr2));    // w^2
+    a[2 + 8] = mul_is<SIGN>(a[2 + 8]);            // w^4
     a[2 + 12] = cmul(a[2 + 12], mk<V>(-r2, sr2));  // w^6
-    a[3 + 4] = cmul(a[3 + 4], mk<V>(s, sc));     // w^3
-    a[3 + 8] = cmul(a[3 + 8], mk<V>(-r2, sr2));  // w^6
+    a[3 + 4] = cmul(a[3 + 4], mk<V>(s, sc));      // w^3
+    a[3 + 8] = cmul(a[3 + 8], mk<V>(-r2, sr2));   // w^6
     a[3 + 12] = cmul(a[3 + 12], mk<V>(-c, -ss));  // w^9
     V y[16];
 #pragma unroll
     for (int k1 = 0; k1 < 4; ++k1) {
       V b0 = a[4 * k1], b1 = a[4 * k1 + 1], b2 = a[4 * k1 + 2], b3 = a[4 * k1 + 3];
-      dft4(b0, b1, b2, b3, sign);
+      dft4<SIGN>(b0, b1, b2, b3);
       y[k1] = b0;
       y[k1 + 4] = b1;
       y[k1 + 8] = b2;
@@ -138,57 +155,64 @@ template <typename V> struct Dft<16, V> {
   }
 };
 
+// read-only load of a complex value of any of the three types
+template <typename V> __device__ __forceinline__ V ldg_v(const V* p) { return __ldg(p); }
+template <> __device__ __forceinline__ cdd ldg_v<cdd>(const cdd* p) {
+  const float4 f = __ldg(reinterpret_cast<const float4*>(p));
+  return cdd{dd(f.x, f.y), dd(f.z, f.w)};
+}
+
 // One Stockham stage (Govindaraju et al. 2008 formulation) with radix R over
-// B transforms of length n: item j of a transform reads R points at stride
-// n/R, twiddles them by w_{Ns R}^{r k} (k = j mod Ns), transforms them in
-// registers and writes them at stride Ns.  Ns is a power of two.
-template <int R, typename V>
+// B transforms of length n held in padded shared memory (pad32): item j of
+// a transform reads R points at stride n/R, twiddles them by
+// w_{Ns R}^{r k} (k = j mod Ns), transforms them in registers and writes
+// them at stride Ns.  Ns is a power of two.  twst holds this stage's forward
+// twiddles, R-1 consecutive values per k (twst[k (R-1) + r-1]), so one item
+// reads one contiguous run.
+template <int R, int SIGN, typename V>
 __device__ __forceinline__ void stockham_stage(const V* __restrict__ src, V* __restrict__ dst, int B, int n, int Ns,
-                                               int sign, const V* __restrict__ tw) {
+                                               const V* __restrict__ twst) {
   const int nb = n / R;
   const int total = B * nb;
-  const int twstep = n / (Ns * R);
   const FastDiv by_nb(nb);
   for (int item = threadIdx.x; item < total; item += blockDim.x) {
     const int t = by_nb.div(item);
     const int j = item - t * nb;
     const int k = j & (Ns - 1);
-    const V* s = src + (size_t)t * n;
-    V* d = dst + (size_t)t * n;
+    const int sbase = t * n + j;
     V a[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) a[r] = s[j + r * nb];
-    if (k != 0) {
+    for (int r = 0; r < R; ++r) a[r] = src[pad32(sbase + r * nb)];
+    if (Ns > 1) {
+      const V* w = twst + k * (R - 1);
 #pragma unroll
-      for (int r = 1; r < R; ++r) {
-        V w = tw[r * k * twstep];
-        if (sign > 0) w = conjg(w);
-        a[r] = cmul(a[r], w);
-      }
+      for (int r = 1; r < R; ++r) a[r] = cmul_s<SIGN>(a[r], ldg_v(w + r - 1));
     }
-    Dft<R, V>::run(a, sign);
-    const int idxD = (j - k) * R + k;
+    Dft<R, V>::template run<SIGN>(a);
+    const int dbase = t * n + (j - k) * R + k;
 #pragma unroll
-    for (int r = 0; r < R; ++r) d[idxD + r * Ns] = a[r];
+    for (int r = 0; r < R; ++r) dst[pad32(dbase + r * Ns)] = a[r];
   }
 }
 
-// Batched in-shared-memory FFT: `B` transforms of length rad.n, contiguous,
-// in `a`; `b` is scratch of the same size. Unnormalised; sign -1: exp(-i...),
-// +1: exp(+i...). `tw` holds the forward roots exp(-2 pi i m / n), m<n.
-// Returns the buffer holding the result. Every thread of the block calls it.
-template <typename V>
-__device__ V* fft_block(V* a, V* b, int B, const RadixDev& rad, int sign, const V* __restrict__ tw) {
+// Batched in-shared-memory FFT: B transforms of length rad.n, contiguous in
+// the padded layout, in `a`; `b` is scratch of the same size.  Unnormalised;
+// SIGN -1: exp(-i...), +1: exp(+i...).  `tw` is the per-stage twiddle table
+// of this length (make_stage_twiddles).  Returns the buffer holding the
+// result.  Every thread of the block calls it.
+template <int SIGN, typename V>
+__device__ V* fft_block(V* a, V* b, int B, const RadixDev& rad, const V* __restrict__ tw) {
   const int n = rad.n;
   int Ns = 1;
   for (int st = 0; st < rad.nst; ++st) {
     const int R = rad.r[st];
+    const V* twst = tw + rad.twoff[st];
     switch (R) {
-      case 16: stockham_stage<16>(a, b, B, n, Ns, sign, tw); break;
-      case 8: stockham_stage<8>(a, b, B, n, Ns, sign, tw); break;
-      case 4: stockham_stage<4>(a, b, B, n, Ns, sign, tw); break;
-      case 2: stockham_stage<2>(a, b, B, n, Ns, sign, tw); break;
-      default: stockham_stage<3>(a, b, B, n, Ns, sign, tw); break;
+      case 16: stockham_stage<16, SIGN>(a, b, B, n, Ns, twst); break;
+      case 8: stockham_stage<8, SIGN>(a, b, B, n, Ns, twst); break;
+      case 4: stockham_stage<4, SIGN>(a, b, B, n, Ns, twst); break;
+      case 2: stockham_stage<2, SIGN>(a, b, B, n, Ns, twst); break;
+      default: stockham_stage<3, SIGN>(a, b, B, n, Ns, twst); break;
     }
     __syncthreads();
     V* tmp = a;

@@ -10,7 +10,8 @@
 //   Dati.cart.<n>.out  snapshots every dt_field (dnsdata.f90:895-918)
 //   Runtimedata   one line per step (dnsdata.f90:878), rewound to the restart
 //                 time when time_from_restart (get_record, dnsdata.f90:181-218)
-// Usage: channel_gb300 [--mixed | --fp64dd] [--quiet]   (in the run directory)
+// Usage: channel_gb300 [--mixed | --fp64dd] [--quiet] [--no-tune]   (in the run
+// directory; --no-tune keeps the default transform tiles instead of timing them)
 #include <chgpu.h>
 
 #include "hostio.h"
@@ -89,14 +90,15 @@ int check(int rc, chgpu_handle* h, const char* what) {
 }  // namespace
 
 int main(int argc, char** argv) {
-  bool quiet = false;
+  bool quiet = false, tune = true;
   int precision = CHGPU_FP64;
   for (int i = 1; i < argc; ++i) {
     if (!std::strcmp(argv[i], "--mixed")) precision = CHGPU_MIXED;
     else if (!std::strcmp(argv[i], "--fp64dd")) precision = CHGPU_FP64DD;
     else if (!std::strcmp(argv[i], "--quiet")) quiet = true;
+    else if (!std::strcmp(argv[i], "--no-tune")) tune = false;
     else {
-      std::fprintf(stderr, "usage: %s [--mixed | --fp64dd] [--quiet]\n", argv[0]);
+      std::fprintf(stderr, "usage: %s [--mixed | --fp64dd] [--quiet] [--no-tune]\n", argv[0]);
       return 2;
     }
   }
@@ -110,6 +112,7 @@ int main(int argc, char** argv) {
   d.p.precision = precision;
   chgpu_handle* h = nullptr;
   check(chgpu_create(&d.p, &h), nullptr, "chgpu_create");
+  if (tune) check(chgpu_autotune(h), h, "chgpu_autotune");  // transform tiles; results do not depend on them
   chgpu_params& p = d.p;
   std::vector<double> V;
   double time = p.time;

@@ -41,6 +41,7 @@ struct ConvLaunch {
   const void* cst;  // in the transform type: factor, 1/dx, 1/dz, then 1/dy(iy) at [3 + plane]
   DevScalars* sc;
   int zcols, xrows;
+  int xminb;  // register-cap variant of the x-row kernel (1, 2 or 3 blocks per SM)
   int plane0, nplanes;
   int compute_cfl;
   int products;  // 0: stop after the x pass (the start-up CFL pass)
@@ -49,6 +50,9 @@ struct ConvLaunch {
 // stage 0: z-inverse, 1: x rows, 2: z-forward
 template <typename T> void launch_convolutions(const ConvLaunch& L, cudaStream_t s, int stage);
 cudaError_t conv_set_smem_limits();
+// dynamic shared memory of the z-transform and x-row kernels (padded buffers)
+size_t conv_z_smem(int zcols, int nzd, size_t ts);
+size_t conv_x_smem(int xrows, int nxd, size_t ts);
 
 struct SolveLaunch {
   Dims d;

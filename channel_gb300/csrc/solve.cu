@@ -391,22 +391,32 @@ __global__ void __launch_bounds__(64) k_linsolve(double2* __restrict__ V, const 
     double2 x1[2] = {cz(), cz()}, x2[2] = {cz(), cz()};
     double2 xc1 = cz(), xc2 = cz();
     const double2* rsrc = rhs + (role == 0 ? rcs : 0);
+    // right-hand sides one row ahead of the recurrence (global-load latency)
+    double2 bnext[2] = {cz(), cz()};
+#pragma unroll
+    for (int t = 0; t < 2; ++t)
+      if (t < nm) bnext[t] = rsrc[(size_t)(ny - 1 + roff) * d.nmodes + mm[t]];
     for (int iy = ny - 1; iy >= 1; --iy) {
       const double* dr = der + (size_t)iy * 20;
-      double A[5];
+      double2 b[2] = {bnext[0], bnext[1]};
+      if (iy > 1) {
 #pragma unroll
-      for (int j = 0; j < 5; ++j) {
-        const double d0 = __ldg(dr + j), d2 = __ldg(dr + 10 + j);
-        A[j] = role ? ac.ce0 * d0 + ac.ce2 * d2 : ac.cv4 * __ldg(dr + 15 + j) + ac.cv2 * d2 + ac.cv0 * d0;
+        for (int t = 0; t < 2; ++t)
+          if (t < nm) bnext[t] = rsrc[(size_t)(iy - 1 + roff) * d.nmodes + mm[t]];
+      }
+      double A[5];
+      if (role) {  // warp-uniform: each warp assembles only its own matrix
+#pragma unroll
+        for (int j = 0; j < 5; ++j) A[j] = ac.ce0 * __ldg(dr + j) + ac.ce2 * __ldg(dr + 10 + j);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 5; ++j)
+          A[j] = ac.cv4 * __ldg(dr + 15 + j) + ac.cv2 * __ldg(dr + 10 + j) + ac.cv0 * __ldg(dr + j);
       }
       if (iy == ny - 1) bc_top1(A, top, topp1);
       if (iy == ny - 2) bc_top2(A, top);
       if (iy == 1) bc_bot1(A, bot, botm1);
       if (iy == 2) bc_bot2(A, bot);
-      double2 b[2];
-#pragma unroll
-      for (int t = 0; t < 2; ++t)
-        if (t < nm) b[t] = rsrc[(size_t)(iy + roff) * d.nmodes + mm[t]];
       if (role == 1 && is00) {  // the packed wall velocity enters rows 1, 2, ny-2, ny-1 (linsolve_blocking.inc:26-27,40-41)
         if (iy == 1) b[0] = b[0] - make_double2(A[1] * bval0 / bot[1], A[1] * 0.0 / bot[1]);
         if (iy == 2) b[0] = b[0] - make_double2(A[0] * bval0 / bot[1], A[0] * 0.0 / bot[1]);
@@ -443,13 +453,28 @@ __global__ void __launch_bounds__(64) k_linsolve(double2* __restrict__ V, const 
     double2 lo[2][3], hi[2][3], clo[3], chi[3];
     {
       double2 m2[2] = {cz(), cz()}, m1[2] = {cz(), cz()}, c2 = cz(), c1 = cz();
+      // factors and Step1 results one row ahead
+      const double* f1 = fac + ((size_t)0 * 4 + 2 * role) * P + q;
+      double l2n = f1[0], l1n = f1[P];
+      double2 vn[2] = {cz(), cz()};
+#pragma unroll
+      for (int t = 0; t < 2; ++t)
+        if (t < nm) vn[t] = V[vidx(d, vc, 1, mm[t])];
       for (int iy = 1; iy <= ny - 1; ++iy) {
-        const double* f = fac + ((size_t)(iy - 1) * 4 + 2 * role) * P + q;
-        const double l2 = f[0], l1 = f[P];
+        const double l2 = l2n, l1 = l1n;
+        const double2 vcur[2] = {vn[0], vn[1]};
+        if (iy < ny - 1) {
+          const double* f = fac + ((size_t)iy * 4 + 2 * role) * P + q;
+          l2n = f[0];
+          l1n = f[P];
+#pragma unroll
+          for (int t = 0; t < 2; ++t)
+            if (t < nm) vn[t] = V[vidx(d, vc, iy + 1, mm[t])];
+        }
 #pragma unroll
         for (int t = 0; t < 2; ++t) {
           if (t < nm) {
-            const double2 nv = step2(V[vidx(d, vc, iy, mm[t])], l2, l1, m2[t], m1[t]);
+            const double2 nv = step2(vcur[t], l2, l1, m2[t], m1[t]);
             V[vidx(d, vc, iy, mm[t])] = nv;
             m2[t] = m1[t];
             m1[t] = nv;
@@ -559,9 +584,11 @@ __global__ void __launch_bounds__(64) k_linsolve(double2* __restrict__ V, const 
     win[3] = vhi[3];
     win[4] = vhi[4];
     double2 x1 = cz(), x2 = cz();
+    double2 wnext = V[vidx(d, 1, ny - 3, m)];  // v one row ahead
     for (int iy = ny - 1; iy >= 1; --iy) {
       const double* dr = der + (size_t)iy * 20;
-      win[0] = V[vidx(d, 1, iy - 2, m)];
+      win[0] = wnext;
+      if (iy > 1) wnext = V[vidx(d, 1, iy - 3, m)];
       double2 f = rmul(__ldg(dr + 5), win[0]);
 #pragma unroll
       for (int j = 1; j < 5; ++j) f = f + rmul(__ldg(dr + 5 + j), win[j]);
@@ -582,21 +609,23 @@ __global__ void __launch_bounds__(64) k_linsolve(double2* __restrict__ V, const 
   }
   {
     double2 bm2 = cz(), bm1 = fm1;
+    double2 etn = V[vidx(d, 0, -1, m)], xn = cz();  // eta and Step1 results one row ahead
     for (int iy = -1; iy <= ny + 1; ++iy) {
+      const double2 et = etn, xs = xn;
+      if (iy < ny + 1) etn = V[vidx(d, 0, iy + 1, m)];
+      if (iy + 1 >= 1 && iy + 1 <= ny - 1) xn = V[vidx(d, 2, iy + 1, m)];
       double2 vp;
       if (iy == -1) vp = fm1;
       else if (iy == 0) vp = f0;
       else if (iy == ny) vp = fn;
       else if (iy == ny + 1) vp = fn1;
       else {
-        vp = step2(V[vidx(d, 2, iy, m)], __ldg(d0lu + (size_t)(iy - 1) * 5 + 0), __ldg(d0lu + (size_t)(iy - 1) * 5 + 1),
-                   bm2, bm1);
+        vp = step2(xs, __ldg(d0lu + (size_t)(iy - 1) * 5 + 0), __ldg(d0lu + (size_t)(iy - 1) * 5 + 1), bm2, bm1);
       }
       if (iy >= 0 && iy <= ny - 1) {
         bm2 = bm1;
         bm1 = vp;
       }
-      const double2 et = V[vidx(d, 0, iy, m)];
       // u = (i kx v' - i kz eta)/k2, w = (i kz v' + i kx eta)/k2
       V[vidx(d, 0, iy, m)] = make_double2(bu * et.y - au * vp.y, au * vp.x - bu * et.x);
       V[vidx(d, 2, iy, m)] = make_double2(-(bu * vp.y) - au * et.y, bu * vp.x + au * et.x);

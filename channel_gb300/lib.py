@@ -81,6 +81,9 @@ SIGNATURES = {
     "chgpu_kernel_times": (C.c_int, [_P, _DP, C.POINTER(C.c_longlong)]),
     "chgpu_kernel_kind_name": (C.c_char_p, [C.c_int]),
     "chgpu_set_body_force": (C.c_int, [_P, _DP]),
+    "chgpu_autotune": (C.c_int, [_P]),
+    "chgpu_tiles": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "chgpu_set_tiles": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "chgpu_export_dims": (C.c_int, [_P, C.c_float, C.POINTER(C.c_int)]),
     "chgpu_export_physical": (C.c_int, [_P, C.POINTER(ExportOpts), _DP]),
     "chgpu_stats_reset": (C.c_int, [_P]),
@@ -222,6 +225,20 @@ class Channel:
         n = (C.c_longlong * NKINDS)()
         self._check(self.lib.chgpu_kernel_times(self.h, _dp(ms), n))
         return {self.lib.chgpu_kernel_kind_name(k).decode(): (float(ms[k]), int(n[k])) for k in range(NKINDS)}
+
+    def autotune(self) -> tuple[int, int, int]:
+        """Times the transform tiles on this handle and keeps the fastest;
+        returns (z columns, x rows, x-row register variant)."""
+        self._check(self.lib.chgpu_autotune(self.h))
+        return self.tiles()
+
+    def tiles(self) -> tuple[int, int, int]:
+        t = (C.c_int * 3)()
+        self._check(self.lib.chgpu_tiles(self.h, t))
+        return t[0], t[1], t[2]
+
+    def set_tiles(self, tiles) -> None:
+        self._check(self.lib.chgpu_set_tiles(self.h, (C.c_int * 3)(*tiles)))
 
     def export_dims(self, undersample: float = 1.0) -> tuple[int, int, int]:
         d = (C.c_int * 3)()

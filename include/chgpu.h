@@ -120,6 +120,21 @@ int chgpu_get_stats(chgpu_handle* h, chgpu_stats* st);
  * error flags (non-finite CFL) as CHGPU_E_NONFINITE. */
 int chgpu_synchronize(chgpu_handle* h);
 
+/* Autotuner of the transform tiles: times the z-transform kernels for 1, 2,
+ * 4 and 8 columns per block and the x-row kernel for 1, 2 and 4 rows per
+ * block in each of its register-cap variants (compiled for 1, 2 and 3
+ * resident blocks per SM) on this handle's sizes, and keeps the fastest.
+ * Takes a few dozen kernel launches; the field, the RK history and the
+ * module scalars are untouched, and the results of a step do not depend on
+ * the tiles.  Optional: without it the handle uses tiles sized from the
+ * shared-memory budget.  No counterpart in the reference. */
+int chgpu_autotune(chgpu_handle* h);
+/* tiles = {z columns per block, x rows per block, x-row register variant}. */
+int chgpu_tiles(const chgpu_handle* h, int tiles[3]);
+/* Applies tiles found by chgpu_autotune on another handle of the same sizes
+ * and precision; CHGPU_E_PARAM when they do not fit this handle. */
+int chgpu_set_tiles(chgpu_handle* h, const int tiles[3]);
+
 /* Physical-space export of the field: the reference's exporter
  * out_exporter/out2bin.f90 (convert_outfile :141-203, xz_interpolation
  * :236-275, undersampled_to_fullindex :279-299, filter_vfield :338-347) on

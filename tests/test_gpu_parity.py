@@ -174,3 +174,31 @@ def test_nonfinite_field_is_reported(gpu_lib):
         g.start()
     assert e.value.code == -4
     g.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_autotuned_tiles_give_identical_steps(gpu_lib, prec):
+    """The tiles chosen by the autotuner change launch shapes only: the field
+    after three steps is bit-identical to the default tiles' field, and
+    set_tiles applies a tuned choice to a second handle."""
+    p, V0, _, g = make("small", 0.01, 0, prec)
+    from channel_gb300 import Channel
+
+    t = Channel(p, prec)
+    t.upload(V0)
+    tiles = t.autotune()
+    assert tiles == t.tiles()
+    for h in (g, t):
+        h.start()
+        for _ in range(3):
+            h.step()
+    assert np.array_equal(g.download(), t.download())
+    u = Channel(p, prec)
+    u.set_tiles(tiles)
+    assert u.tiles() == tiles
+    from channel_gb300 import ChannelError
+
+    with pytest.raises(ChannelError):
+        u.set_tiles((9, 3, 1))
+    for h in (g, t, u):
+        h.close()
