@@ -5,10 +5,10 @@
 // run several times faster than in FP64 while keeping errors near 1e-14.
 //
 // Building blocks are the error-free transformations of Knuth (two-sum) and
-// Dekker (fast two-sum), with the product error taken from an FMA; the
-// addition is the accurate variant that normalises both the high and the low
-// sums (Hida, Li & Bailey, "Library for double-double and quad-double
-// arithmetic", 2007, Algorithm 6 adapted to FP32 components).
+// Dekker (fast two-sum), with the product error taken from an FMA (Dekker,
+// "A floating-point technique for extending the available precision", 1971;
+// error bounds in Joldes, Muller & Popescu, "Tight and rigorous error bounds
+// for basic building blocks of double-word arithmetic", 2017).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -36,13 +36,15 @@ __device__ __forceinline__ dd fast_two_sum(float a, float b) {  // |a| >= |b|
   float e = __fsub_rn(b, __fsub_rn(s, a));
   return dd(s, e);
 }
+// Dekker's addition ("sloppy" double-word add): the high parts added
+// error-free, the low parts and the error summed in FP32, one
+// renormalisation; 11 FP32 operations.  Its error is bounded relative to
+// |a| + |b| (about 2^-46 of it), the same form as the error of an FP64
+// addition of inputs that carry their own rounding.
 __device__ __forceinline__ dd operator+(dd a, dd b) {
-  dd s = two_sum(a.hi, b.hi);
-  dd t = two_sum(a.lo, b.lo);
-  s.lo = __fadd_rn(s.lo, t.hi);
-  s = fast_two_sum(s.hi, s.lo);
-  s.lo = __fadd_rn(s.lo, t.lo);
-  return fast_two_sum(s.hi, s.lo);
+  const dd s = two_sum(a.hi, b.hi);
+  const float e = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return fast_two_sum(s.hi, e);
 }
 __device__ __forceinline__ dd operator-(dd a) { return dd(-a.hi, -a.lo); }
 __device__ __forceinline__ dd operator-(dd a, dd b) { return a + (-b); }

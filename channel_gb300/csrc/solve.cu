@@ -20,6 +20,8 @@
 // The recurrences of each mode are sequential in y; parallelism is across modes.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "chgpu_internal.h"
 #include "cplx.cuh"
 #include "kernels.cuh"
@@ -84,10 +86,35 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
   using V2 = typename C2<T>::t;
   using O2 = typename HistT<T>::t;
   using OT = decltype(O2::x);
-  using L = typename LinT<T>::t;
-  using LV = typename C2<L>::t;
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   const int iy = blockIdx.y + 1;
+  // ---- linear terms of the field in L (FP64, or double-float in the mixed
+  //      path: the FP64 pipe is 1/58 of FP32 here) ----
+  // timescheme (dnsdata.f90:486) combines ODE(1)/deltat * unkn + impl, which
+  // for D2v (:647) is, with S_k = Dk(V2) and lambda = ODE(1)/deltat,
+  //   lambda (S2 - k2 S0) + ni (S4 - 2 k2 S2 + k2^2 S0) = sum_j (A_j + k2 B_j + k2^2 C_j) V2_j
+  // and for eta (:658) with w = i kz V1 - i kx V3
+  //   lambda S0(w) + ni (S2(w) - k2 S0(w)) = sum_j (D_j + k2 E_j) w_j,
+  // the mean mode (:653) being the k2 = 0 case on (U, W).  The per-row
+  // coefficients A..E are formed once per block.
+  using L = typename LinT<T>::t;
+  using LV = typename C2<L>::t;
+  const size_t tailL = (size_t)(d.ny + 1) * 20;  // der rows, then alfa0, beta0, ni
+  __shared__ __align__(16) unsigned char cf_raw[25 * sizeof(L)];
+  L* cf = reinterpret_cast<L*>(cf_raw);
+  if (std::is_same<L, dd>::value && threadIdx.x < 5) {
+    const int j = threadIdx.x;
+    const L* dr = derL + (size_t)iy * 20;
+    const L c0 = dr[j], c2 = dr[10 + j], c4 = dr[15 + j];
+    const L lam = Num<L>::from_double(ode1 * sc->rdt);  // ODE(1)/deltat
+    const L nu = derL[tailL + 2];
+    cf[j] = lam * c2 + nu * c4;
+    cf[5 + j] = L() - (lam * c0 + (nu + nu) * c2);
+    cf[10 + j] = nu * c0;
+    cf[15 + j] = lam * c0 + nu * c2;
+    cf[20 + j] = L() - nu * c0;
+  }
+  __syncthreads();
   if (m >= d.nmodes) return;
   const int ix = m / d.nzt;
   const int iz = m - ix * d.nzt - d.nz;
@@ -122,20 +149,8 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
   V2 explv = mul_ia<V2>(ta, mul_ia<V2>(ta, DD(e1, 0)) + DD(e2, 3) + mul_ia<V2>(tb, DD1_6)) +
              mul_ia<V2>(tb, mul_ia<V2>(ta, DD1_6) + DD(e2, 4) + mul_ia<V2>(tb, DD(e1, 2)));
   explv = explv - mk<V2>(tk2 * rhsv.x, tk2 * rhsv.y);
-  // ---- linear terms of the field and the RK combination, in L (FP64, or
-  //      double-float in the mixed path: the FP64 pipe is 1/62 of FP32 here) ----
-  const L* drL = derL + (size_t)iy * 20;
-  const size_t tailL = (size_t)(d.ny + 1) * 20;  // then alfa0, beta0, ni
   const L a = L((float)ix) * derL[tailL], b = L((float)iz) * derL[tailL + 1];
   const L k2 = a * a + b * b;
-  const L ni = derL[tailL + 2];
-  L c0[5], c2[5], c4[5];
-#pragma unroll
-  for (int j = 0; j < 5; ++j) {
-    c0[j] = drL[j];
-    c2[j] = drL[10 + j];
-    c4[j] = drL[15 + j];
-  }
   // body-force terms (dnsdata.f90:644, 651, 658): fv for the v equation,
   // fe for eta (or the mean mode's D0 of Re F1, Re F3)
   LV fv = czero<LV>(), fe = czero<LV>();
@@ -144,17 +159,17 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
     L r1 = L(), r3 = L();
 #pragma unroll
     for (int j = 0; j < 5; ++j) {
-      const L c1 = drL[5 + j];
+      const L c0 = derL[(size_t)iy * 20 + j], c1 = derL[(size_t)iy * 20 + 5 + j];
       const LV f1 = cvt2<LV>(F[vidx(d, 0, iy - 2 + j, m)]);
       const LV f2 = cvt2<LV>(F[vidx(d, 1, iy - 2 + j, m)]);
       const LV f3 = cvt2<LV>(F[vidx(d, 2, iy - 2 + j, m)]);
-      D0f1 = D0f1 + lmul(c0[j], f1);
-      D0f2 = D0f2 + lmul(c0[j], f2);
-      D0f3 = D0f3 + lmul(c0[j], f3);
+      D0f1 = D0f1 + lmul(c0, f1);
+      D0f2 = D0f2 + lmul(c0, f2);
+      D0f3 = D0f3 + lmul(c0, f3);
       D1f1 = D1f1 + lmul(c1, f1);
       D1f3 = D1f3 + lmul(c1, f3);
-      r1 = r1 + c0[j] * f1.x;
-      r3 = r3 + c0[j] * f3.x;
+      r1 = r1 + c0 * f1.x;
+      r3 = r3 + c0 * f3.x;
     }
     fv = czero<LV>() - lmul(k2, D0f2) - mul_ia<LV>(a, D1f1) - mul_ia<LV>(b, D1f3);
     fe = (ix == 0 && iz == 0) ? mk<LV>(r1, r3) : mul_ia<LV>(b, D0f1) - mul_ia<LV>(a, D0f3);
@@ -166,26 +181,37 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
     v2[j] = cvt2<LV>(V[vidx(d, 1, iy - 2 + j, m)]);
     v3[j] = cvt2<LV>(V[vidx(d, 2, iy - 2 + j, m)]);
   }
-  const L odt = Num<L>::from_double(ode1 * sc->rdt);  // ODE(1)/deltat
   const L lode2 = Num<L>::from_double(ode2), lode3 = Num<L>::from_double(ode3);
   const size_t r0 = ((size_t)0 * (d.ny - 1) + (iy - 1)) * d.nmodes + m;  // eta
   const size_t r1 = ((size_t)1 * (d.ny - 1) + (iy - 1)) * d.nmodes + m;  // d2v
-  // timescheme (dnsdata.f90:486) for D2v (:647): with S_k = Dk(V2),
-  //   unkn = S2 - k2 S0,  impl = sum OS V2 = ni (S4 - 2 k2 S2 + k2^2 S0)
+  // FP64 linear terms keep the reference's evaluation order: the flow-rate
+  // correction divides by a difference ~1e-3 of its terms, and the order of
+  // the roundings shows there at 1e-10.  The double-float ones have ~48 bits
+  // to spare and take the combined coefficients.
+  constexpr bool kCombined = std::is_same<L, dd>::value;
+  const L* drL = derL + (size_t)iy * 20;
+  const L lam = Num<L>::from_double(ode1 * sc->rdt), nu = derL[(size_t)(d.ny + 1) * 20 + 2];
   {
-    LV s0 = lmul(c0[0], v2[0]), s2 = lmul(c2[0], v2[0]), s4 = lmul(c4[0], v2[0]);
+    LV r;
+    if constexpr (kCombined) {
+      r = lmul(cf[0] + k2 * (cf[5] + k2 * cf[10]), v2[0]);
 #pragma unroll
-    for (int j = 1; j < 5; ++j) {
-      s0 = s0 + lmul(c0[j], v2[j]);
-      s2 = s2 + lmul(c2[j], v2[j]);
-      s4 = s4 + lmul(c4[j], v2[j]);
+      for (int j = 1; j < 5; ++j) r = r + lmul(cf[j] + k2 * (cf[5 + j] + k2 * cf[10 + j]), v2[j]);
+    } else {
+      LV s0 = lmul(drL[0], v2[0]), s2 = lmul(drL[10], v2[0]), s4 = lmul(drL[15], v2[0]);
+#pragma unroll
+      for (int j = 1; j < 5; ++j) {
+        s0 = s0 + lmul(drL[j], v2[j]);
+        s2 = s2 + lmul(drL[10 + j], v2[j]);
+        s4 = s4 + lmul(drL[15 + j], v2[j]);
+      }
+      const LV unkn = s2 - lmul(k2, s0);
+      const LV impl = lmul(nu, s4 - lmul(k2 + k2, s2) + lmul(k2 * k2, s0));
+      r = lmul(lam, unkn) + impl;
     }
-    const LV unkn = s2 - lmul(k2, s0);
-    const LV impl = lmul(ni, s4 - lmul(k2 + k2, s2) + lmul(k2 * k2, s0));
     const O2 o = old[r1];
     LV e = mk<LV>(conv<L>(explv.x), conv<L>(explv.y));
     if (F) e = e + fv;
-    LV r = lmul(odt, unkn) + impl;
     r = r + lmul(lode2, e);
     r = r - lmul(lode3, mk<LV>(conv<L>(o.x), conv<L>(o.y)));
     old[r1] = mk<O2>(store_as<OT>(e.x), store_as<OT>(e.y));
@@ -195,37 +221,58 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
     LV e = mk<LV>(conv<L>(rhsu.x) + Num<L>::from_double(sc->meanpx),
                   conv<L>(rhsw.x) + Num<L>::from_double(sc->meanpz));
     if (F) e = e + fe;
-    L su = c0[0] * v1[0].x, sw = c0[0] * v3[0].x, tu = c2[0] * v1[0].x, tw = c2[0] * v3[0].x;
+    LV r;
+    if constexpr (kCombined) {
+      L su = cf[15] * v1[0].x, sw = cf[15] * v3[0].x;
 #pragma unroll
-    for (int j = 1; j < 5; ++j) {
-      su = su + c0[j] * v1[j].x;
-      sw = sw + c0[j] * v3[j].x;
-      tu = tu + c2[j] * v1[j].x;
-      tw = tw + c2[j] * v3[j].x;
+      for (int j = 1; j < 5; ++j) {
+        su = su + cf[15 + j] * v1[j].x;
+        sw = sw + cf[15 + j] * v3[j].x;
+      }
+      r = mk<LV>(su, sw);
+    } else {
+      L su = drL[0] * v1[0].x, sw = drL[0] * v3[0].x, tu = drL[10] * v1[0].x, tw = drL[10] * v3[0].x;
+#pragma unroll
+      for (int j = 1; j < 5; ++j) {
+        su = su + drL[j] * v1[j].x;
+        sw = sw + drL[j] * v3[j].x;
+        tu = tu + drL[10 + j] * v1[j].x;
+        tw = tw + drL[10 + j] * v3[j].x;
+      }
+      r = lmul(lam, mk<LV>(su, sw)) + mk<LV>(nu * tu, nu * tw);
     }
-    const LV unkn = mk<LV>(su, sw);
-    const LV impl = mk<LV>(ni * tu, ni * tw);
     const O2 o = old[r0];
-    LV r = lmul(odt, unkn) + impl;
     r = r + lmul(lode2, e);
     r = r - lmul(lode3, mk<LV>(conv<L>(o.x), conv<L>(o.y)));
     old[r0] = mk<O2>(store_as<OT>(e.x), store_as<OT>(e.y));
     rhs[r0] = make_double2(Num<L>::to_double(r.x), Num<L>::to_double(r.y));
   } else {  // eta (:656-661): with w = i kz V1 - i kx V3, unkn = D0(w), impl = ni (D2(w) - k2 D0(w))
     const V2 ee = mul_ia<V2>(tb, rhsu) - mul_ia<V2>(ta, rhsw);
-    LV w = mul_ia<LV>(b, v1[0]) - mul_ia<LV>(a, v3[0]);
-    LV s0 = lmul(c0[0], w), s2 = lmul(c2[0], w);
+    LV r;
+    if constexpr (kCombined) {
+      L nj = cf[15] + k2 * cf[20];
+      LV s1 = lmul(nj, v1[0]), s3 = lmul(nj, v3[0]);
 #pragma unroll
-    for (int j = 1; j < 5; ++j) {
-      w = mul_ia<LV>(b, v1[j]) - mul_ia<LV>(a, v3[j]);
-      s0 = s0 + lmul(c0[j], w);
-      s2 = s2 + lmul(c2[j], w);
+      for (int j = 1; j < 5; ++j) {
+        nj = cf[15 + j] + k2 * cf[20 + j];
+        s1 = s1 + lmul(nj, v1[j]);
+        s3 = s3 + lmul(nj, v3[j]);
+      }
+      r = mul_ia<LV>(b, s1) - mul_ia<LV>(a, s3);
+    } else {  // with w = i kz V1 - i kx V3: unkn = D0(w), impl = ni (D2(w) - k2 D0(w))
+      LV w = mul_ia<LV>(b, v1[0]) - mul_ia<LV>(a, v3[0]);
+      LV s0 = lmul(drL[0], w), s2 = lmul(drL[10], w);
+#pragma unroll
+      for (int j = 1; j < 5; ++j) {
+        w = mul_ia<LV>(b, v1[j]) - mul_ia<LV>(a, v3[j]);
+        s0 = s0 + lmul(drL[j], w);
+        s2 = s2 + lmul(drL[10 + j], w);
+      }
+      r = lmul(lam, s0) + lmul(nu, s2 - lmul(k2, s0));
     }
-    const LV impl = lmul(ni, s2 - lmul(k2, s0));
     const O2 o = old[r0];
     LV e = mk<LV>(conv<L>(ee.x), conv<L>(ee.y));
     if (F) e = e + fe;
-    LV r = lmul(odt, s0) + impl;
     r = r + lmul(lode2, e);
     r = r - lmul(lode3, mk<LV>(conv<L>(o.x), conv<L>(o.y)));
     old[r0] = mk<O2>(store_as<OT>(e.x), store_as<OT>(e.y));
