@@ -8,4 +8,4 @@ generator.  There is no CPU fallback: if the library is missing, loading
 fails loudly.
 """
 from .dnsin import DnsIn, padded_sizes, fft_fit, workload  # noqa: F401
-from .lib import Channel, ChannelError, load_library, library_path, RK  # noqa: F401
+from .lib import Channel, ChannelError, Ensemble, load_library, library_path, RK  # noqa: F401

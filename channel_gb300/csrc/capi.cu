@@ -70,6 +70,7 @@ struct chgpu_handle {
   DevScalars* sc = nullptr;
   DevScalars* sc_host = nullptr;  // pinned
   cudaGraphExec_t graph = nullptr;
+  long long version = 0;  // bumped whenever the launch sequence of a step changes
   bool field_set = false;
   // on-device statistics: [S1, comp S1, S2, comp S2][3][nplanes]
   double* stats_acc = nullptr;
@@ -723,6 +724,155 @@ const char* chgpu_kernel_kind_name(int kind) {
 }
 
 // ---------------------------------------------------------------------------
+// ensemble of independent runs: one graph launch per step for all members
+// ---------------------------------------------------------------------------
+struct chgpu_ensemble {
+  std::vector<chgpu_handle*> m;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaGraphExec_t graph = nullptr;
+  std::vector<long long> versions;  // member versions the graph was captured with
+  std::string err;
+};
+
+namespace {
+
+int ens_fail(chgpu_ensemble* e, int code, const std::string& msg) {
+  if (e) e->err = msg;
+  else g_create_error = msg;
+  return code;
+}
+
+#define CKE(e, call)                                                                             \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess)                                                                       \
+      return ens_fail((e), e_ == cudaErrorMemoryAllocation ? CHGPU_E_NOMEM : CHGPU_E_CUDA,        \
+                      std::string(#call) + ": " + cudaGetErrorName(e_) + " (" + cudaGetErrorString(e_) + ")"); \
+  } while (0)
+
+void ens_release(chgpu_ensemble* e) {
+  if (e->graph) cudaGraphExecDestroy(e->graph);
+  for (cudaEvent_t ev : e->join)
+    if (ev) cudaEventDestroy(ev);
+  if (e->fork) cudaEventDestroy(e->fork);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  for (chgpu_handle* h : e->m)
+    if (h) chgpu_destroy(h);
+}
+
+}  // namespace
+
+int chgpu_ensemble_create(const chgpu_params* params, int n, chgpu_ensemble** out) {
+  if (!out) return ens_fail(nullptr, CHGPU_E_PARAM, "chgpu_ensemble_create: null output");
+  *out = nullptr;
+  if (!params || n < 1) return ens_fail(nullptr, CHGPU_E_PARAM, "chgpu_ensemble_create: need n >= 1 parameter sets");
+  chgpu_ensemble* e = new (std::nothrow) chgpu_ensemble;
+  if (!e) return ens_fail(nullptr, CHGPU_E_NOMEM, "chgpu_ensemble_create: out of host memory");
+  e->m.assign(n, nullptr);
+  e->join.assign(n, nullptr);
+  for (int i = 0; i < n; ++i) {
+    if (int rc = chgpu_create(&params[i], &e->m[i])) {
+      const std::string msg = "member " + std::to_string(i) + ": " + chgpu_last_error(nullptr);
+      ens_release(e);
+      delete e;
+      return ens_fail(nullptr, rc, msg);
+    }
+  }
+  cudaError_t c = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+  if (c == cudaSuccess) c = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
+  for (int i = 0; i < n && c == cudaSuccess; ++i) c = cudaEventCreateWithFlags(&e->join[i], cudaEventDisableTiming);
+  if (c != cudaSuccess) {
+    ens_release(e);
+    delete e;
+    return ens_fail(nullptr, CHGPU_E_CUDA, std::string("chgpu_ensemble_create: ") + cudaGetErrorString(c));
+  }
+  *out = e;
+  return 0;
+}
+
+int chgpu_ensemble_destroy(chgpu_ensemble* e) {
+  if (!e) return 0;
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  ens_release(e);
+  delete e;
+  return 0;
+}
+
+int chgpu_ensemble_size(const chgpu_ensemble* e) { return e ? (int)e->m.size() : 0; }
+
+chgpu_handle* chgpu_ensemble_member(chgpu_ensemble* e, int i) {
+  return (e && i >= 0 && i < (int)e->m.size()) ? e->m[i] : nullptr;
+}
+
+int chgpu_ensemble_step(chgpu_ensemble* e, chgpu_stats* st) {
+  if (!e) return ens_fail(e, CHGPU_E_PARAM, "chgpu_ensemble_step: null ensemble");
+  const int n = (int)e->m.size();
+  bool stale = !e->graph || (int)e->versions.size() != n;
+  for (int i = 0; i < n; ++i) {
+    if (!e->m[i]->field_set) return ens_fail(e, CHGPU_E_STATE, "chgpu_ensemble_step: member without a field");
+    if (!stale && e->versions[i] != e->m[i]->version) stale = true;
+  }
+  if (stale) {
+    if (e->graph) {
+      cudaGraphExecDestroy(e->graph);
+      e->graph = nullptr;
+    }
+    // fork from the ensemble stream into every member's stream, enqueue each
+    // member's step there, join back: one graph whose branches run together
+    cudaGraph_t g = nullptr;
+    CKE(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    CKE(e, cudaEventRecord(e->fork, e->stream));
+    for (int i = 0; i < n; ++i) {
+      chgpu_handle* h = e->m[i];
+      const bool prof = h->profiling;
+      h->profiling = false;
+      const long long before = h->launches;
+      cudaStreamWaitEvent(h->stream, e->fork, 0);
+      enqueue_step(h);
+      cudaEventRecord(e->join[i], h->stream);
+      cudaStreamWaitEvent(e->stream, e->join[i], 0);
+      h->launches = before;
+      h->profiling = prof;
+    }
+    cudaError_t c = cudaStreamEndCapture(e->stream, &g);
+    if (c != cudaSuccess) return ens_fail(e, CHGPU_E_CUDA, std::string("ensemble capture: ") + cudaGetErrorString(c));
+    c = cudaGraphInstantiate(&e->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (c != cudaSuccess) {
+      e->graph = nullptr;
+      return ens_fail(e, CHGPU_E_CUDA, std::string("ensemble graph: ") + cudaGetErrorString(c));
+    }
+    e->versions.resize(n);
+    for (int i = 0; i < n; ++i) e->versions[i] = e->m[i]->version;
+  }
+  CKE(e, cudaGraphLaunch(e->graph, e->stream));
+  for (chgpu_handle* h : e->m) h->launches += 19;
+  if (!st) return 0;
+  for (chgpu_handle* h : e->m)
+    CKE(e, cudaMemcpyAsync(h->sc_host, h->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, e->stream));
+  CKE(e, cudaStreamSynchronize(e->stream));
+  int rc = 0;
+  for (int i = 0; i < n; ++i) {
+    fill_stats(e->m[i], &st[i]);
+    if ((e->m[i]->sc_host->error & 1) && rc == 0)
+      rc = ens_fail(e, CHGPU_E_NONFINITE, "member " + std::to_string(i) + ": non-finite CFL or statistics");
+  }
+  return rc;
+}
+
+int chgpu_ensemble_synchronize(chgpu_ensemble* e) {
+  if (!e) return ens_fail(e, CHGPU_E_PARAM, "null ensemble");
+  CKE(e, cudaStreamSynchronize(e->stream));
+  return 0;
+}
+
+void* chgpu_ensemble_stream(chgpu_ensemble* e) { return e ? (void*)e->stream : nullptr; }
+
+const char* chgpu_ensemble_last_error(const chgpu_ensemble* e) { return e ? e->err.c_str() : g_create_error.c_str(); }
+
+// ---------------------------------------------------------------------------
 // autotuner of the transform tiles
 // ---------------------------------------------------------------------------
 namespace {
@@ -798,6 +948,7 @@ int chgpu_autotune(chgpu_handle* h) {
   h->xrows = best_r;
   h->xminb = best_b;
   h->tuned = true;
+  ++h->version;
   if (h->graph) {  // the captured step holds the old launch shapes
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
@@ -818,6 +969,7 @@ int chgpu_set_tiles(chgpu_handle* h, const int tiles[3]) {
   h->zcols = zc;
   h->xrows = xr;
   h->xminb = xb;
+  ++h->version;
   if (h->graph) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
@@ -966,6 +1118,7 @@ int chgpu_set_body_force(chgpu_handle* h, const double* F) {
     CK(h, cudaStreamSynchronize(h->stream));
     h->use_F = true;
   }
+  if (was != h->use_F) ++h->version;
   if (was != h->use_F && h->graph) {  // the captured step holds the old launch parameters
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;

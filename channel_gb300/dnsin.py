@@ -192,3 +192,23 @@ def workload(name: str) -> DnsIn:
         return DnsIn(nx=47, ny=96, nz=47, alfa0=0.5, beta0=1.0, re=14000.0, a=1.8, ymin=0.0, ymax=2.0,
                      meanflowx=4.0 / 3.0, deltat=0.0, cflmax=1.0, nstep=100)
     raise KeyError(name)
+
+
+def ensemble_workloads(n: int = 64, seed: int = 0) -> list[DnsIn]:
+    """The batched-ensemble workload: n independent minimal channels with
+    nx, nz drawn from {16, 24, 32}, ny from {48, 64, 96}, Re uniform in
+    [2000, 4000], alfa0 in [1, 2], beta0 in [2, 4] by numpy's default_rng(seed);
+    fixed dt = 0.004 and constant flow rate 4/3 as in the 32x64x32 case.
+    Member i starts from perturbed_laminar(p_i, 0.01, seed=i)."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        nx, nz = (int(v) for v in rng.choice([16, 24, 32], size=2))
+        ny = int(rng.choice([48, 64, 96]))
+        re = float(rng.uniform(2000.0, 4000.0))
+        alfa0, beta0 = float(rng.uniform(1.0, 2.0)), float(rng.uniform(2.0, 4.0))
+        out.append(DnsIn(nx=nx, ny=ny, nz=nz, alfa0=alfa0, beta0=beta0, re=re, a=1.6, ymin=0.0, ymax=2.0,
+                         meanflowx=4.0 / 3.0, deltat=0.004, cflmax=0.0, nstep=200))
+    return out

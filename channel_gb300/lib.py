@@ -81,6 +81,14 @@ SIGNATURES = {
     "chgpu_kernel_times": (C.c_int, [_P, _DP, C.POINTER(C.c_longlong)]),
     "chgpu_kernel_kind_name": (C.c_char_p, [C.c_int]),
     "chgpu_set_body_force": (C.c_int, [_P, _DP]),
+    "chgpu_ensemble_create": (C.c_int, [C.POINTER(Params), C.c_int, C.POINTER(C.c_void_p)]),
+    "chgpu_ensemble_destroy": (C.c_int, [_P]),
+    "chgpu_ensemble_size": (C.c_int, [_P]),
+    "chgpu_ensemble_member": (C.c_void_p, [_P, C.c_int]),
+    "chgpu_ensemble_step": (C.c_int, [_P, C.POINTER(Stats)]),
+    "chgpu_ensemble_synchronize": (C.c_int, [_P]),
+    "chgpu_ensemble_stream": (C.c_void_p, [_P]),
+    "chgpu_ensemble_last_error": (C.c_char_p, [_P]),
     "chgpu_autotune": (C.c_int, [_P]),
     "chgpu_tiles": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "chgpu_set_tiles": (C.c_int, [_P, C.POINTER(C.c_int)]),
@@ -130,19 +138,27 @@ def _dp(a: np.ndarray):
     return a.ctypes.data_as(_DP)
 
 
+def _precision(precision: str | int) -> int:
+    return {"fp64": FP64, "mixed": MIXED, "fp64dd": FP64DD}[precision] if isinstance(precision, str) else precision
+
+
 class Channel:
     """One channel run on the current CUDA device."""
 
-    def __init__(self, p: DnsIn, precision: str | int = "fp64"):
+    def __init__(self, p: DnsIn, precision: str | int = "fp64", _handle=None):
         self.lib = load_library()
         self.p = p
-        prec = {"fp64": FP64, "mixed": MIXED, "fp64dd": FP64DD}.get(precision, precision) if isinstance(precision, str) else precision
+        prec = _precision(precision)
         self.precision = prec
         self._params = params_struct(p, prec)
-        h = C.c_void_p()
-        rc = self.lib.chgpu_create(C.byref(self._params), C.byref(h))
-        if rc != 0:
-            raise ChannelError(rc, self.lib.chgpu_last_error(None).decode())
+        self._owned = _handle is None
+        if _handle is None:
+            h = C.c_void_p()
+            rc = self.lib.chgpu_create(C.byref(self._params), C.byref(h))
+            if rc != 0:
+                raise ChannelError(rc, self.lib.chgpu_last_error(None).decode())
+        else:
+            h = C.c_void_p(_handle)
         self.h = h
         self.shape = (3, p.nx + 1, 2 * p.nz + 1, p.ny + 3)
 
@@ -152,7 +168,8 @@ class Channel:
 
     def close(self):
         if getattr(self, "h", None):
-            self.lib.chgpu_destroy(self.h)
+            if self._owned:
+                self.lib.chgpu_destroy(self.h)
             self.h = None
 
     def __enter__(self):
@@ -296,3 +313,60 @@ class Channel:
     @property
     def stream(self) -> int:
         return int(self.lib.chgpu_stream(self.h) or 0)
+
+
+class Ensemble:
+    """Independent channel runs (uneven sizes allowed) advanced together: one
+    graph launch per step.  members[i] is a Channel view of member i (upload,
+    start, download, statistics, tiles); closing the ensemble frees them."""
+
+    def __init__(self, params: list, precision: str | int | list = "mixed"):
+        self.lib = load_library()
+        precs = precision if isinstance(precision, list) else [precision] * len(params)
+        arr = (Params * len(params))(*[params_struct(p, _precision(q)) for p, q in zip(params, precs)])
+        e = C.c_void_p()
+        rc = self.lib.chgpu_ensemble_create(arr, len(params), C.byref(e))
+        if rc != 0:
+            raise ChannelError(rc, self.lib.chgpu_ensemble_last_error(None).decode())
+        self.e = e
+        self.members = [Channel(p, q, _handle=self.lib.chgpu_ensemble_member(e, i))
+                        for i, (p, q) in enumerate(zip(params, precs))]
+        self._stats = (Stats * len(params))()
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise ChannelError(rc, self.lib.chgpu_ensemble_last_error(self.e).decode())
+
+    def step(self, sync: bool = True):
+        """One RK3 step of every member; with sync, the Runtimedata records."""
+        if not sync:
+            self._check(self.lib.chgpu_ensemble_step(self.e, None))
+            return None
+        self._check(self.lib.chgpu_ensemble_step(self.e, self._stats))
+        return [np.array(s.line) for s in self._stats]
+
+    def synchronize(self):
+        self._check(self.lib.chgpu_ensemble_synchronize(self.e))
+
+    @property
+    def stream(self) -> int:
+        return self.lib.chgpu_ensemble_stream(self.e)
+
+    def close(self):
+        if getattr(self, "e", None):
+            for m in self.members:
+                m.close()
+            self.lib.chgpu_ensemble_destroy(self.e)
+            self.e = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

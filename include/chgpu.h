@@ -120,6 +120,26 @@ int chgpu_get_stats(chgpu_handle* h, chgpu_stats* st);
  * error flags (non-finite CFL) as CHGPU_E_NONFINITE. */
 int chgpu_synchronize(chgpu_handle* h);
 
+/* Ensemble of independent runs (uneven sizes and precisions allowed): every
+ * member is an ordinary handle, reached with chgpu_ensemble_member for
+ * uploads, chgpu_start, downloads, statistics, tiles or a body force; one
+ * chgpu_ensemble_step advances all members by one RK3 step with a single
+ * CUDA-graph launch whose branches (one per member, each the member's own
+ * 19-launch step) run concurrently.  The graph is re-captured when a
+ * member's launch sequence changes (tiles, body force on/off).  st: NULL, or
+ * one record per member (synchronises).  No counterpart in the reference,
+ * which runs one channel per MPI job. */
+typedef struct chgpu_ensemble chgpu_ensemble;
+int chgpu_ensemble_create(const chgpu_params* params, int n, chgpu_ensemble** out);
+int chgpu_ensemble_destroy(chgpu_ensemble* e);
+int chgpu_ensemble_size(const chgpu_ensemble* e);
+chgpu_handle* chgpu_ensemble_member(chgpu_ensemble* e, int i);
+int chgpu_ensemble_step(chgpu_ensemble* e, chgpu_stats* st);
+int chgpu_ensemble_synchronize(chgpu_ensemble* e);
+void* chgpu_ensemble_stream(chgpu_ensemble* e);
+/* Message of the ensemble's last failing call (or of a failed create). */
+const char* chgpu_ensemble_last_error(const chgpu_ensemble* e);
+
 /* Autotuner of the transform tiles: times the z-transform kernels for 1, 2,
  * 4 and 8 columns per block and the x-row kernel for 1, 2 and 4 rows per
  * block in each of its register-cap variants (compiled for 1, 2 and 3
