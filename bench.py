@@ -275,6 +275,46 @@ def e2e_run(p, V0, prec, K, W):
     return {"s": t1 - t0, "h2d": nbytes, "d2h": nbytes + 8 * 24}
 
 
+def ensemble_run(K=10, W=3, n=64):
+    """The batched-ensemble workload (64 uneven minimal channels, mixed
+    precision, one graph launch per step for all members)."""
+    import torch
+
+    from channel_gb300 import Ensemble, dnsin, initial
+
+    ps = dnsin.ensemble_workloads(n, 0)
+    ens = Ensemble(ps, "mixed")
+    tiles = {}
+    for p, m in zip(ps, ens.members):
+        key = (p.nx, p.ny, p.nz)
+        if key not in tiles:
+            tiles[key] = m.autotune()
+        else:
+            m.set_tiles(tiles[key])
+    for i, (p, m) in enumerate(zip(ps, ens.members)):
+        m.upload(initial.perturbed_laminar(p, 0.01, i))
+        m.start()
+    for _ in range(W):
+        ens.step(sync=False)
+    ens.synchronize()
+    s = torch.cuda.ExternalStream(ens.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(K):
+        ens.step(sync=False)
+    e1.record(s)
+    e1.synchronize()
+    lines = ens.step()
+    ms = e0.elapsed_time(e1) / K
+    ens.close()
+    pts = sum((p.nx + 1) * (2 * p.nz + 1) * (p.ny + 3) for p in ps)
+    ok = all(np.isfinite(l).all() for l in lines)
+    return {"members": n, "precision": "mixed", "ms_per_ensemble_step": ms, "member_steps_per_s": n * 1e3 / ms,
+            "spectral_points": pts, "ns_per_spectral_pt_step": ms * 1e6 / pts, "steps": K, "warmup": W,
+            "finite": ok, "workload": "dnsin.ensemble_workloads(64, seed 0): nx,nz in {16,24,32}, ny in {48,64,96}, "
+                                      "Re 2000-4000, alfa0 1-2, beta0 2-4, dt 0.004; one graph launch per step"}
+
+
 def profiles(V):
     nz = V.shape[2] // 2
     U = V[0, 0, nz, :].real
@@ -381,6 +421,7 @@ def run_ours(args):
         except Exception:
             traffic = None
     e2e = e2e_run(p, V0, "fp64", min(K, 10), 2)
+    ens = ensemble_run()
     cpu = cpu_baseline(p, V0) if rank == 0 else None
 
     def variant(r, dom_, per_, gbs_, tfl_, kin_, what):
@@ -417,6 +458,7 @@ def run_ours(args):
         "mixed": variant(rmx, domm, perm, gbsm, tflm, kinmx,
                          "transforms, products and nonlinear stencils FP32; linear terms double-float; banded "
                          "solves, walls and mean flow FP64"),
+        "ensemble": ens,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": gbs / hbm_peak, "traffic": traffic, "peak_source": peak_src,
                      "launch_ms": per * 1e3,

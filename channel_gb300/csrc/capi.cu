@@ -62,6 +62,7 @@ struct chgpu_handle {
   void* derL = nullptr;
   void* cst = nullptr;  // transform-type constants: factor, 1/dx, 1/dz, 1/dy per plane
   double* d0lu = nullptr;
+  void* lindd = nullptr;  // double-float d1 / D0mat / d0 rows for v' and u, w (mixed path)
   double* yint = nullptr;
   double* dy = nullptr;
   void* twz = nullptr;
@@ -282,6 +283,7 @@ SolveLaunch solve_launch(chgpu_handle* h, const double* ode) {
   L.derT = h->derT;
   L.derL = h->derL;
   L.d0lu = h->d0lu;
+  L.lindd = h->lindd;
   L.yint = h->yint;
   L.sc = h->sc;
   if (ode) {
@@ -380,7 +382,7 @@ void release(chgpu_handle* h) {
     cudaEventDestroy(pe.second.second);
   }
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
-  void* bufs[] = {h->V, h->F, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->derT, h->derL, h->cst, h->d0lu, h->yint, h->dy,
+  void* bufs[] = {h->V, h->F, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->derT, h->derL, h->cst, h->d0lu, h->lindd, h->yint, h->dy,
                   h->twz, h->twx, h->twh, h->sc, h->ex_W, h->ex_P, h->ex_out, h->ex_twz, h->ex_twx};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -508,6 +510,21 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
       if ((rc = upload_roots<double2>(h, &h->twh, 2 * nxd))) break;
       if ((rc = upload_derT<double>(h))) break;
       if ((rc = upload_derL<double>(h))) break;
+    }
+    // mixed path: v' and u, w in double-float (FP64DD keeps them FP64, whose
+    // flow-rate correction amplifies their rounding ~1e3 into Runtimedata);
+    // per y row: d1 row, D0mat factors (rows 1..ny-1), d0 row
+    if (h->prec == CHGPU_MIXED) {
+      std::vector<dd> ld((size_t)(p->ny + 1) * 15, dd());
+      for (int iy = 0; iy <= p->ny; ++iy)
+        for (int j = 0; j < 5; ++j) {
+          ld[(size_t)iy * 15 + j] = from_ld<dd>((long double)t.der[(size_t)iy * 20 + 5 + j]);
+          ld[(size_t)iy * 15 + 10 + j] = from_ld<dd>((long double)t.der[(size_t)iy * 20 + j]);
+          if (iy >= 1 && iy <= p->ny - 1)
+            ld[(size_t)iy * 15 + 5 + j] = from_ld<dd>((long double)t.d0lu[(size_t)(iy - 1) * 5 + j]);
+        }
+      if ((rc = dev_alloc(&h->lindd, sizeof(dd) * ld.size(), "double-float derivative rows"))) break;
+      cudaMemcpy(h->lindd, ld.data(), sizeof(dd) * ld.size(), cudaMemcpyHostToDevice);
     }
     cudaMemcpy(h->der, t.der.data(), sizeof(double) * t.der.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(h->d0lu, t.d0lu.data(), sizeof(double) * t.d0lu.size(), cudaMemcpyHostToDevice);

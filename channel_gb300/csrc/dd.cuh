@@ -115,6 +115,22 @@ __device__ __forceinline__ dd dd_from_double(double v) {
 }
 __device__ __forceinline__ double dd_to_double(dd a) { return (double)a.hi + (double)a.lo; }
 
+// FP32 -> FP64 by bit assembly (sign, exponent rebiased by 1023-127, fraction
+// shifted into place): exact for normal numbers, zero for FP32 subnormals
+// (below 1.2e-38), Inf/NaN kept.  Integer operations only, where the
+// conversion instruction would run on the FP64 pipe.
+__device__ __forceinline__ double f32_to_f64_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned long long frac = (unsigned long long)(u & 0x7fffffu) << 29;
+  if (e == 0u) return __longlong_as_double((long long)sign);
+  const unsigned long long ef = (e == 0xffu) ? 0x7ffull : (unsigned long long)(e + 896u);
+  return __longlong_as_double((long long)(sign | (ef << 52) | frac));
+}
+// double-float -> FP64 with one FP64 addition
+__device__ __forceinline__ double dd_to_double_int(dd a) { return f32_to_f64_bits(a.hi) + f32_to_f64_bits(a.lo); }
+
 // Conversions and constants per arithmetic type T (double, float, dd).
 template <typename T> struct Num;
 template <> struct Num<double> {

@@ -75,6 +75,8 @@ struct SolveLaunch {
   double ode[3];
   double lambda;  // used when lambda_from_dt == 0
   int lambda_from_dt;
+  const void* lindd;  // double-float d1 row, D0mat factors, d0 row per y row: v' and u, w in
+                      // double-float; null: FP64
 };
 
 template <typename T> void launch_rhs(const SolveLaunch& L, cudaStream_t s);

@@ -390,6 +390,129 @@ __device__ __forceinline__ double2 dot5(const double2* v, const double* c) {
 
 }  // namespace
 
+// Arithmetic of the v' / u, w pass: FP64, or double-float in the mixed path
+// (the FP64 pipe is the bound of this kernel).  The Step1
+// result is parked in the field's w slot between the two sweeps (16 bytes
+// either way).
+template <typename R> struct DerivOps;
+template <> struct DerivOps<double> {
+  using C = double2;
+  __device__ static C in(double2 v) { return v; }
+  __device__ static double scal(double v) { return v; }
+  __device__ static C rm(double c, C x) { return make_double2(c * x.x, c * x.y); }
+  __device__ static void park(double2* p, C x) { *p = x; }
+  __device__ static C unpark(const double2* p) { return *p; }
+  __device__ static double2 out(C x) { return x; }
+  // coefficient tables: d1 and d0 rows of der, D0mat factors
+  __device__ static double d1(const double* der, const dd*, int iy, int j) { return __ldg(der + (size_t)iy * 20 + 5 + j); }
+  __device__ static double d0(const double* der, const dd*, int iy, int j) { return __ldg(der + (size_t)iy * 20 + j); }
+  __device__ static double lu(const double* d0lu, const dd*, int iy, int j) { return __ldg(d0lu + (size_t)(iy - 1) * 5 + j); }
+};
+template <> struct DerivOps<dd> {
+  using C = cdd;
+  __device__ static C in(double2 v) { return cdd{dd_from_double(v.x), dd_from_double(v.y)}; }
+  __device__ static dd scal(double v) { return dd_from_double(v); }
+  __device__ static C rm(dd c, C x) { return cdd{c * x.x, c * x.y}; }
+  __device__ static void park(double2* p, C x) { *reinterpret_cast<cdd*>(p) = x; }
+  __device__ static C unpark(const double2* p) { return *reinterpret_cast<const cdd*>(p); }
+  __device__ static double2 out(C x) { return make_double2(dd_to_double_int(x.x), dd_to_double_int(x.y)); }
+  __device__ static dd ld(const dd* t) {
+    const float2 f = __ldg(reinterpret_cast<const float2*>(t));
+    return dd(f.x, f.y);
+  }
+  __device__ static dd d1(const double*, const dd* t, int iy, int j) { return ld(t + (size_t)iy * 15 + j); }
+  __device__ static dd d0(const double*, const dd* t, int iy, int j) { return ld(t + (size_t)iy * 15 + 10 + j); }
+  __device__ static dd lu(const double*, const dd* t, int iy, int j) { return ld(t + (size_t)iy * 15 + 5 + j); }
+};
+
+// One mode per thread: COMPLEXderiv + Step1(D0mat) bottom-up, then
+// Step2(D0mat) and u, w top-down (dnsdata.f90:339-373,
+// linsolve_blocking.inc:99-103).  lindd: per row y, the d1 row, the D0mat
+// factors and the d0 row in double-float (15 values).
+template <typename R>
+__device__ __forceinline__ void deriv_uw(double2* __restrict__ V, const double* __restrict__ der,
+                                         const double* __restrict__ d0lu, const dd* __restrict__ lindd,
+                                         const BcRows& bc, const Dims& d, int m, double ka, double kz, double k2) {
+  using O = DerivOps<R>;
+  using C = typename O::C;
+  const int ny = d.ny;
+  const double rk2 = 1.0 / k2;
+  const R au = O::scal(ka * rk2), bu = O::scal(kz * rk2);
+  C vlo[5], vhi[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    vlo[j] = O::in(V[vidx(d, 1, -1 + j, m)]);
+    vhi[j] = O::in(V[vidx(d, 1, ny - 3 + j, m)]);
+  }
+  auto dot5r = [&](const C* v, const double* c) {
+    C acc = O::rm(O::scal(c[0]), v[0]);
+#pragma unroll
+    for (int j = 1; j < 5; ++j) acc = acc + O::rm(O::scal(c[j]), v[j]);
+    return acc;
+  };
+  const C f0 = dot5r(vlo, bc.d140), fm1 = dot5r(vlo, bc.d14m1);
+  const C fn = dot5r(vhi, bc.d14n), fn1 = dot5r(vhi, bc.d14np1);
+  {
+    C win[5];  // v(iy-2..iy+2) sliding downwards
+    win[1] = vhi[1];
+    win[2] = vhi[2];
+    win[3] = vhi[3];
+    win[4] = vhi[4];
+    C x1 = C(), x2 = C();
+    x1.x = R(); x1.y = R(); x2 = x1;
+    double2 wnext = V[vidx(d, 1, ny - 3, m)];  // v one row ahead
+    for (int iy = ny - 1; iy >= 1; --iy) {
+      win[0] = O::in(wnext);
+      if (iy > 1) wnext = V[vidx(d, 1, iy - 3, m)];
+      C f = O::rm(O::d1(der, lindd, iy, 0), win[0]);
+#pragma unroll
+      for (int j = 1; j < 5; ++j) f = f + O::rm(O::d1(der, lindd, iy, j), win[j]);
+      if (iy == ny - 1) f = f - (O::rm(O::d0(der, lindd, iy, 3), fn) + O::rm(O::d0(der, lindd, iy, 4), fn1));
+      if (iy == ny - 2) f = f - O::rm(O::d0(der, lindd, iy, 4), fn);
+      if (iy == 1) f = f - (O::rm(O::d0(der, lindd, iy, 1), f0) + O::rm(O::d0(der, lindd, iy, 0), fm1));
+      if (iy == 2) f = f - O::rm(O::d0(der, lindd, iy, 0), f0);
+      // Step1 of D0mat: x = A2 (f - A3 x1 - A4 x2)
+      const C s = O::rm(O::lu(d0lu, lindd, iy, 3), x1) + O::rm(O::lu(d0lu, lindd, iy, 4), x2);
+      const C x = O::rm(O::lu(d0lu, lindd, iy, 2), f - s);
+      x2 = x1;
+      x1 = x;
+      O::park(&V[vidx(d, 2, iy, m)], x);
+#pragma unroll
+      for (int j = 4; j > 0; --j) win[j] = win[j - 1];
+    }
+  }
+  {
+    C bm2 = fm1, bm1 = fm1;
+    bm2.x = R(); bm2.y = R();
+    double2 etn = V[vidx(d, 0, -1, m)], xn = make_double2(0.0, 0.0);  // eta and Step1 results one row ahead
+    for (int iy = -1; iy <= ny + 1; ++iy) {
+      const C et = O::in(etn);
+      const double2 xs = xn;
+      if (iy < ny + 1) etn = V[vidx(d, 0, iy + 1, m)];
+      if (iy + 1 >= 1 && iy + 1 <= ny - 1) xn = V[vidx(d, 2, iy + 1, m)];
+      C vp;
+      if (iy == -1) vp = fm1;
+      else if (iy == 0) vp = f0;
+      else if (iy == ny) vp = fn;
+      else if (iy == ny + 1) vp = fn1;
+      else  // Step2 of D0mat: vp = x - (l2 bm2 + l1 bm1)
+        vp = O::unpark(&xs) - (O::rm(O::lu(d0lu, lindd, iy, 0), bm2) + O::rm(O::lu(d0lu, lindd, iy, 1), bm1));
+      if (iy >= 0 && iy <= ny - 1) {
+        bm2 = bm1;
+        bm1 = vp;
+      }
+      // u = (i kx v' - i kz eta)/k2, w = (i kz v' + i kx eta)/k2
+      C u, w;
+      u.x = bu * et.y - au * vp.y;
+      u.y = au * vp.x - bu * et.x;
+      w.x = R() - bu * vp.y - au * et.y;
+      w.y = bu * vp.x + au * et.x;
+      V[vidx(d, 0, iy, m)] = O::out(u);
+      V[vidx(d, 2, iy, m)] = O::out(w);
+    }
+  }
+}
+
 // Two threads per pair (kx, +-kz): role 0 owns the v system (D2vmat), role 1
 // the eta system (etamat; for the mean mode also the unit-forcing response).
 // A block holds 32 pairs: warp 0 the v systems, warp 1 the eta systems.  After
@@ -399,7 +522,8 @@ __global__ void __launch_bounds__(64) k_linsolve(double2* __restrict__ V, const 
                                                  double* __restrict__ fac, const double* __restrict__ der,
                                                  const double* __restrict__ d0lu, const double* __restrict__ yint,
                                                  BcRows bc, Dims d, double lambda_in, double ode1,
-                                                 int lambda_from_dt, DevScalars* __restrict__ sc) {
+                                                 int lambda_from_dt, DevScalars* __restrict__ sc,
+                                                 const dd* __restrict__ lindd) {
   const int lane = threadIdx.x & 31, role = threadIdx.x >> 5;
   const int q = blockIdx.x * 32 + lane;
   const bool active = q < d.npairs;
@@ -610,80 +734,14 @@ __global__ void __launch_bounds__(64) k_linsolve(double2* __restrict__ V, const 
   __syncthreads();  // v and eta of this block's pairs are in V
   if (!active || is00 || role >= nm) return;
 
-  // ---- one mode per thread: COMPLEXderiv + Step1(D0mat) bottom-up, then
-  //      Step2(D0mat) and u, w top-down (dnsdata.f90:339-373, linsolve_blocking.inc:99-103) ----
-  const int m = mm[role];
-  const double kz = (role == 0 ? 1.0 : -1.0) * kb;
-  const double rk2 = 1.0 / k2;
-  const double au = ka * rk2, bu = kz * rk2;
-  double2 vlo[5], vhi[5];
-#pragma unroll
-  for (int j = 0; j < 5; ++j) {
-    vlo[j] = V[vidx(d, 1, -1 + j, m)];
-    vhi[j] = V[vidx(d, 1, ny - 3 + j, m)];
-  }
-  const double2 f0 = dot5(vlo, bc.d140), fm1 = dot5(vlo, bc.d14m1);
-  const double2 fn = dot5(vhi, bc.d14n), fn1 = dot5(vhi, bc.d14np1);
-  {
-    double2 win[5];  // v(iy-2..iy+2) sliding downwards
-    win[1] = vhi[1];
-    win[2] = vhi[2];
-    win[3] = vhi[3];
-    win[4] = vhi[4];
-    double2 x1 = cz(), x2 = cz();
-    double2 wnext = V[vidx(d, 1, ny - 3, m)];  // v one row ahead
-    for (int iy = ny - 1; iy >= 1; --iy) {
-      const double* dr = der + (size_t)iy * 20;
-      win[0] = wnext;
-      if (iy > 1) wnext = V[vidx(d, 1, iy - 3, m)];
-      double2 f = rmul(__ldg(dr + 5), win[0]);
-#pragma unroll
-      for (int j = 1; j < 5; ++j) f = f + rmul(__ldg(dr + 5 + j), win[j]);
-      if (iy == ny - 1) f = f - (rmul(__ldg(dr + 3), fn) + rmul(__ldg(dr + 4), fn1));
-      if (iy == ny - 2) f = f - rmul(__ldg(dr + 4), fn);
-      if (iy == 1) f = f - (rmul(__ldg(dr + 1), f0) + rmul(__ldg(dr + 0), fm1));
-      if (iy == 2) f = f - rmul(__ldg(dr + 0), f0);
-      double A[5];
-#pragma unroll
-      for (int j = 0; j < 5; ++j) A[j] = __ldg(d0lu + (size_t)(iy - 1) * 5 + j);
-      const double2 x = step1(f, A, x1, x2);
-      x2 = x1;
-      x1 = x;
-      V[vidx(d, 2, iy, m)] = x;
-#pragma unroll
-      for (int j = 4; j > 0; --j) win[j] = win[j - 1];
-    }
-  }
-  {
-    double2 bm2 = cz(), bm1 = fm1;
-    double2 etn = V[vidx(d, 0, -1, m)], xn = cz();  // eta and Step1 results one row ahead
-    for (int iy = -1; iy <= ny + 1; ++iy) {
-      const double2 et = etn, xs = xn;
-      if (iy < ny + 1) etn = V[vidx(d, 0, iy + 1, m)];
-      if (iy + 1 >= 1 && iy + 1 <= ny - 1) xn = V[vidx(d, 2, iy + 1, m)];
-      double2 vp;
-      if (iy == -1) vp = fm1;
-      else if (iy == 0) vp = f0;
-      else if (iy == ny) vp = fn;
-      else if (iy == ny + 1) vp = fn1;
-      else {
-        vp = step2(xs, __ldg(d0lu + (size_t)(iy - 1) * 5 + 0), __ldg(d0lu + (size_t)(iy - 1) * 5 + 1), bm2, bm1);
-      }
-      if (iy >= 0 && iy <= ny - 1) {
-        bm2 = bm1;
-        bm1 = vp;
-      }
-      // u = (i kx v' - i kz eta)/k2, w = (i kz v' + i kx eta)/k2
-      V[vidx(d, 0, iy, m)] = make_double2(bu * et.y - au * vp.y, au * vp.x - bu * et.x);
-      V[vidx(d, 2, iy, m)] = make_double2(-(bu * vp.y) - au * et.y, bu * vp.x + au * et.x);
-    }
-  }
+  if (lindd) deriv_uw<dd>(V, der, d0lu, lindd, bc, d, mm[role], ka, (role == 0 ? 1.0 : -1.0) * kb, k2);
+  else deriv_uw<double>(V, der, d0lu, lindd, bc, d, mm[role], ka, (role == 0 ? 1.0 : -1.0) * kb, k2);
 }
 
 void launch_linsolve(const SolveLaunch& L, cudaStream_t s) {
   dim3 grid((L.d.npairs + 31) / 32);
   k_linsolve<<<grid, 64, 0, s>>>(L.V, L.rhs_src, L.rhs_cstride, L.rhs_plane_off, L.fac, L.der, L.d0lu, L.yint, L.bc, L.d, L.lambda, L.ode[0],
-                                  L.lambda_from_dt, L.sc);
+                                  L.lambda_from_dt, L.sc, (const dd*)L.lindd);
 }
 
 // ---------------------------------------------------------------------------
