@@ -450,7 +450,7 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (field " + f"{V0.nbytes / 1e6:.0f} MB" + " + product spectra per step)",
                    "parallelism": f"replicas x{ws}",
                    "tiles": {k: {"z_cols": t[0], "x_rows": t[1], "x_variant": t[2]} for k, t in TILES.items()},
-                   "tiles_from": "chgpu_autotune on the first handle of each precision"},
+                   "tiles_from": "--tiles" if args.tiles else "chgpu_autotune on the first handle of each precision"},
         "ns_per_pt_step": ms64 * 1e6 / gpts,
         "fp64dd": variant(rdd, domd, perd, gbsd, tfld, kindd,
                           "transforms, products and nonlinear stencils in double-float (2 x FP32, ~48 bits) on the "
@@ -532,9 +532,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="retau180", choices=list(AMPLITUDE))
+    ap.add_argument("--tiles", default="",
+                    help="fixed transform tiles instead of autotuning, e.g. fp64:8,4,2/fp64dd:8,4,3/mixed:8,4,3 "
+                         "(z columns, x rows, x-row variant; for reproducible profiler captures)")
     ap.add_argument("--mode", default="full", choices=["full", "timed"],
                     help="timed: only the FP64 and mixed timed runs (for profiler captures)")
     args = ap.parse_args()
+    for item in filter(None, args.tiles.split("/")):
+        prec, t = item.split(":")
+        TILES[prec] = tuple(int(v) for v in t.split(","))
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     from channel_gb300 import build as b
