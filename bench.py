@@ -427,7 +427,8 @@ def run_ours(args):
     def variant(r, dom_, per_, gbs_, tfl_, kin_, what):
         msv = r["ms"] / K
         return {"value": whole_job_steps_per_s(r["ms"], K, ws), "unit": "steps/s", "ms_per_step": msv,
-                "ns_per_pt_step": msv * 1e6 / gpts, "speedup_vs_fp64": ms64 / msv, "arithmetic": what,
+                "ns_per_pt_step": msv * 1e6 / gpts, "ns_per_spectral_pt_step": msv * 1e6 / p.spectral_points(),
+                "speedup_vs_fp64": ms64 / msv, "arithmetic": what,
                 "stats_err_vs_fp64": stats_err(r), "dominant_kernel": dom_, "kernels": kin_,
                 "roofline": {"bound": "hbm", "kernel": dom_, "achieved": gbs_, "peak": hbm_peak, "unit": "GB/s",
                              "frac": gbs_ / hbm_peak, "traffic": None, "launch_ms": per_ * 1e3,
@@ -449,9 +450,11 @@ def run_ours(args):
         "config": {"workload": workload_desc(p, "FP64"), "grid_points": gpts, "spectral_points": p.spectral_points(),
                    "l2": "inputs larger than L2 (field " + f"{V0.nbytes / 1e6:.0f} MB" + " + product spectra per step)",
                    "parallelism": f"replicas x{ws}",
-                   "tiles": {k: {"z_cols": t[0], "x_rows": t[1], "x_variant": t[2]} for k, t in TILES.items()},
+                   "tiles": {k: {"z_cols": t[0], "x_rows": t[1], "x_variant": t[2], "z_threads": t[3],
+                                 "x_threads": t[4]} for k, t in TILES.items()},
                    "tiles_from": "--tiles" if args.tiles else "chgpu_autotune on the first handle of each precision"},
         "ns_per_pt_step": ms64 * 1e6 / gpts,
+        "ns_per_spectral_pt_step": ms64 * 1e6 / p.spectral_points(),
         "fp64dd": variant(rdd, domd, perd, gbsd, tfld, kindd,
                           "transforms, products and nonlinear stencils in double-float (2 x FP32, ~48 bits) on the "
                           "FP32 pipes; linear terms, banded solves, walls and mean flow FP64; meets the FP64 parity bars"),
@@ -533,8 +536,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="retau180", choices=list(AMPLITUDE))
     ap.add_argument("--tiles", default="",
-                    help="fixed transform tiles instead of autotuning, e.g. fp64:8,4,2/fp64dd:8,4,3/mixed:8,4,3 "
-                         "(z columns, x rows, x-row variant; for reproducible profiler captures)")
+                    help="fixed transform tiles instead of autotuning, e.g. fp64:8,4,2,256,256/mixed:8,4,3,256,192 "
+                         "(z columns, x rows, x-row variant, z threads, x threads; for reproducible profiler "
+                         "captures)")
     ap.add_argument("--mode", default="full", choices=["full", "timed"],
                     help="timed: only the FP64 and mixed timed runs (for profiler captures)")
     args = ap.parse_args()

@@ -45,6 +45,7 @@ struct chgpu_handle {
   int prec = CHGPU_FP64;  // CHGPU_FP64, CHGPU_MIXED or CHGPU_FP64DD
   int zcols = 1, xrows = 1;
   int xminb = 2;  // register-cap variant of the x-row kernel
+  int zthreads = 256, xthreads = 256;  // threads per block of the transform kernels
   bool tuned = false;
   cudaStream_t stream = nullptr;
   // device buffers
@@ -262,6 +263,8 @@ ConvLaunch conv_launch(chgpu_handle* h, int compute_cfl, int products, int plane
   L.zcols = h->zcols;
   L.xrows = h->xrows;
   L.xminb = h->xminb;
+  L.zthreads = h->zthreads;
+  L.xthreads = h->xthreads;
   L.plane0 = plane0;
   L.nplanes = nplanes;
   L.compute_cfl = compute_cfl;
@@ -932,24 +935,41 @@ int chgpu_autotune(chgpu_handle* h) {
   // valid spectra in the work buffers before timing the later stages
   if (int rc = time_conv_stage(h, 0, 1, &ms)) return rc;
   if (int rc = time_conv_stage(h, 1, 1, &ms)) return rc;
-  // columns per block of the two z-transform kernels
+  // columns per block of the two z-transform kernels, then their block size
   int best_z = h->zcols;
   float best = 1e30f;
-  for (int zc = 1; zc <= 8; zc *= 2) {
-    if (conv_z_smem(zc, nzd, ts) > lim) break;
-    h->zcols = zc;
+  auto time_z = [&](float* t) -> int {
     float m0 = 0, m2 = 0;
     if (int rc = time_conv_stage(h, 0, reps, &m0)) return rc;
     if (int rc = time_conv_stage(h, 2, reps, &m2)) return rc;
-    if (m0 + m2 < best) {
-      best = m0 + m2;
+    *t = m0 + m2;
+    return 0;
+  };
+  h->zthreads = 256;
+  for (int zc = 1; zc <= 8; zc *= 2) {
+    if (conv_z_smem(zc, nzd, ts) > lim) break;
+    h->zcols = zc;
+    if (int rc = time_z(&ms)) return rc;
+    if (ms < best) {
+      best = ms;
       best_z = zc;
     }
   }
   h->zcols = best_z;
-  // rows per block and register-cap variant of the x-row kernel
+  int best_zt = 256;
+  for (int zt : {128, 192}) {
+    h->zthreads = zt;
+    if (int rc = time_z(&ms)) return rc;
+    if (ms < best) {
+      best = ms;
+      best_zt = zt;
+    }
+  }
+  h->zthreads = best_zt;
+  // rows per block and register-cap variant of the x-row kernel, then its block size
   int best_r = h->xrows, best_b = h->xminb;
   best = 1e30f;
+  h->xthreads = 256;
   for (int xb = 1; xb <= 3; ++xb)
     for (int xr = 1; xr <= 4; xr *= 2) {
       if (nzd % xr != 0 || conv_x_smem(xr, nxd, ts) > lim) continue;
@@ -964,6 +984,16 @@ int chgpu_autotune(chgpu_handle* h) {
     }
   h->xrows = best_r;
   h->xminb = best_b;
+  int best_xt = 256;
+  for (int xt : {128, 192}) {
+    h->xthreads = xt;
+    if (int rc = time_conv_stage(h, 1, reps, &ms)) return rc;
+    if (ms < best) {
+      best = ms;
+      best_xt = xt;
+    }
+  }
+  h->xthreads = best_xt;
   h->tuned = true;
   ++h->version;
   if (h->graph) {  // the captured step holds the old launch shapes
@@ -973,19 +1003,23 @@ int chgpu_autotune(chgpu_handle* h) {
   return 0;
 }
 
-int chgpu_set_tiles(chgpu_handle* h, const int tiles[3]) {
+int chgpu_set_tiles(chgpu_handle* h, const int tiles[CHGPU_NTILES]) {
   if (!h || !tiles) return fail(h, CHGPU_E_PARAM, "chgpu_set_tiles: null argument");
   int dev = 0, optin = 0;
   CK(h, cudaGetDevice(&dev));
   CK(h, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   const size_t ts = tsize(h), lim = (size_t)optin - 1024;
-  const int zc = tiles[0], xr = tiles[1], xb = tiles[2];
+  const int zc = tiles[0], xr = tiles[1], xb = tiles[2], zt = tiles[3], xt = tiles[4];
+  auto threads_ok = [](int t) { return t >= 64 && t <= 256 && t % 32 == 0; };
   if (zc < 1 || zc > 8 || conv_z_smem(zc, h->d.nzd, ts) > lim || (xr != 1 && xr != 2 && xr != 4) ||
-      h->d.nzd % xr != 0 || conv_x_smem(xr, h->d.nxd, ts) > lim || xb < 1 || xb > 3)
+      h->d.nzd % xr != 0 || conv_x_smem(xr, h->d.nxd, ts) > lim || xb < 1 || xb > 3 || !threads_ok(zt) ||
+      !threads_ok(xt))
     return fail(h, CHGPU_E_PARAM, "chgpu_set_tiles: tiles outside what this handle's sizes allow");
   h->zcols = zc;
   h->xrows = xr;
   h->xminb = xb;
+  h->zthreads = zt;
+  h->xthreads = xt;
   ++h->version;
   if (h->graph) {
     cudaGraphExecDestroy(h->graph);
@@ -994,11 +1028,13 @@ int chgpu_set_tiles(chgpu_handle* h, const int tiles[3]) {
   return 0;
 }
 
-int chgpu_tiles(const chgpu_handle* h, int tiles[3]) {
+int chgpu_tiles(const chgpu_handle* h, int tiles[CHGPU_NTILES]) {
   if (!h || !tiles) return CHGPU_E_PARAM;
   tiles[0] = h->zcols;
   tiles[1] = h->xrows;
   tiles[2] = h->xminb;
+  tiles[3] = h->zthreads;
+  tiles[4] = h->xthreads;
   return 0;
 }
 

@@ -220,19 +220,19 @@ void launch_convolutions(const ConvLaunch& L, cudaStream_t s, int stage) {
   if (stage == 0) {
     dim3 grid((nxp + L.zcols - 1) / L.zcols, L.nplanes, 3);
     size_t sm = conv_z_smem(L.zcols, d.nzd, sizeof(V2));
-    k_zinv<T><<<grid, 256, sm, s>>>(L.V, (V2*)L.Zb, (const V2*)L.twz, d, L.rz, L.zcols, L.plane0);
+    k_zinv<T><<<grid, L.zthreads, sm, s>>>(L.V, (V2*)L.Zb, (const V2*)L.twz, d, L.rz, L.zcols, L.plane0);
   }
   if (stage == 1) {
     dim3 grid(d.nzd / L.xrows, L.nplanes);
     size_t sm = conv_x_smem(L.xrows, d.nxd, sizeof(V2));
     auto kern = L.xminb == 1 ? k_xrow<T, 1> : L.xminb == 3 ? k_xrow<T, 3> : k_xrow<T, 2>;
-    kern<<<grid, 256, sm, s>>>((const V2*)L.Zb, (V2*)L.Pb, (const V2*)L.twx, (const V2*)L.twh, (const T*)L.cst, d, L.rx,
+    kern<<<grid, L.xthreads, sm, s>>>((const V2*)L.Zb, (V2*)L.Pb, (const V2*)L.twx, (const V2*)L.twh, (const T*)L.cst, d, L.rx,
                                L.xrows, L.plane0, L.compute_cfl, L.sc);
   }
   if (stage == 2) {
     dim3 grid((nxp + L.zcols - 1) / L.zcols, L.nplanes, 6);
     size_t sm = conv_z_smem(L.zcols, d.nzd, sizeof(V2));
-    k_zfwd<T><<<grid, 256, sm, s>>>((const V2*)L.Pb, (V2*)L.VV, (const V2*)L.twz, d, L.rz, L.zcols, L.plane0);
+    k_zfwd<T><<<grid, L.zthreads, sm, s>>>((const V2*)L.Pb, (V2*)L.VV, (const V2*)L.twz, d, L.rz, L.zcols, L.plane0);
   }
 }
 

@@ -42,6 +42,7 @@ struct ConvLaunch {
   DevScalars* sc;
   int zcols, xrows;
   int xminb;  // register-cap variant of the x-row kernel (1, 2 or 3 blocks per SM)
+  int zthreads, xthreads;  // threads per block of the z-transform and x-row kernels (<= 256)
   int plane0, nplanes;
   int compute_cfl;
   int products;  // 0: stop after the x pass (the start-up CFL pass)

@@ -243,19 +243,20 @@ class Channel:
         self._check(self.lib.chgpu_kernel_times(self.h, _dp(ms), n))
         return {self.lib.chgpu_kernel_kind_name(k).decode(): (float(ms[k]), int(n[k])) for k in range(NKINDS)}
 
-    def autotune(self) -> tuple[int, int, int]:
+    def autotune(self) -> tuple:
         """Times the transform tiles on this handle and keeps the fastest;
-        returns (z columns, x rows, x-row register variant)."""
+        returns them (see tiles())."""
         self._check(self.lib.chgpu_autotune(self.h))
         return self.tiles()
 
-    def tiles(self) -> tuple[int, int, int]:
-        t = (C.c_int * 3)()
+    def tiles(self) -> tuple:
+        """(z columns, x rows, x-row variant, z threads, x threads)."""
+        t = (C.c_int * 5)()
         self._check(self.lib.chgpu_tiles(self.h, t))
-        return t[0], t[1], t[2]
+        return tuple(t)
 
     def set_tiles(self, tiles) -> None:
-        self._check(self.lib.chgpu_set_tiles(self.h, (C.c_int * 3)(*tiles)))
+        self._check(self.lib.chgpu_set_tiles(self.h, (C.c_int * 5)(*tiles)))
 
     def export_dims(self, undersample: float = 1.0) -> tuple[int, int, int]:
         d = (C.c_int * 3)()

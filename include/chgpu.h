@@ -141,19 +141,22 @@ void* chgpu_ensemble_stream(chgpu_ensemble* e);
 const char* chgpu_ensemble_last_error(const chgpu_ensemble* e);
 
 /* Autotuner of the transform tiles: times the z-transform kernels for 1, 2,
- * 4 and 8 columns per block and the x-row kernel for 1, 2 and 4 rows per
- * block in each of its register-cap variants (compiled for 1, 2 and 3
- * resident blocks per SM) on this handle's sizes, and keeps the fastest.
- * Takes a few dozen kernel launches; the field, the RK history and the
- * module scalars are untouched, and the results of a step do not depend on
- * the tiles.  Optional: without it the handle uses tiles sized from the
+ * 4 and 8 columns per block and then 128, 192 or 256 threads per block, and
+ * the x-row kernel for 1, 2 and 4 rows per block in each of its
+ * register-cap variants (compiled for 1, 2 and 3 resident blocks per SM) and
+ * then its block size, on this handle's sizes, and keeps the fastest.  Takes
+ * a few dozen kernel launches; the field, the RK history and the module
+ * scalars are untouched, and the results of a step do not depend on the
+ * tiles.  Optional: without it the handle uses tiles sized from the
  * shared-memory budget.  No counterpart in the reference. */
+#define CHGPU_NTILES 5
 int chgpu_autotune(chgpu_handle* h);
-/* tiles = {z columns per block, x rows per block, x-row register variant}. */
-int chgpu_tiles(const chgpu_handle* h, int tiles[3]);
+/* tiles = {z columns per block, x rows per block, x-row register variant,
+ *          z threads per block, x threads per block}. */
+int chgpu_tiles(const chgpu_handle* h, int tiles[CHGPU_NTILES]);
 /* Applies tiles found by chgpu_autotune on another handle of the same sizes
  * and precision; CHGPU_E_PARAM when they do not fit this handle. */
-int chgpu_set_tiles(chgpu_handle* h, const int tiles[3]);
+int chgpu_set_tiles(chgpu_handle* h, const int tiles[CHGPU_NTILES]);
 
 /* Physical-space export of the field: the reference's exporter
  * out_exporter/out2bin.f90 (convert_outfile :141-203, xz_interpolation

@@ -199,6 +199,31 @@ def test_autotuned_tiles_give_identical_steps(gpu_lib, prec):
     from channel_gb300 import ChannelError
 
     with pytest.raises(ChannelError):
-        u.set_tiles((9, 3, 1))
+        u.set_tiles((9, 3, 1, 256, 256))
     for h in (g, t, u):
         h.close()
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("fp64dd", 1e-12), ("mixed", 1e-9)])
+def test_stepped_field_is_divergence_free(gpu_lib, prec, tol):
+    """i alfa u + v' + i beta w = 0 mode by mode (the solenoidal condition the
+    v-eta recovery of u and w builds in, linsolve_blocking.inc:99-103), with
+    v' the oracle's compact derivative of the GPU's v."""
+    p, _, o, g = make("small", 0.05, 4, prec)
+    g.start()
+    for _ in range(5):
+        g.step()
+    V = g.download()
+    nz = p.nz
+    worst = 0.0
+    for ix in range(p.nx + 1):
+        for iz in range(-nz, nz + 1):
+            if ix == 0 and iz == 0:
+                continue
+            u, v, w = V[0, ix, iz + nz], V[1, ix, iz + nz], V[2, ix, iz + nz]
+            vp = o.deriv(v)
+            res = 1j * p.alfa0 * ix * u + vp + 1j * p.beta0 * iz * w
+            scale = max(np.abs(vp).max(), np.abs(p.alfa0 * ix * u).max(), 1e-30)
+            worst = max(worst, float(np.abs(res).max() / scale))
+    assert worst <= tol, worst
+    g.close()

@@ -235,3 +235,27 @@ def test_oracle_body_force_ghost_rows_are_rebuilt(oracle_mod):
     o.step()
     assert not np.array_equal(o.field(), out[0])
     o.close()
+
+
+def test_oracle_stepped_field_is_divergence_free(oracle_mod):
+    """i alfa u + v' + i beta w = 0 for every mode of a stepped field
+    (linsolve_blocking.inc:99-103 builds u, w from v' and eta)."""
+    p = dnsin.workload("small")
+    p.nx, p.ny, p.nz = 8, 24, 8
+    o = oracle_mod.Oracle(p)
+    o.set_field(initial.perturbed_laminar(p, 0.05, 2))
+    o.start()
+    for _ in range(3):
+        o.step()
+    V = o.field()
+    worst = 0.0
+    for ix in range(p.nx + 1):
+        for iz in range(-p.nz, p.nz + 1):
+            if ix == 0 and iz == 0:
+                continue
+            u, v, w = V[0, ix, iz + p.nz], V[1, ix, iz + p.nz], V[2, ix, iz + p.nz]
+            vp = o.deriv(v)
+            res = 1j * p.alfa0 * ix * u + vp + 1j * p.beta0 * iz * w
+            worst = max(worst, float(np.abs(res).max() / max(np.abs(vp).max(), 1e-30)))
+    o.close()
+    assert worst <= 1e-13, worst
