@@ -446,7 +446,9 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
   std::memcpy(h->bc.etanbc, t.etanbc, 40); std::memcpy(h->bc.etanp1bc, t.etanp1bc, 40);
   std::memcpy(h->bc.d140, t.d140, 40); std::memcpy(h->bc.d14m1, t.d14m1, 40);
   std::memcpy(h->bc.d14n, t.d14n, 40); std::memcpy(h->bc.d14np1, t.d14np1, 40);
-  Radix rz = make_radix(nzd), rx = make_radix(nxd);
+  // composite tail stage where measured faster: the FP32 x transforms (the
+  // z ones lose occupancy to its registers)
+  Radix rz = make_radix(nzd, false), rx = make_radix(nxd, h->prec == CHGPU_MIXED);
   if (rz.nst < 0 || rx.nst < 0) { delete h; return fail(nullptr, CHGPU_E_PARAM, "unsupported FFT length"); }
   h->rz.n = rz.n; h->rz.nst = rz.nst; std::memcpy(h->rz.r, rz.r, sizeof rz.r);
   h->rx.n = rx.n; h->rx.nst = rx.nst; std::memcpy(h->rx.r, rx.r, sizeof rx.r);

@@ -50,7 +50,9 @@ struct Radix {
   int n = 0, nst = 0;
   int r[24];
 };
-Radix make_radix(int n);
+// radices 16, then 8/4/2, then 3; with composite, a tail of 6, 12 or 24
+// points is one stage
+Radix make_radix(int n, bool composite = false);
 
 // Scalars the reference keeps as module globals, resident on the device so
 // that whole steps (including the CFL-driven time step) run without the host.

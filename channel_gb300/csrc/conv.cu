@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(256, MINB) k_xrow(const typename C2<T>::t* __r
     A[pad32(idx)] = e + mul_is<+1>(o);
   }
   __syncthreads();
-  V2* U = fft_block<+1>(A, B, 3 * nrows, rx, twx);
+  V2* U = fft_block<+1, V2, true>(A, B, 3 * nrows, rx, twx);
   V2* freeb = (U == A) ? B : A;
   // CFL (dnsdata.f90:552-556) and products uu,vv,ww (:584)
   const T f = cst[0];
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(256, MINB) k_xrow(const typename C2<T>::t* __r
       }
       __syncthreads();
     }
-    V2* P = fft_block<-1>(Cb, freeb, 3 * nrows, rx, twx);
+    V2* P = fft_block<-1, V2, true>(Cb, freeb, 3 * nrows, rx, twx);
     // r2c unpacking, kx = 0..nx (HFT + xTOz, dnsdata.f90:586-588)
     for (int idx = threadIdx.x; idx < 3 * nxp * nrows; idx += blockDim.x) {
       const int r = idx & (nrows - 1);

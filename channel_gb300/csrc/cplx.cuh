@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "dd.cuh"
 
 namespace chgpu {
@@ -67,6 +69,34 @@ template <int SIGN, typename V> __device__ __forceinline__ V cmul_s(V a, V w) {
 }
 template <int SIGN> __device__ __forceinline__ cdd cmul_s(cdd a, cdd w) {
   return SIGN < 0 ? cmul(a, w) : cdd{dd_dot2(a.x, w.x, a.y, w.y), dd_dot2(a.y, w.x, -a.x, w.y)};
+}
+
+// w_N^m = exp(SIGN 2 pi i m / N) for N dividing 24 (m fixed at compile
+// time after unrolling), from the constants of the type: angles are
+// multiples of 15 degrees.
+template <int N, int SIGN, typename V> __device__ __forceinline__ V root(int m) {
+  using T = decltype(V::x);
+  const int e = (m * (24 / N)) % 24;  // in units of 15 degrees
+  const T c15 = Num<T>::cos_pi12(), s15 = Num<T>::sin_pi12(), c30 = Num<T>::sqrt3_2(), h = T(0.5f);
+  const T r2 = Num<T>::sqrt1_2(), one = T(1.0f), zero = T();
+  // cos and sin of e * 15 degrees for e in [0, 6], then quadrant by symmetry
+  const int q = e / 6, f = e % 6;
+  T c, s;
+  switch (f) {
+    case 0: c = one; s = zero; break;
+    case 1: c = c15; s = s15; break;
+    case 2: c = c30; s = h; break;
+    case 3: c = r2; s = r2; break;
+    case 4: c = h; s = c30; break;
+    default: c = s15; s = c15; break;
+  }
+  // rotate by q quarter turns: (c, s) -> (-s, c)
+  for (int i = 0; i < q; ++i) {
+    const T t = c;
+    c = zero - s;
+    s = t;
+  }
+  return mk<V>(c, SIGN > 0 ? s : zero - s);
 }
 
 // In-register DFTs of length R (natural order in and out), SIGN -1: exp(-i),
@@ -155,6 +185,45 @@ template <typename V> struct Dft<16, V> {
   }
 };
 
+// Composite register DFTs of length 3 P (P = 2, 4, 8): r = P r1 + r2,
+// k = k1 + 3 k2 -- DFT3 over r1 for each r2, twiddle w_{3P}^(r2 k1), DFT_P
+// over r2 for each k1.  w(m) is w_{3P}^m for the transform's sign.
+template <int P, typename V> struct DftComposite {
+  template <int SIGN> __device__ static void run(V* a) {
+    using T = decltype(V::x);
+    constexpr int N = 3 * P;
+#pragma unroll
+    for (int r2 = 0; r2 < P; ++r2) {
+      V b[3] = {a[r2], a[P + r2], a[2 * P + r2]};
+      Dft<3, V>::template run<SIGN>(b);
+      a[r2] = b[0];
+      a[P + r2] = b[1];
+      a[2 * P + r2] = b[2];
+    }
+    // a[k1 P + r2] holds the DFT3 output k1 of column r2
+#pragma unroll
+    for (int k1 = 1; k1 < 3; ++k1)
+#pragma unroll
+      for (int r2 = 1; r2 < P; ++r2) a[k1 * P + r2] = cmul(a[k1 * P + r2], root<N, SIGN, V>(r2 * k1));
+    V y[N];
+#pragma unroll
+    for (int k1 = 0; k1 < 3; ++k1) {
+      V c[P];
+#pragma unroll
+      for (int r2 = 0; r2 < P; ++r2) c[r2] = a[k1 * P + r2];
+      Dft<P, V>::template run<SIGN>(c);
+#pragma unroll
+      for (int k2 = 0; k2 < P; ++k2) y[k1 + 3 * k2] = c[k2];
+    }
+#pragma unroll
+    for (int k = 0; k < N; ++k) a[k] = y[k];
+    (void)sizeof(T);
+  }
+};
+template <typename V> struct Dft<6, V> : DftComposite<2, V> {};
+template <typename V> struct Dft<12, V> : DftComposite<4, V> {};
+template <typename V> struct Dft<24, V> : DftComposite<8, V> {};
+
 // read-only load of a complex value of any of the three types
 template <typename V> __device__ __forceinline__ V ldg_v(const V* p) { return __ldg(p); }
 template <> __device__ __forceinline__ cdd ldg_v<cdd>(const cdd* p) {
@@ -198,15 +267,29 @@ __device__ __forceinline__ void stockham_stage(const V* __restrict__ src, V* __r
 // Batched in-shared-memory FFT: B transforms of length rad.n, contiguous in
 // the padded layout, in `a`; `b` is scratch of the same size.  Unnormalised;
 // SIGN -1: exp(-i...), +1: exp(+i...).  `tw` is the per-stage twiddle table
-// of this length (make_stage_twiddles).  Returns the buffer holding the
-// result.  Every thread of the block calls it.
-template <int SIGN, typename V>
+// of this length.  COMPOSITE compiles the 6/12/24-point tail stages in (FP32
+// only; their registers would cost the other kernels occupancy).  Returns the
+// buffer holding the result.  Every thread of the block calls it.
+template <int SIGN, typename V, bool COMPOSITE = false>
 __device__ V* fft_block(V* a, V* b, int B, const RadixDev& rad, const V* __restrict__ tw) {
   const int n = rad.n;
   int Ns = 1;
   for (int st = 0; st < rad.nst; ++st) {
     const int R = rad.r[st];
     const V* twst = tw + rad.twoff[st];
+    if constexpr (COMPOSITE && std::is_same<V, float2>::value) {  // composite tails: FP32 x plans only
+      if (R == 24 || R == 12 || R == 6) {
+        if (R == 24) stockham_stage<24, SIGN>(a, b, B, n, Ns, twst);
+        else if (R == 12) stockham_stage<12, SIGN>(a, b, B, n, Ns, twst);
+        else stockham_stage<6, SIGN>(a, b, B, n, Ns, twst);
+        __syncthreads();
+        V* tmp = a;
+        a = b;
+        b = tmp;
+        Ns *= R;
+        continue;
+      }
+    }
     switch (R) {
       case 16: stockham_stage<16, SIGN>(a, b, B, n, Ns, twst); break;
       case 8: stockham_stage<8, SIGN>(a, b, B, n, Ns, twst); break;

@@ -143,6 +143,8 @@ template <> struct Num<double> {
   __device__ static constexpr double cos_pi8() { return 0.9238795325112867; }
   __device__ static constexpr double sin_pi8() { return 0.3826834323650898; }
   __device__ static constexpr double sqrt1_2() { return 0.7071067811865476; }
+  __device__ static constexpr double cos_pi12() { return 0.9659258262890683; }
+  __device__ static constexpr double sin_pi12() { return 0.25881904510252074; }
 };
 template <> struct Num<float> {
   __device__ static float from_double(double v) { return (float)v; }
@@ -154,6 +156,8 @@ template <> struct Num<float> {
   __device__ static constexpr float cos_pi8() { return 0.923879533f; }
   __device__ static constexpr float sin_pi8() { return 0.382683432f; }
   __device__ static constexpr float sqrt1_2() { return 0.707106781f; }
+  __device__ static constexpr float cos_pi12() { return 0.965925826f; }
+  __device__ static constexpr float sin_pi12() { return 0.258819045f; }
 };
 template <> struct Num<dd> {
   __device__ static dd from_double(double v) { return dd_from_double(v); }
@@ -165,6 +169,8 @@ template <> struct Num<dd> {
   __device__ static constexpr dd cos_pi8() { return dd(0.923879504f, 2.83074897e-08f); }
   __device__ static constexpr dd sin_pi8() { return dd(0.382683426f, 6.22335072e-09f); }
   __device__ static constexpr dd sqrt1_2() { return dd(0.707106769f, 1.21016175e-08f); }
+  __device__ static constexpr dd cos_pi12() { return dd(0.965925813f, 1.35678162e-08f); }
+  __device__ static constexpr dd sin_pi12() { return dd(0.258819044f, 1.46619872e-09f); }
 };
 
 }  // namespace chgpu

@@ -27,11 +27,13 @@ void padded_sizes(int nx, int nz, int* nxd, int* nzd) {
   *nzd = b;
 }
 
-Radix make_radix(int n) {
+Radix make_radix(int n, bool composite) {
   Radix r;
   r.n = n;
   int m = n;
   while (m % 16 == 0) { r.r[r.nst++] = 16; m /= 16; }
+  // the tail 2^b * 3 (b = 1..3) as one register DFT of 6, 12 or 24 points
+  if (composite && (m == 6 || m == 12 || m == 24)) { r.r[r.nst++] = m; m = 1; }
   if (m % 8 == 0) { r.r[r.nst++] = 8; m /= 8; }
   else if (m % 4 == 0) { r.r[r.nst++] = 4; m /= 4; }
   else if (m % 2 == 0) { r.r[r.nst++] = 2; m /= 2; }
