@@ -77,8 +77,16 @@ template <> __device__ __forceinline__ float store_as<float>(dd x) { return __fa
 template <typename T> struct HistT { using t = typename C2<T>::t; };
 template <> struct HistT<dd> { using t = double2; };
 
-template <typename T>
-__global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, const typename C2<T>::t* __restrict__ VV,
+// resident 128-thread blocks per SM the registers are capped for
+template <typename T> struct RhsBlocks { static constexpr int value = 4; };
+template <> struct RhsBlocks<float> { static constexpr int value = 3; };
+template <> struct RhsBlocks<dd> { static constexpr int value = 5; };
+
+// RB consecutive rows per thread: the five-row windows of the products and
+// of the field slide down the rows, so each row is loaded (and, in the mixed
+// path, converted to double-float) once instead of five times.
+template <typename T, int RB>
+__global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2* __restrict__ V, const typename C2<T>::t* __restrict__ VV,
                                              typename HistT<T>::t* __restrict__ old, double2* __restrict__ rhs,
                                              const typename LinT<T>::t* __restrict__ derL, const T* __restrict__ derT,
                                              Dims d, double ode1, double ode2, double ode3,
@@ -87,7 +95,8 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
   using O2 = typename HistT<T>::t;
   using OT = decltype(O2::x);
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  const int iy = blockIdx.y + 1;
+  const int iy0 = blockIdx.y * RB + 1;
+  const int nrows = min(RB, d.ny - iy0);
   // ---- linear terms of the field in L (FP64, or double-float in the mixed
   //      path: the FP64 pipe is 1/58 of FP32 here) ----
   // timescheme (dnsdata.f90:486) combines ODE(1)/deltat * unkn + impl, which
@@ -96,32 +105,69 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
   // and for eta (:658) with w = i kz V1 - i kx V3
   //   lambda S0(w) + ni (S2(w) - k2 S0(w)) = sum_j (D_j + k2 E_j) w_j,
   // the mean mode (:653) being the k2 = 0 case on (U, W).  The per-row
-  // coefficients A..E are formed once per block.
+  // coefficients A..E are formed once per block and row.
   using L = typename LinT<T>::t;
   using LV = typename C2<L>::t;
   const size_t tailL = (size_t)(d.ny + 1) * 20;  // der rows, then alfa0, beta0, ni
-  __shared__ __align__(16) unsigned char cf_raw[25 * sizeof(L)];
+  __shared__ __align__(16) unsigned char cf_raw[RB * 25 * sizeof(L)];
   L* cf = reinterpret_cast<L*>(cf_raw);
-  if (std::is_same<L, dd>::value && threadIdx.x < 5) {
-    const int j = threadIdx.x;
-    const L* dr = derL + (size_t)iy * 20;
+  for (int t = threadIdx.x; std::is_same<L, dd>::value && t < 5 * nrows; t += blockDim.x) {
+    const int j = t % 5, rr = t / 5;
+    const L* dr = derL + (size_t)(iy0 + rr) * 20;
     const L c0 = dr[j], c2 = dr[10 + j], c4 = dr[15 + j];
     const L lam = Num<L>::from_double(ode1 * sc->rdt);  // ODE(1)/deltat
     const L nu = derL[tailL + 2];
-    cf[j] = lam * c2 + nu * c4;
-    cf[5 + j] = L() - (lam * c0 + (nu + nu) * c2);
-    cf[10 + j] = nu * c0;
-    cf[15 + j] = lam * c0 + nu * c2;
-    cf[20 + j] = L() - nu * c0;
+    L* c = cf + rr * 25;
+    c[j] = lam * c2 + nu * c4;
+    c[5 + j] = L() - (lam * c0 + (nu + nu) * c2);
+    c[10 + j] = nu * c0;
+    c[15 + j] = lam * c0 + nu * c2;
+    c[20 + j] = L() - nu * c0;
   }
   __syncthreads();
   if (m >= d.nmodes) return;
   const int ix = m / d.nzt;
   const int iz = m - ix * d.nzt - d.nz;
-  // wavenumbers and stencil coefficients in T (derT holds der in T, then alfa0, beta0)
-  const T* drT = derT + (size_t)iy * 20;
+  // wavenumbers (derT holds der in T, then alfa0, beta0; derL likewise in L, then ni)
   const size_t tail = (size_t)(d.ny + 1) * 20;
   const T ta = T((float)ix) * derT[tail], tb = T((float)iz) * derT[tail + 1];
+  const T tk2 = ta * ta + tb * tb;
+  const L a = L((float)ix) * derL[tailL], b = L((float)iz) * derL[tailL + 1];
+  const L k2 = a * a + b * b;
+  const L lode2 = Num<L>::from_double(ode2), lode3 = Num<L>::from_double(ode3);
+  const L lam = Num<L>::from_double(ode1 * sc->rdt), nu = derL[tailL + 2];
+  // windows over rows iy-2..iy+2: the six product spectra (plane = row + 1) and the field
+  V2 vv[6][5];
+  LV v1[5], v2[5], v3[5];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) vv[k][j + 1] = VV[((size_t)k * d.nplanes + (iy0 - 1 + j)) * d.nmodes + m];
+    v1[j + 1] = cvt2<LV>(V[vidx(d, 0, iy0 - 2 + j, m)]);
+    v2[j + 1] = cvt2<LV>(V[vidx(d, 1, iy0 - 2 + j, m)]);
+    v3[j + 1] = cvt2<LV>(V[vidx(d, 2, iy0 - 2 + j, m)]);
+  }
+#pragma unroll 1
+  for (int rr = 0; rr < RB; ++rr) {
+  if (rr >= nrows) break;
+  const int iy = iy0 + rr;
+  const L* cfr = cf + rr * 25;
+  // slide the windows one row down and load row iy+2
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) vv[k][j] = vv[k][j + 1];
+    v1[j] = v1[j + 1];
+    v2[j] = v2[j + 1];
+    v3[j] = v3[j + 1];
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) vv[k][4] = VV[((size_t)k * d.nplanes + (iy + 3)) * d.nmodes + m];
+  v1[4] = cvt2<LV>(V[vidx(d, 0, iy + 2, m)]);
+  v2[4] = cvt2<LV>(V[vidx(d, 1, iy + 2, m)]);
+  v3[4] = cvt2<LV>(V[vidx(d, 2, iy + 2, m)]);
+  // stencil coefficients of this row in T
+  const T* drT = derT + (size_t)iy * 20;
   T e0[5], e1[5], e2[5];
 #pragma unroll
   for (int j = 0; j < 5; ++j) {
@@ -130,11 +176,6 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
     e2[j] = drT[10 + j];
   }
   // DD(f,k) (dnsdata.f90:609-610) on product k (0-based) at rows iy-2..iy+2
-  V2 vv[6][5];
-#pragma unroll
-  for (int k = 0; k < 6; ++k)
-#pragma unroll
-    for (int j = 0; j < 5; ++j) vv[k][j] = VV[((size_t)k * d.nplanes + (iy - 1 + j)) * d.nmodes + m];
   auto DD = [&](const T* c, int k) -> V2 {
     V2 s = mk<V2>(c[0] * vv[k][0].x, c[0] * vv[k][0].y);
 #pragma unroll
@@ -145,12 +186,9 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
   const V2 rhsu = czero<V2>() - mul_ia<V2>(ta, DD(e0, 0)) - DD(e1, 3) - mul_ia<V2>(tb, DD0_6);
   const V2 rhsv = czero<V2>() - mul_ia<V2>(ta, DD(e0, 3)) - DD(e1, 1) - mul_ia<V2>(tb, DD(e0, 4));
   const V2 rhsw = czero<V2>() - mul_ia<V2>(ta, DD0_6) - DD(e1, 4) - mul_ia<V2>(tb, DD(e0, 2));
-  const T tk2 = ta * ta + tb * tb;
   V2 explv = mul_ia<V2>(ta, mul_ia<V2>(ta, DD(e1, 0)) + DD(e2, 3) + mul_ia<V2>(tb, DD1_6)) +
              mul_ia<V2>(tb, mul_ia<V2>(ta, DD1_6) + DD(e2, 4) + mul_ia<V2>(tb, DD(e1, 2)));
   explv = explv - mk<V2>(tk2 * rhsv.x, tk2 * rhsv.y);
-  const L a = L((float)ix) * derL[tailL], b = L((float)iz) * derL[tailL + 1];
-  const L k2 = a * a + b * b;
   // body-force terms (dnsdata.f90:644, 651, 658): fv for the v equation,
   // fe for eta (or the mean mode's D0 of Re F1, Re F3)
   LV fv = czero<LV>(), fe = czero<LV>();
@@ -174,14 +212,6 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
     fv = czero<LV>() - lmul(k2, D0f2) - mul_ia<LV>(a, D1f1) - mul_ia<LV>(b, D1f3);
     fe = (ix == 0 && iz == 0) ? mk<LV>(r1, r3) : mul_ia<LV>(b, D0f1) - mul_ia<LV>(a, D0f3);
   }
-  LV v1[5], v2[5], v3[5];
-#pragma unroll
-  for (int j = 0; j < 5; ++j) {
-    v1[j] = cvt2<LV>(V[vidx(d, 0, iy - 2 + j, m)]);
-    v2[j] = cvt2<LV>(V[vidx(d, 1, iy - 2 + j, m)]);
-    v3[j] = cvt2<LV>(V[vidx(d, 2, iy - 2 + j, m)]);
-  }
-  const L lode2 = Num<L>::from_double(ode2), lode3 = Num<L>::from_double(ode3);
   const size_t r0 = ((size_t)0 * (d.ny - 1) + (iy - 1)) * d.nmodes + m;  // eta
   const size_t r1 = ((size_t)1 * (d.ny - 1) + (iy - 1)) * d.nmodes + m;  // d2v
   // FP64 linear terms keep the reference's evaluation order: the flow-rate
@@ -190,13 +220,12 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
   // to spare and take the combined coefficients.
   constexpr bool kCombined = std::is_same<L, dd>::value;
   const L* drL = derL + (size_t)iy * 20;
-  const L lam = Num<L>::from_double(ode1 * sc->rdt), nu = derL[(size_t)(d.ny + 1) * 20 + 2];
   {
     LV r;
     if constexpr (kCombined) {
-      r = lmul(cf[0] + k2 * (cf[5] + k2 * cf[10]), v2[0]);
+      r = lmul(cfr[0] + k2 * (cfr[5] + k2 * cfr[10]), v2[0]);
 #pragma unroll
-      for (int j = 1; j < 5; ++j) r = r + lmul(cf[j] + k2 * (cf[5 + j] + k2 * cf[10 + j]), v2[j]);
+      for (int j = 1; j < 5; ++j) r = r + lmul(cfr[j] + k2 * (cfr[5 + j] + k2 * cfr[10 + j]), v2[j]);
     } else {
       LV s0 = lmul(drL[0], v2[0]), s2 = lmul(drL[10], v2[0]), s4 = lmul(drL[15], v2[0]);
 #pragma unroll
@@ -223,11 +252,11 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
     if (F) e = e + fe;
     LV r;
     if constexpr (kCombined) {
-      L su = cf[15] * v1[0].x, sw = cf[15] * v3[0].x;
+      L su = cfr[15] * v1[0].x, sw = cfr[15] * v3[0].x;
 #pragma unroll
       for (int j = 1; j < 5; ++j) {
-        su = su + cf[15 + j] * v1[j].x;
-        sw = sw + cf[15 + j] * v3[j].x;
+        su = su + cfr[15 + j] * v1[j].x;
+        sw = sw + cfr[15 + j] * v3[j].x;
       }
       r = mk<LV>(su, sw);
     } else {
@@ -250,11 +279,11 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
     const V2 ee = mul_ia<V2>(tb, rhsu) - mul_ia<V2>(ta, rhsw);
     LV r;
     if constexpr (kCombined) {
-      L nj = cf[15] + k2 * cf[20];
+      L nj = cfr[15] + k2 * cfr[20];
       LV s1 = lmul(nj, v1[0]), s3 = lmul(nj, v3[0]);
 #pragma unroll
       for (int j = 1; j < 5; ++j) {
-        nj = cf[15 + j] + k2 * cf[20 + j];
+        nj = cfr[15 + j] + k2 * cfr[20 + j];
         s1 = s1 + lmul(nj, v1[j]);
         s3 = s3 + lmul(nj, v3[j]);
       }
@@ -278,15 +307,22 @@ __global__ void __launch_bounds__(128) k_rhs(const double2* __restrict__ V, cons
     old[r0] = mk<O2>(store_as<OT>(e.x), store_as<OT>(e.y));
     rhs[r0] = make_double2(Num<L>::to_double(r.x), Num<L>::to_double(r.y));
   }
+  }  // rows
 }
+
+// rows per thread: several where the kernel waits on loads (the FP32 path),
+// one where the FP64 pipe binds it and registers are dear
+template <typename T> struct RhsRows { static constexpr int value = 1; };
+template <> struct RhsRows<float> { static constexpr int value = 16; };
 
 template <typename T>
 void launch_rhs(const SolveLaunch& L, cudaStream_t s) {
   using V2 = typename C2<T>::t;
   using O2 = typename HistT<T>::t;
-  dim3 grid((L.d.nmodes + 127) / 128, L.d.ny - 1);
+  constexpr int RB = RhsRows<T>::value;
+  dim3 grid((L.d.nmodes + 127) / 128, (L.d.ny - 1 + RB - 1) / RB);
   using LT = typename LinT<T>::t;
-  k_rhs<T><<<grid, 128, 0, s>>>(L.V, (const V2*)L.VV, (O2*)L.old, L.rhs, (const LT*)L.derL, (const T*)L.derT, L.d,
+  k_rhs<T, RB><<<grid, 128, 0, s>>>(L.V, (const V2*)L.VV, (O2*)L.old, L.rhs, (const LT*)L.derL, (const T*)L.derT, L.d,
                                 L.ode[0], L.ode[1], L.ode[2], L.sc, L.F);
 }
 template void launch_rhs<double>(const SolveLaunch&, cudaStream_t);
