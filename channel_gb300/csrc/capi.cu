@@ -63,6 +63,7 @@ struct chgpu_handle {
   void* derL = nullptr;
   void* cst = nullptr;  // transform-type constants: factor, 1/dx, 1/dz, 1/dy per plane
   double* d0lu = nullptr;
+  double* nud = nullptr;  // per row: -ni d4, -ni d2 (the mode-independent matrix terms)
   void* lindd = nullptr;  // double-float d1 / D0mat / d0 rows for v' and u, w (mixed path)
   double* yint = nullptr;
   double* dy = nullptr;
@@ -287,6 +288,7 @@ SolveLaunch solve_launch(chgpu_handle* h, const double* ode) {
   L.derL = h->derL;
   L.d0lu = h->d0lu;
   L.lindd = h->lindd;
+  L.nud = h->nud;
   L.yint = h->yint;
   L.sc = h->sc;
   if (ode) {
@@ -385,7 +387,7 @@ void release(chgpu_handle* h) {
     cudaEventDestroy(pe.second.second);
   }
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
-  void* bufs[] = {h->V, h->F, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->derT, h->derL, h->cst, h->d0lu, h->lindd, h->yint, h->dy,
+  void* bufs[] = {h->V, h->F, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->derT, h->derL, h->cst, h->d0lu, h->nud, h->lindd, h->yint, h->dy,
                   h->twz, h->twx, h->twh, h->sc, h->ex_W, h->ex_P, h->ex_out, h->ex_twz, h->ex_twx};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -530,6 +532,17 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
         }
       if ((rc = dev_alloc(&h->lindd, sizeof(dd) * ld.size(), "double-float derivative rows"))) break;
       cudaMemcpy(h->lindd, ld.data(), sizeof(dd) * ld.size(), cudaMemcpyHostToDevice);
+    }
+    {
+      std::vector<double> nu((size_t)(p->ny + 1) * 10, 0.0);
+      const double mni = -p->ni;
+      for (int iy = 0; iy <= p->ny; ++iy)
+        for (int j = 0; j < 5; ++j) {
+          nu[(size_t)iy * 10 + j] = mni * t.der[(size_t)iy * 20 + 15 + j];
+          nu[(size_t)iy * 10 + 5 + j] = mni * t.der[(size_t)iy * 20 + 10 + j];
+        }
+      if ((rc = dev_alloc((void**)&h->nud, sizeof(double) * nu.size(), "viscous rows"))) break;
+      cudaMemcpy(h->nud, nu.data(), sizeof(double) * nu.size(), cudaMemcpyHostToDevice);
     }
     cudaMemcpy(h->der, t.der.data(), sizeof(double) * t.der.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(h->d0lu, t.d0lu.data(), sizeof(double) * t.d0lu.size(), cudaMemcpyHostToDevice);

@@ -78,6 +78,7 @@ struct SolveLaunch {
   int lambda_from_dt;
   const void* lindd;  // double-float d1 row, D0mat factors, d0 row per y row: v' and u, w in
                       // double-float; null: FP64
+  const double* nud;  // per y row: -ni d4 (5), -ni d2 (5); null: formed in the kernel
 };
 
 template <typename T> void launch_rhs(const SolveLaunch& L, cudaStream_t s);

@@ -559,7 +559,7 @@ __global__ void __launch_bounds__(64) k_linsolve(double2* __restrict__ V, const 
                                                  const double* __restrict__ d0lu, const double* __restrict__ yint,
                                                  BcRows bc, Dims d, double lambda_in, double ode1,
                                                  int lambda_from_dt, DevScalars* __restrict__ sc,
-                                                 const dd* __restrict__ lindd) {
+                                                 const dd* __restrict__ lindd, const double* __restrict__ nud) {
   const int lane = threadIdx.x & 31, role = threadIdx.x >> 5;
   const int q = blockIdx.x * 32 + lane;
   const bool active = q < d.npairs;
@@ -611,14 +611,22 @@ __global__ void __launch_bounds__(64) k_linsolve(double2* __restrict__ V, const 
         for (int t = 0; t < 2; ++t)
           if (t < nm) bnext[t] = rsrc[(size_t)(iy - 1 + roff) * d.nmodes + mm[t]];
       }
+      // warp-uniform: each warp assembles only its own matrix; the products
+      // -ni d4 and -ni d2, the same for every mode, come from the per-row
+      // table nud when there is one
       double A[5];
-      if (role) {  // warp-uniform: each warp assembles only its own matrix
+      if (role) {
 #pragma unroll
-        for (int j = 0; j < 5; ++j) A[j] = ac.ce0 * __ldg(dr + j) + ac.ce2 * __ldg(dr + 10 + j);
+        for (int j = 0; j < 5; ++j) {
+          const double p2 = nud ? __ldg(nud + (size_t)iy * 10 + 5 + j) : ac.ce2 * __ldg(dr + 10 + j);
+          A[j] = fma(ac.ce0, __ldg(dr + j), p2);
+        }
       } else {
 #pragma unroll
-        for (int j = 0; j < 5; ++j)
-          A[j] = ac.cv4 * __ldg(dr + 15 + j) + ac.cv2 * __ldg(dr + 10 + j) + ac.cv0 * __ldg(dr + j);
+        for (int j = 0; j < 5; ++j) {
+          const double p4 = nud ? __ldg(nud + (size_t)iy * 10 + j) : ac.cv4 * __ldg(dr + 15 + j);
+          A[j] = fma(ac.cv0, __ldg(dr + j), fma(ac.cv2, __ldg(dr + 10 + j), p4));
+        }
       }
       if (iy == ny - 1) bc_top1(A, top, topp1);
       if (iy == ny - 2) bc_top2(A, top);
@@ -777,7 +785,7 @@ __global__ void __launch_bounds__(64) k_linsolve(double2* __restrict__ V, const 
 void launch_linsolve(const SolveLaunch& L, cudaStream_t s) {
   dim3 grid((L.d.npairs + 31) / 32);
   k_linsolve<<<grid, 64, 0, s>>>(L.V, L.rhs_src, L.rhs_cstride, L.rhs_plane_off, L.fac, L.der, L.d0lu, L.yint, L.bc, L.d, L.lambda, L.ode[0],
-                                  L.lambda_from_dt, L.sc, (const dd*)L.lindd);
+                                  L.lambda_from_dt, L.sc, (const dd*)L.lindd, L.nud);
 }
 
 // ---------------------------------------------------------------------------
