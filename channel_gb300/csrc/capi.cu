@@ -48,6 +48,11 @@ struct chgpu_handle {
   int zthreads = 256, xthreads = 256;  // threads per block of the transform kernels
   bool tuned = false;
   cudaStream_t stream = nullptr;
+  // the step in two kx halves (rhs / solve / next z-inverse of one half
+  // overlapping the other's): side stream and its fork / join events
+  int halves = 2;
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t ev_vv = nullptr, ev_solved = nullptr;
   // device buffers
   double2* V = nullptr;
   void* old = nullptr;
@@ -100,6 +105,7 @@ struct chgpu_handle {
   double kind_ms[CHGPU_NKINDS] = {0};
   long long kind_n[CHGPU_NKINDS] = {0};
   long long launches = 0;
+  long long step_launches = 19;  // kernels in one captured step
   std::string err;
 };
 
@@ -266,6 +272,8 @@ ConvLaunch conv_launch(chgpu_handle* h, int compute_cfl, int products, int plane
   L.xminb = h->xminb;
   L.zthreads = h->zthreads;
   L.xthreads = h->xthreads;
+  L.ix_lo = 0;
+  L.ix_hi = h->d.nx + 1;
   L.plane0 = plane0;
   L.nplanes = nplanes;
   L.compute_cfl = compute_cfl;
@@ -289,6 +297,10 @@ SolveLaunch solve_launch(chgpu_handle* h, const double* ode) {
   L.d0lu = h->d0lu;
   L.lindd = h->lindd;
   L.nud = h->nud;
+  L.m_lo = 0;
+  L.m_hi = h->d.nmodes;
+  L.q_lo = 0;
+  L.q_hi = h->d.npairs;
   L.yint = h->yint;
   L.sc = h->sc;
   if (ode) {
@@ -299,35 +311,51 @@ SolveLaunch solve_launch(chgpu_handle* h, const double* ode) {
   return L;
 }
 
-void run_convolutions(chgpu_handle* h, int compute_cfl, int products, int plane0, int nplanes) {
+void run_convolutions(chgpu_handle* h, int compute_cfl, int products, int plane0, int nplanes, int stage_lo = 0,
+                      int stage_hi = 3, int ix_lo = 0, int ix_hi = -1) {
   ConvLaunch L = conv_launch(h, compute_cfl, products, plane0, nplanes);
+  if (ix_hi >= 0) {
+    L.ix_lo = ix_lo;
+    L.ix_hi = ix_hi;
+  }
   const int nst = products ? 3 : 2;
-  for (int stage = 0; stage < nst; ++stage)
+  for (int stage = stage_lo; stage < std::min(nst, stage_hi); ++stage) {
     timed(h, stage, [&] {
       if (h->prec == CHGPU_MIXED) launch_convolutions<float>(L, h->stream, stage);
       else if (h->prec == CHGPU_FP64DD) launch_convolutions<dd>(L, h->stream, stage);
       else launch_convolutions<double>(L, h->stream, stage);
     });
-  h->launches += nst;
+    h->launches += 1;
+  }
 }
 
-void run_rhs(chgpu_handle* h, const double* ode) {
+void run_rhs(chgpu_handle* h, const double* ode, cudaStream_t s = nullptr, int m_lo = 0, int m_hi = -1) {
   SolveLaunch L = solve_launch(h, ode);
+  if (m_hi >= 0) {
+    L.m_lo = m_lo;
+    L.m_hi = m_hi;
+  }
+  if (!s) s = h->stream;
   timed(h, 3, [&] {
-    if (h->prec == CHGPU_MIXED) launch_rhs<float>(L, h->stream);
-    else if (h->prec == CHGPU_FP64DD) launch_rhs<dd>(L, h->stream);
-    else launch_rhs<double>(L, h->stream);
+    if (h->prec == CHGPU_MIXED) launch_rhs<float>(L, s);
+    else if (h->prec == CHGPU_FP64DD) launch_rhs<dd>(L, s);
+    else launch_rhs<double>(L, s);
   });
   h->launches += 1;
 }
 
 // rhs_in_field: read the right-hand sides from V (the reference's in-place
 // convention) instead of the separate buffer k_rhs writes.
-void run_linsolve(chgpu_handle* h, double ode1, double lambda, int from_dt, bool rhs_in_field) {
+void run_linsolve(chgpu_handle* h, double ode1, double lambda, int from_dt, bool rhs_in_field,
+                  cudaStream_t s = nullptr, int q_lo = 0, int q_hi = -1) {
   SolveLaunch L = solve_launch(h, nullptr);
   L.ode[0] = ode1;
   L.lambda = lambda;
   L.lambda_from_dt = from_dt;
+  if (q_hi >= 0) {
+    L.q_lo = q_lo;
+    L.q_hi = q_hi;
+  }
   if (rhs_in_field) {
     L.rhs_src = h->V;
     L.rhs_cstride = (size_t)h->d.nplanes * h->d.nmodes;
@@ -337,7 +365,8 @@ void run_linsolve(chgpu_handle* h, double ode1, double lambda, int from_dt, bool
     L.rhs_cstride = (size_t)(h->d.ny - 1) * h->d.nmodes;
     L.rhs_plane_off = -1;
   }
-  timed(h, 4, [&] { launch_linsolve(L, h->stream); });
+  if (!s) s = h->stream;
+  timed(h, 4, [&] { launch_linsolve(L, s); });
   h->launches += 1;
 }
 
@@ -348,14 +377,47 @@ void run_outstats(chgpu_handle* h) {
 }
 
 // One time-loop iteration (channel.f90:118-167) on the stream.
+//
+// With halves = 2 (and no per-kernel timing) the kx columns split in two
+// halves A (kx < KA, holding the mean mode) and B: k_rhs, k_linsolve and the
+// next substep's z-inverse touch only the modes of their half, so half B's
+// rhs and solve run on the side stream, started after half A's rhs, while
+// half A's solve and next z-inverse run on the main one -- the
+// latency-bound solve of one half overlaps the other half's work.  The x pass, which needs every kx, joins
+// both; so does the end of the step.  Nothing half B's kernels read is
+// written by half A's (the mean-mode scalars are read only for the mean mode).
 void enqueue_step(chgpu_handle* h) {
+  const bool split = h->halves == 2 && !h->profiling && h->d.nx >= 1;
+  const int KA = (h->d.nx + 1 + 1) / 2, nxp = h->d.nx + 1;
+  const int mA = KA * h->d.nzt, qA = KA * (h->d.nz + 1);
   for (int k = 0; k < 3; ++k) {
     timed(h, 5, [&] { launch_advance_time(h->sc, 2.0 / RK[k][0], k == 0, h->stream); });
     h->launches += 1;
-    run_convolutions(h, k == 2, 1, 0, h->d.nplanes);
-    run_rhs(h, RK[k]);
-    run_linsolve(h, RK[k][0], 0.0, 1, false);
+    if (!split) {
+      run_convolutions(h, k == 2, 1, 0, h->d.nplanes);
+      run_rhs(h, RK[k]);
+      run_linsolve(h, RK[k][0], 0.0, 1, false);
+      continue;
+    }
+    if (k == 0) {
+      run_convolutions(h, 0, 1, 0, h->d.nplanes, 0, 1);  // z-inverse, all kx
+    } else {
+      run_convolutions(h, 0, 1, 0, h->d.nplanes, 0, 1, 0, KA);  // half A (its solve is done)
+      cudaStreamWaitEvent(h->stream, h->ev_solved, 0);
+      run_convolutions(h, 0, 1, 0, h->d.nplanes, 0, 1, KA, nxp);  // half B
+    }
+    run_convolutions(h, k == 2, 1, 0, h->d.nplanes, 1, 3);  // x pass and z-forward, all kx
+    // staggered: half B's rhs starts when half A's is done, so it overlaps
+    // half A's solve, and half A's next z-inverse overlaps half B's solve
+    run_rhs(h, RK[k], h->stream, 0, mA);
+    cudaEventRecord(h->ev_vv, h->stream);
+    cudaStreamWaitEvent(h->stream2, h->ev_vv, 0);
+    run_rhs(h, RK[k], h->stream2, mA, h->d.nmodes);
+    run_linsolve(h, RK[k][0], 0.0, 1, false, h->stream2, qA, h->d.npairs);
+    cudaEventRecord(h->ev_solved, h->stream2);
+    run_linsolve(h, RK[k][0], 0.0, 1, false, h->stream, 0, qA);
   }
+  if (split) cudaStreamWaitEvent(h->stream, h->ev_solved, 0);
   run_outstats(h);
 }
 
@@ -398,6 +460,9 @@ void release(chgpu_handle* h) {
   if (h->snap_read) cudaEventDestroy(h->snap_read);
   if (h->snap_done) cudaEventDestroy(h->snap_done);
   if (h->snap_stream) cudaStreamDestroy(h->snap_stream);
+  if (h->ev_vv) cudaEventDestroy(h->ev_vv);
+  if (h->ev_solved) cudaEventDestroy(h->ev_solved);
+  if (h->stream2) cudaStreamDestroy(h->stream2);
   if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -481,6 +546,9 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
   const size_t nplanes = d.nplanes, nmodes = d.nmodes, nxp = p->nx + 1;
   do {
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_vv, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_solved, cudaEventDisableTiming);
     if (e != cudaSuccess) { rc = cuda_fail(h, e, "cudaStreamCreate"); break; }
     e = conv_set_smem_limits();
     if (e != cudaSuccess) { rc = cuda_fail(h, e, "cudaFuncSetAttribute"); break; }
@@ -692,6 +760,7 @@ int chgpu_step(chgpu_handle* h, chgpu_stats* st) {
     CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     const long long before = h->launches;
     enqueue_step(h);
+    h->step_launches = h->launches - before;
     h->launches = before;
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
@@ -703,7 +772,7 @@ int chgpu_step(chgpu_handle* h, chgpu_stats* st) {
     }
   }
   CK(h, cudaGraphLaunch(h->graph, h->stream));
-  h->launches += 19;  // 3 x (time advance, 3 transform kernels, rhs, linsolve) + outstats
+  h->launches += h->step_launches;
   if (st) {
     int rc = pull_scalars(h);
     fill_stats(h, st);
@@ -868,6 +937,7 @@ int chgpu_ensemble_step(chgpu_ensemble* e, chgpu_stats* st) {
       enqueue_step(h);
       cudaEventRecord(e->join[i], h->stream);
       cudaStreamWaitEvent(e->stream, e->join[i], 0);
+      h->step_launches = h->launches - before;
       h->launches = before;
       h->profiling = prof;
     }
@@ -883,7 +953,7 @@ int chgpu_ensemble_step(chgpu_ensemble* e, chgpu_stats* st) {
     for (int i = 0; i < n; ++i) e->versions[i] = e->m[i]->version;
   }
   CKE(e, cudaGraphLaunch(e->graph, e->stream));
-  for (chgpu_handle* h : e->m) h->launches += 19;
+  for (chgpu_handle* h : e->m) h->launches += h->step_launches;
   if (!st) return 0;
   for (chgpu_handle* h : e->m)
     CKE(e, cudaMemcpyAsync(h->sc_host, h->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, e->stream));

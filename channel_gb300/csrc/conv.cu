@@ -28,7 +28,7 @@ namespace chgpu {
 template <typename T>
 __global__ void __launch_bounds__(256) k_zinv(const double2* __restrict__ V, typename C2<T>::t* __restrict__ Zb,
                                               const typename C2<T>::t* __restrict__ twz, Dims d, RadixDev rz,
-                                              int nb_cols, int plane0) {
+                                              int nb_cols, int plane0, int ix_lo, int ix_hi) {
   using V2 = typename C2<T>::t;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nzd = d.nzd, nz = d.nz, nxp = d.nx + 1;
@@ -36,8 +36,8 @@ __global__ void __launch_bounds__(256) k_zinv(const double2* __restrict__ V, typ
   V2* bufB = bufA + pad32_size(nb_cols * nzd);
   const int c = blockIdx.z;
   const int plane = plane0 + blockIdx.y;
-  const int ix0 = blockIdx.x * nb_cols;
-  const int nb = min(nb_cols, nxp - ix0);
+  const int ix0 = ix_lo + blockIdx.x * nb_cols;
+  const int nb = min(nb_cols, ix_hi - ix0);
   const size_t colbase = ((size_t)c * d.nplanes + plane) * nxp;
   const FastDiv by_nzd(nzd);
   for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) {
@@ -218,9 +218,11 @@ void launch_convolutions(const ConvLaunch& L, cudaStream_t s, int stage) {
   const Dims& d = L.d;
   const int nxp = d.nx + 1;
   if (stage == 0) {
-    dim3 grid((nxp + L.zcols - 1) / L.zcols, L.nplanes, 3);
+    const int ncol = L.ix_hi - L.ix_lo;
+    dim3 grid((ncol + L.zcols - 1) / L.zcols, L.nplanes, 3);
     size_t sm = conv_z_smem(L.zcols, d.nzd, sizeof(V2));
-    k_zinv<T><<<grid, L.zthreads, sm, s>>>(L.V, (V2*)L.Zb, (const V2*)L.twz, d, L.rz, L.zcols, L.plane0);
+    k_zinv<T><<<grid, L.zthreads, sm, s>>>(L.V, (V2*)L.Zb, (const V2*)L.twz, d, L.rz, L.zcols, L.plane0, L.ix_lo,
+                                           L.ix_hi);
   }
   if (stage == 1) {
     dim3 grid(d.nzd / L.xrows, L.nplanes);

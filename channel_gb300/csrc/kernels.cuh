@@ -43,6 +43,7 @@ struct ConvLaunch {
   int zcols, xrows;
   int xminb;  // register-cap variant of the x-row kernel (1, 2 or 3 blocks per SM)
   int zthreads, xthreads;  // threads per block of the z-transform and x-row kernels (<= 256)
+  int ix_lo, ix_hi;        // kx columns of the z-inverse pass (all: 0, nx+1)
   int plane0, nplanes;
   int compute_cfl;
   int products;  // 0: stop after the x pass (the start-up CFL pass)
@@ -79,6 +80,8 @@ struct SolveLaunch {
   const void* lindd;  // double-float d1 row, D0mat factors, d0 row per y row: v' and u, w in
                       // double-float; null: FP64
   const double* nud;  // per y row: -ni d4 (5), -ni d2 (5); null: formed in the kernel
+  int m_lo, m_hi;     // modes of k_rhs (all: 0, nmodes); a range of whole kx columns
+  int q_lo, q_hi;     // (kx, +-kz) pairs of k_linsolve (all: 0, npairs)
 };
 
 template <typename T> void launch_rhs(const SolveLaunch& L, cudaStream_t s);

@@ -148,6 +148,10 @@ extern "C" int chgpu_linsolve_noalloc(const chgpu_params* p, double lambda, doub
   d.meanflowx = p->meanflowx; d.meanflowz = p->meanflowz;
   d.cflmax = p->cflmax; d.gamma = p->gamma;
   d.cpi = p->cpi; d.cpi_type = p->cpi_type;
+  L.q_lo = 0;
+  L.q_hi = (int)npairs;
+  L.m_lo = 0;
+  L.m_hi = d.nmodes;
   std::memcpy(L.bc.v0bc, t.v0bc, 40); std::memcpy(L.bc.v0m1bc, t.v0m1bc, 40);
   std::memcpy(L.bc.eta0bc, t.eta0bc, 40); std::memcpy(L.bc.eta0m1bc, t.eta0m1bc, 40);
   std::memcpy(L.bc.vnbc, t.vnbc, 40); std::memcpy(L.bc.vnp1bc, t.vnp1bc, 40);

@@ -90,11 +90,12 @@ __global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2*
                                              typename HistT<T>::t* __restrict__ old, double2* __restrict__ rhs,
                                              const typename LinT<T>::t* __restrict__ derL, const T* __restrict__ derT,
                                              Dims d, double ode1, double ode2, double ode3,
-                                             const DevScalars* __restrict__ sc, const double2* __restrict__ F) {
+                                             const DevScalars* __restrict__ sc, const double2* __restrict__ F,
+                                             int m_lo, int m_hi) {
   using V2 = typename C2<T>::t;
   using O2 = typename HistT<T>::t;
   using OT = decltype(O2::x);
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = m_lo + blockIdx.x * blockDim.x + threadIdx.x;
   const int iy0 = blockIdx.y * RB + 1;
   const int nrows = min(RB, d.ny - iy0);
   // ---- linear terms of the field in L (FP64, or double-float in the mixed
@@ -125,7 +126,7 @@ __global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2*
     c[20 + j] = L() - nu * c0;
   }
   __syncthreads();
-  if (m >= d.nmodes) return;
+  if (m >= m_hi) return;
   const int ix = m / d.nzt;
   const int iz = m - ix * d.nzt - d.nz;
   // wavenumbers (derT holds der in T, then alfa0, beta0; derL likewise in L, then ni)
@@ -320,10 +321,11 @@ void launch_rhs(const SolveLaunch& L, cudaStream_t s) {
   using V2 = typename C2<T>::t;
   using O2 = typename HistT<T>::t;
   constexpr int RB = RhsRows<T>::value;
-  dim3 grid((L.d.nmodes + 127) / 128, (L.d.ny - 1 + RB - 1) / RB);
+  if (L.m_hi <= L.m_lo) return;
+  dim3 grid((L.m_hi - L.m_lo + 127) / 128, (L.d.ny - 1 + RB - 1) / RB);
   using LT = typename LinT<T>::t;
   k_rhs<T, RB><<<grid, 128, 0, s>>>(L.V, (const V2*)L.VV, (O2*)L.old, L.rhs, (const LT*)L.derL, (const T*)L.derT, L.d,
-                                L.ode[0], L.ode[1], L.ode[2], L.sc, L.F);
+                                L.ode[0], L.ode[1], L.ode[2], L.sc, L.F, L.m_lo, L.m_hi);
 }
 template void launch_rhs<double>(const SolveLaunch&, cudaStream_t);
 template void launch_rhs<float>(const SolveLaunch&, cudaStream_t);
@@ -559,10 +561,11 @@ __global__ void __launch_bounds__(64) k_linsolve(double2* __restrict__ V, const 
                                                  const double* __restrict__ d0lu, const double* __restrict__ yint,
                                                  BcRows bc, Dims d, double lambda_in, double ode1,
                                                  int lambda_from_dt, DevScalars* __restrict__ sc,
-                                                 const dd* __restrict__ lindd, const double* __restrict__ nud) {
+                                                 const dd* __restrict__ lindd, const double* __restrict__ nud,
+                                                 int q_lo, int q_hi) {
   const int lane = threadIdx.x & 31, role = threadIdx.x >> 5;
-  const int q = blockIdx.x * 32 + lane;
-  const bool active = q < d.npairs;
+  const int q = q_lo + blockIdx.x * 32 + lane;
+  const bool active = q < q_hi;
   const int ny = d.ny, nz = d.nz;
   const int ix = active ? q / (nz + 1) : 0;
   const int a = active ? q - ix * (nz + 1) : 0;
@@ -783,9 +786,10 @@ __global__ void __launch_bounds__(64) k_linsolve(double2* __restrict__ V, const 
 }
 
 void launch_linsolve(const SolveLaunch& L, cudaStream_t s) {
-  dim3 grid((L.d.npairs + 31) / 32);
+  if (L.q_hi <= L.q_lo) return;
+  dim3 grid((L.q_hi - L.q_lo + 31) / 32);
   k_linsolve<<<grid, 64, 0, s>>>(L.V, L.rhs_src, L.rhs_cstride, L.rhs_plane_off, L.fac, L.der, L.d0lu, L.yint, L.bc, L.d, L.lambda, L.ode[0],
-                                  L.lambda_from_dt, L.sc, (const dd*)L.lindd, L.nud);
+                                  L.lambda_from_dt, L.sc, (const dd*)L.lindd, L.nud, L.q_lo, L.q_hi);
 }
 
 // ---------------------------------------------------------------------------

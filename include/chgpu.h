@@ -125,7 +125,7 @@ int chgpu_synchronize(chgpu_handle* h);
  * uploads, chgpu_start, downloads, statistics, tiles or a body force; one
  * chgpu_ensemble_step advances all members by one RK3 step with a single
  * CUDA-graph launch whose branches (one per member, each the member's own
- * 19-launch step) run concurrently.  The graph is re-captured when a
+ * step) run concurrently.  The graph is re-captured when a
  * member's launch sequence changes (tiles, body force on/off).  st: NULL, or
  * one record per member (synchronises).  No counterpart in the reference,
  * which runs one channel per MPI job. */
