@@ -160,9 +160,9 @@ int upload_derT(chgpu_handle* h) {
   t[der.size() + 1] = from_ld<T>((long double)h->p.beta0);
   CK(h, cudaMalloc(&h->derT, sizeof(T) * t.size()));
   CK(h, cudaMemcpy(h->derT, t.data(), sizeof(T) * t.size(), cudaMemcpyHostToDevice));
-  // constants of the x-row pass: factor, 1/dx, 1/dz (dnsdata.f90:124), 1/dy(iy) per plane (:155)
+  // constants of the x-row pass: factor/2, 1/dx, 1/dz (dnsdata.f90:124), 1/dy(iy) per plane (:155)
   std::vector<T> c(3 + h->d.nplanes, T());
-  c[0] = from_ld<T>((long double)h->d.factor);
+  c[0] = from_ld<T>(0.5L * (long double)h->d.factor);
   c[1] = from_ld<T>((long double)h->d.rdx);
   c[2] = from_ld<T>((long double)h->d.rdz);
   for (int iy = 1; iy <= h->p.ny - 1; ++iy) c[3 + iy + 1] = from_ld<T>(1.0L / (long double)h->tab.dy[iy]);
@@ -219,11 +219,21 @@ int upload_stage_twiddles(chgpu_handle* h, void** dst, const RadixDev& rad) {
   return 0;
 }
 
+// roots of 2 nxd for the real-to-complex packing, then the same scaled by
+// factor/2 for the unpacking of the products (factor = dnsdata.f90:124)
 template <typename V2>
-int upload_roots(chgpu_handle* h, void** dst, int n) {
-  std::vector<V2> w = roots<V2>(n);
-  CK(h, cudaMalloc(dst, sizeof(V2) * n));
-  CK(h, cudaMemcpy(*dst, w.data(), sizeof(V2) * n, cudaMemcpyHostToDevice));
+int upload_pack_roots(chgpu_handle* h, void** dst, int n, long double scale) {
+  using T = decltype(V2::x);
+  std::vector<V2> w(2 * (size_t)n);
+  for (int m = 0; m < n; ++m) {
+    const long double ang = 2.0L * 3.14159265358979323846264338327950288L * (long double)m / (long double)n;
+    w[m].x = from_ld<T>(cosl(ang));
+    w[m].y = from_ld<T>(-sinl(ang));
+    w[n + m].x = from_ld<T>(scale * cosl(ang));
+    w[n + m].y = from_ld<T>(-scale * sinl(ang));
+  }
+  CK(h, cudaMalloc(dst, sizeof(V2) * w.size()));
+  CK(h, cudaMemcpy(*dst, w.data(), sizeof(V2) * w.size(), cudaMemcpyHostToDevice));
   return 0;
 }
 
@@ -570,19 +580,19 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
     if (h->prec == CHGPU_MIXED) {
       if ((rc = upload_stage_twiddles<float2>(h, &h->twz, h->rz))) break;
       if ((rc = upload_stage_twiddles<float2>(h, &h->twx, h->rx))) break;
-      if ((rc = upload_roots<float2>(h, &h->twh, 2 * nxd))) break;
+      if ((rc = upload_pack_roots<float2>(h, &h->twh, 2 * nxd, 0.5L * (long double)d.factor))) break;
       if ((rc = upload_derT<float>(h))) break;
       if ((rc = upload_derL<dd>(h))) break;
     } else if (h->prec == CHGPU_FP64DD) {
       if ((rc = upload_stage_twiddles<cdd>(h, &h->twz, h->rz))) break;
       if ((rc = upload_stage_twiddles<cdd>(h, &h->twx, h->rx))) break;
-      if ((rc = upload_roots<cdd>(h, &h->twh, 2 * nxd))) break;
+      if ((rc = upload_pack_roots<cdd>(h, &h->twh, 2 * nxd, 0.5L * (long double)d.factor))) break;
       if ((rc = upload_derT<dd>(h))) break;
       if ((rc = upload_derL<double>(h))) break;
     } else {
       if ((rc = upload_stage_twiddles<double2>(h, &h->twz, h->rz))) break;
       if ((rc = upload_stage_twiddles<double2>(h, &h->twx, h->rx))) break;
-      if ((rc = upload_roots<double2>(h, &h->twh, 2 * nxd))) break;
+      if ((rc = upload_pack_roots<double2>(h, &h->twh, 2 * nxd, 0.5L * (long double)d.factor))) break;
       if ((rc = upload_derT<double>(h))) break;
       if ((rc = upload_derL<double>(h))) break;
     }

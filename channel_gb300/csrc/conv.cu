@@ -117,8 +117,9 @@ __global__ void __launch_bounds__(256, MINB) k_xrow(const typename C2<T>::t* __r
   __syncthreads();
   V2* U = fft_block<+1, V2, true>(A, B, 3 * nrows, rx, twx);
   V2* freeb = (U == A) ? B : A;
-  // CFL (dnsdata.f90:552-556) and products uu,vv,ww (:584)
-  const T f = cst[0];
+  // CFL (dnsdata.f90:552-556) and products uu,vv,ww (:584); their factor
+  // (:581-584) is applied in the r2c unpacking below (the transform is linear)
+  const T g = cst[0];  // factor / 2
   T cfl = T();
   bool bad = false;
   const bool do_cfl = compute_cfl && plane >= 2 && plane <= d.ny;
@@ -136,9 +137,9 @@ __global__ void __launch_bounds__(256, MINB) k_xrow(const typename C2<T>::t* __r
       cfl = N::max(cfl, N::max(c0, c1));
       bad = bad || !N::finite(c0) || !N::finite(c1);
     }
-    Cb[pad32((0 * nrows + r) * M + m)] = mk<V2>(u.x * u.x * f, u.y * u.y * f);
-    Cb[pad32((1 * nrows + r) * M + m)] = mk<V2>(v.x * v.x * f, v.y * v.y * f);
-    Cb[pad32((2 * nrows + r) * M + m)] = mk<V2>(w.x * w.x * f, w.y * w.y * f);
+    Cb[pad32((0 * nrows + r) * M + m)] = mk<V2>(u.x * u.x, u.y * u.y);
+    Cb[pad32((1 * nrows + r) * M + m)] = mk<V2>(v.x * v.x, v.y * v.y);
+    Cb[pad32((2 * nrows + r) * M + m)] = mk<V2>(w.x * w.x, w.y * w.y);
   }
   if (bad) cfl = T((float)INFINITY);  // a non-finite velocity shows up as an infinite CFL
   if (compute_cfl) block_max_atomic(Num<T>::to_double(cfl), &sc->cfl);
@@ -150,9 +151,9 @@ __global__ void __launch_bounds__(256, MINB) k_xrow(const typename C2<T>::t* __r
         V2 u = U[pad32((0 * nrows + r) * M + m)];
         V2 v = U[pad32((1 * nrows + r) * M + m)];
         V2 w = U[pad32((2 * nrows + r) * M + m)];
-        Cb[pad32((0 * nrows + r) * M + m)] = mk<V2>(u.x * v.x * f, u.y * v.y * f);
-        Cb[pad32((1 * nrows + r) * M + m)] = mk<V2>(v.x * w.x * f, v.y * w.y * f);
-        Cb[pad32((2 * nrows + r) * M + m)] = mk<V2>(u.x * w.x * f, u.y * w.y * f);
+        Cb[pad32((0 * nrows + r) * M + m)] = mk<V2>(u.x * v.x, u.y * v.y);
+        Cb[pad32((1 * nrows + r) * M + m)] = mk<V2>(v.x * w.x, v.y * w.y);
+        Cb[pad32((2 * nrows + r) * M + m)] = mk<V2>(u.x * w.x, u.y * w.y);
       }
       __syncthreads();
     }
@@ -166,10 +167,12 @@ __global__ void __launch_bounds__(256, MINB) k_xrow(const typename C2<T>::t* __r
       const int zb = (p * nrows + r) * M;
       V2 zk = P[pad32(zb + k)];
       V2 zm = conjg(P[pad32(zb + (k == 0 ? 0 : M - k))]);
-      V2 e = scale(zk + zm, T(0.5f));
+      // X = factor (Z_k + conj Z_{M-k})/2 + (factor/2) w_k (-i)(Z_k - conj Z_{M-k}),
+      // with the second table twh[2M + k] = (factor/2) w_k
+      V2 e = scale(zk + zm, g);
       V2 df = zk - zm;
-      V2 o = mk<V2>(df.y * T(0.5f), -df.x * T(0.5f));
-      V2 X = e + cmul(twh[k], o);
+      V2 o = mk<V2>(df.y, T() - df.x);
+      V2 X = e + cmul(twh[2 * M + k], o);
       Pb[(((size_t)(3 * half + p) * d.nplanes + plane) * nxp + k) * nzd + jz0 + r] = X;
     }
     __syncthreads();
