@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "chgpu_internal.h"
 #include "cplx.cuh"
@@ -169,10 +170,15 @@ __global__ void __launch_bounds__(256, MINB) k_xrow(const typename C2<T>::t* __r
       V2 zm = conjg(P[pad32(zb + (k == 0 ? 0 : M - k))]);
       // X = factor (Z_k + conj Z_{M-k})/2 + (factor/2) w_k (-i)(Z_k - conj Z_{M-k}),
       // with the second table twh[2M + k] = (factor/2) w_k
-      V2 e = scale(zk + zm, g);
-      V2 df = zk - zm;
-      V2 o = mk<V2>(df.y, T() - df.x);
-      V2 X = e + cmul(twh[2 * M + k], o);
+      const V2 sm = zk + zm, df = zk - zm;
+      const V2 w = twh[2 * M + k];
+      // o = (-i) df = (df.y, -df.x); X = g sm + w o, fused
+      V2 X;
+      if constexpr (std::is_same<T, dd>::value) {
+        X = scale(sm, g) + cmul(w, mk<V2>(df.y, T() - df.x));
+      } else {
+        X = mk<V2>(fma(g, sm.x, fma(w.x, df.y, w.y * df.x)), fma(g, sm.y, fma(w.y, df.y, -(w.x * df.x))));
+      }
       Pb[(((size_t)(3 * half + p) * d.nplanes + plane) * nxp + k) * nzd + jz0 + r] = X;
     }
     __syncthreads();
