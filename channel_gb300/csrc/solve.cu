@@ -100,6 +100,9 @@ __global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2*
   const int nrows = min(RB, d.ny - iy0);
   // ---- linear terms of the field in L (FP64, or double-float in the mixed
   //      path: the FP64 pipe is 1/58 of FP32 here) ----
+  // The reference evaluates unkn and impl as separate stencils and combines
+  // them; the combined coefficients agree to rounding (one five-point stencil
+  // per equation instead of three).
   // timescheme (dnsdata.f90:486) combines ODE(1)/deltat * unkn + impl, which
   // for D2v (:647) is, with S_k = Dk(V2) and lambda = ODE(1)/deltat,
   //   lambda (S2 - k2 S0) + ni (S4 - 2 k2 S2 + k2^2 S0) = sum_j (A_j + k2 B_j + k2^2 C_j) V2_j
@@ -112,7 +115,7 @@ __global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2*
   const size_t tailL = (size_t)(d.ny + 1) * 20;  // der rows, then alfa0, beta0, ni
   __shared__ __align__(16) unsigned char cf_raw[RB * 25 * sizeof(L)];
   L* cf = reinterpret_cast<L*>(cf_raw);
-  for (int t = threadIdx.x; std::is_same<L, dd>::value && t < 5 * nrows; t += blockDim.x) {
+  for (int t = threadIdx.x; t < 5 * nrows; t += blockDim.x) {
     const int j = t % 5, rr = t / 5;
     const L* dr = derL + (size_t)(iy0 + rr) * 20;
     const L c0 = dr[j], c2 = dr[10 + j], c4 = dr[15 + j];
@@ -136,7 +139,6 @@ __global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2*
   const L a = L((float)ix) * derL[tailL], b = L((float)iz) * derL[tailL + 1];
   const L k2 = a * a + b * b;
   const L lode2 = Num<L>::from_double(ode2), lode3 = Num<L>::from_double(ode3);
-  const L lam = Num<L>::from_double(ode1 * sc->rdt), nu = derL[tailL + 2];
   // windows over rows iy-2..iy+2: the six product spectra (plane = row + 1) and the field
   V2 vv[6][5];
   LV v1[5], v2[5], v3[5];
@@ -215,30 +217,10 @@ __global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2*
   }
   const size_t r0 = ((size_t)0 * (d.ny - 1) + (iy - 1)) * d.nmodes + m;  // eta
   const size_t r1 = ((size_t)1 * (d.ny - 1) + (iy - 1)) * d.nmodes + m;  // d2v
-  // FP64 linear terms keep the reference's evaluation order: the flow-rate
-  // correction divides by a difference ~1e-3 of its terms, and the order of
-  // the roundings shows there at 1e-10.  The double-float ones have ~48 bits
-  // to spare and take the combined coefficients.
-  constexpr bool kCombined = std::is_same<L, dd>::value;
-  const L* drL = derL + (size_t)iy * 20;
   {
-    LV r;
-    if constexpr (kCombined) {
-      r = lmul(cfr[0] + k2 * (cfr[5] + k2 * cfr[10]), v2[0]);
+    LV r = lmul(cfr[0] + k2 * (cfr[5] + k2 * cfr[10]), v2[0]);
 #pragma unroll
-      for (int j = 1; j < 5; ++j) r = r + lmul(cfr[j] + k2 * (cfr[5 + j] + k2 * cfr[10 + j]), v2[j]);
-    } else {
-      LV s0 = lmul(drL[0], v2[0]), s2 = lmul(drL[10], v2[0]), s4 = lmul(drL[15], v2[0]);
-#pragma unroll
-      for (int j = 1; j < 5; ++j) {
-        s0 = s0 + lmul(drL[j], v2[j]);
-        s2 = s2 + lmul(drL[10 + j], v2[j]);
-        s4 = s4 + lmul(drL[15 + j], v2[j]);
-      }
-      const LV unkn = s2 - lmul(k2, s0);
-      const LV impl = lmul(nu, s4 - lmul(k2 + k2, s2) + lmul(k2 * k2, s0));
-      r = lmul(lam, unkn) + impl;
-    }
+    for (int j = 1; j < 5; ++j) r = r + lmul(cfr[j] + k2 * (cfr[5 + j] + k2 * cfr[10 + j]), v2[j]);
     const O2 o = old[r1];
     LV e = mk<LV>(conv<L>(explv.x), conv<L>(explv.y));
     if (F) e = e + fv;
@@ -251,26 +233,13 @@ __global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2*
     LV e = mk<LV>(conv<L>(rhsu.x) + Num<L>::from_double(sc->meanpx),
                   conv<L>(rhsw.x) + Num<L>::from_double(sc->meanpz));
     if (F) e = e + fe;
-    LV r;
-    if constexpr (kCombined) {
-      L su = cfr[15] * v1[0].x, sw = cfr[15] * v3[0].x;
+    L su = cfr[15] * v1[0].x, sw = cfr[15] * v3[0].x;
 #pragma unroll
-      for (int j = 1; j < 5; ++j) {
-        su = su + cfr[15 + j] * v1[j].x;
-        sw = sw + cfr[15 + j] * v3[j].x;
-      }
-      r = mk<LV>(su, sw);
-    } else {
-      L su = drL[0] * v1[0].x, sw = drL[0] * v3[0].x, tu = drL[10] * v1[0].x, tw = drL[10] * v3[0].x;
-#pragma unroll
-      for (int j = 1; j < 5; ++j) {
-        su = su + drL[j] * v1[j].x;
-        sw = sw + drL[j] * v3[j].x;
-        tu = tu + drL[10 + j] * v1[j].x;
-        tw = tw + drL[10 + j] * v3[j].x;
-      }
-      r = lmul(lam, mk<LV>(su, sw)) + mk<LV>(nu * tu, nu * tw);
+    for (int j = 1; j < 5; ++j) {
+      su = su + cfr[15 + j] * v1[j].x;
+      sw = sw + cfr[15 + j] * v3[j].x;
     }
+    LV r = mk<LV>(su, sw);
     const O2 o = old[r0];
     r = r + lmul(lode2, e);
     r = r - lmul(lode3, mk<LV>(conv<L>(o.x), conv<L>(o.y)));
@@ -278,28 +247,15 @@ __global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2*
     rhs[r0] = make_double2(Num<L>::to_double(r.x), Num<L>::to_double(r.y));
   } else {  // eta (:656-661): with w = i kz V1 - i kx V3, unkn = D0(w), impl = ni (D2(w) - k2 D0(w))
     const V2 ee = mul_ia<V2>(tb, rhsu) - mul_ia<V2>(ta, rhsw);
-    LV r;
-    if constexpr (kCombined) {
-      L nj = cfr[15] + k2 * cfr[20];
-      LV s1 = lmul(nj, v1[0]), s3 = lmul(nj, v3[0]);
+    L nj = cfr[15] + k2 * cfr[20];
+    LV s1 = lmul(nj, v1[0]), s3 = lmul(nj, v3[0]);
 #pragma unroll
-      for (int j = 1; j < 5; ++j) {
-        nj = cfr[15 + j] + k2 * cfr[20 + j];
-        s1 = s1 + lmul(nj, v1[j]);
-        s3 = s3 + lmul(nj, v3[j]);
-      }
-      r = mul_ia<LV>(b, s1) - mul_ia<LV>(a, s3);
-    } else {  // with w = i kz V1 - i kx V3: unkn = D0(w), impl = ni (D2(w) - k2 D0(w))
-      LV w = mul_ia<LV>(b, v1[0]) - mul_ia<LV>(a, v3[0]);
-      LV s0 = lmul(drL[0], w), s2 = lmul(drL[10], w);
-#pragma unroll
-      for (int j = 1; j < 5; ++j) {
-        w = mul_ia<LV>(b, v1[j]) - mul_ia<LV>(a, v3[j]);
-        s0 = s0 + lmul(drL[j], w);
-        s2 = s2 + lmul(drL[10 + j], w);
-      }
-      r = lmul(lam, s0) + lmul(nu, s2 - lmul(k2, s0));
+    for (int j = 1; j < 5; ++j) {
+      nj = cfr[15 + j] + k2 * cfr[20 + j];
+      s1 = s1 + lmul(nj, v1[j]);
+      s3 = s3 + lmul(nj, v3[j]);
     }
+    LV r = mul_ia<LV>(b, s1) - mul_ia<LV>(a, s3);
     const O2 o = old[r0];
     LV e = mk<LV>(conv<L>(ee.x), conv<L>(ee.y));
     if (F) e = e + fe;
