@@ -69,7 +69,7 @@ struct chgpu_handle {
   void* cst = nullptr;  // transform-type constants: factor, 1/dx, 1/dz, 1/dy per plane
   double* d0lu = nullptr;
   double* nud = nullptr;  // per row: -ni d4, -ni d2 (the mode-independent matrix terms)
-  void* lindd = nullptr;  // double-float d1 / D0mat / d0 rows for v' and u, w (mixed path)
+  void* lindd = nullptr;  // double-float d1 / D0mat / d0 rows for v' and u, w (mixed and double-float paths)
   double* yint = nullptr;
   double* dy = nullptr;
   void* twz = nullptr;
@@ -596,10 +596,9 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
       if ((rc = upload_derT<double>(h))) break;
       if ((rc = upload_derL<double>(h))) break;
     }
-    // mixed path: v' and u, w in double-float (FP64DD keeps them FP64, whose
-    // flow-rate correction amplifies their rounding ~1e3 into Runtimedata);
-    // per y row: d1 row, D0mat factors (rows 1..ny-1), d0 row
-    if (h->prec == CHGPU_MIXED) {
+    // mixed and double-float paths: v' and u, w in double-float; per y row:
+    // d1 row, D0mat factors (rows 1..ny-1), d0 row
+    if (h->prec != CHGPU_FP64) {
       std::vector<dd> ld((size_t)(p->ny + 1) * 15, dd());
       for (int iy = 0; iy <= p->ny; ++iy)
         for (int j = 0; j < 5; ++j) {

@@ -384,8 +384,8 @@ __device__ __forceinline__ double2 dot5(const double2* v, const double* c) {
 
 }  // namespace
 
-// Arithmetic of the v' / u, w pass: FP64, or double-float in the mixed path
-// (the FP64 pipe is the bound of this kernel).  The Step1
+// Arithmetic of the v' / u, w pass: FP64, or double-float in the mixed and
+// double-float paths (the FP64 pipe is the bound of this kernel).  The Step1
 // result is parked in the field's w slot between the two sweeps (16 bytes
 // either way).
 template <typename R> struct DerivOps;
