@@ -396,7 +396,7 @@ def run_ours(args):
     hbm_peak = peaks.get("hbm_gbs")
     peak_src = "measured" if hbm_peak else "fallback"
     hbm_peak = hbm_peak or 6800.0
-    fp64_peak_tflops = 1.196  # FP64 FMA throughput measured on this machine's GB300 (profiles/fp64_fp32_peaks.md)
+    fp64_peak_tflops = 1.196  # FP64 FMA throughput of GB300, measured with an FMA loop (8 chains per thread)
     nprof = max(2, min(K, 10))
 
     def attribution(prec, mixed):

@@ -2,7 +2,7 @@
 ! Fortran 2008 interface to libchgpu.so (include/chgpu.h).    !
 ! Lets a Fortran driver shaped like channel.f90 call the GB300 !
 ! time step through iso_c_binding.  Compile with the driver    !
-! and link -lchgpu (see INTEGRATION.md).                       !
+! and link -lchgpu (channel_gb300/_build/libchgpu.so).        !
 !==============================================================!
 MODULE chgpu_interface
   USE, INTRINSIC :: iso_c_binding
