@@ -512,7 +512,10 @@ __device__ __forceinline__ void deriv_uw(double2* __restrict__ V, const double* 
 // A block holds 32 pairs: warp 0 the v systems, warp 1 the eta systems.  After
 // both have written v and eta, role r takes mode (kx, (1-2r)|kz|) for v' and
 // the u, w recovery.
-__global__ void __launch_bounds__(64) k_linsolve(double2* __restrict__ V, const double2* rhs, size_t rcs, int roff,
+// registers capped for 8 resident 64-thread blocks per SM: at 147 456 pairs
+// (383x384x383) the extra warps hide the recurrences' latency (-19% per
+// launch); at 16 384 pairs the grid, not the registers, limits residency
+__global__ void __launch_bounds__(64, 8) k_linsolve(double2* __restrict__ V, const double2* rhs, size_t rcs, int roff,
                                                  double* __restrict__ fac, const double* __restrict__ der,
                                                  const double* __restrict__ d0lu, const double* __restrict__ yint,
                                                  BcRows bc, Dims d, double lambda_in, double ode1,
