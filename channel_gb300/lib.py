@@ -92,6 +92,7 @@ SIGNATURES = {
     "chgpu_autotune": (C.c_int, [_P]),
     "chgpu_tiles": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "chgpu_set_tiles": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "chgpu_set_step_halves": (C.c_int, [_P, C.c_int]),
     "chgpu_export_dims": (C.c_int, [_P, C.c_float, C.POINTER(C.c_int)]),
     "chgpu_export_physical": (C.c_int, [_P, C.POINTER(ExportOpts), _DP]),
     "chgpu_stats_reset": (C.c_int, [_P]),
@@ -257,6 +258,10 @@ class Channel:
 
     def set_tiles(self, tiles) -> None:
         self._check(self.lib.chgpu_set_tiles(self.h, (C.c_int * 5)(*tiles)))
+
+    def set_step_halves(self, halves: int) -> None:
+        """1: the step on one stream; 2: rhs / solve split in two kx halves on two streams."""
+        self._check(self.lib.chgpu_set_step_halves(self.h, halves))
 
     def export_dims(self, undersample: float = 1.0) -> tuple[int, int, int]:
         d = (C.c_int * 3)()

@@ -157,6 +157,11 @@ int chgpu_tiles(const chgpu_handle* h, int tiles[CHGPU_NTILES]);
 /* Applies tiles found by chgpu_autotune on another handle of the same sizes
  * and precision; CHGPU_E_PARAM when they do not fit this handle. */
 int chgpu_set_tiles(chgpu_handle* h, const int tiles[CHGPU_NTILES]);
+/* The captured step as one stream (1) or with k_rhs, k_linsolve and the
+ * next z-inverse split in two kx halves on two streams (2), which overlaps
+ * one half's solve with the other half's work; the default is 2 from 65 536
+ * (kx, +-kz) pairs on, else 1.  Results do not depend on it. */
+int chgpu_set_step_halves(chgpu_handle* h, int halves);
 
 /* Physical-space export of the field: the reference's exporter
  * out_exporter/out2bin.f90 (convert_outfile :141-203, xz_interpolation

@@ -242,3 +242,27 @@ def test_stepped_field_is_divergence_free(gpu_lib, prec, tol):
             worst = max(worst, float(np.abs(res).max() / scale))
     assert worst <= tol, worst
     g.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_two_half_step_is_identical(gpu_lib, prec):
+    """The step split in two kx halves on two streams (the default for large
+    grids) gives the one-stream step's field and Runtimedata bit for bit,
+    also with the body force on."""
+    p, V0, _, g = make("small", 0.02, 5, prec)
+    from channel_gb300 import Channel, initial
+
+    t = Channel(p, prec)
+    t.upload(V0)
+    g.set_step_halves(1)
+    t.set_step_halves(2)
+    F = 0.02 * (initial.perturbed_laminar(p, 1.0, 9) - initial.perturbed_laminar(p, 0.0, 9))
+    for h in (g, t):
+        h.set_body_force(F)
+        h.start()
+    for _ in range(3):
+        lg, lt = g.step(), t.step()
+    assert np.array_equal(g.download(), t.download())
+    assert np.array_equal(lg, lt)
+    g.close()
+    t.close()
