@@ -147,6 +147,16 @@ MODULE chgpu_interface
       TYPE(chgpu_export_opts), INTENT(IN) :: opts
       REAL(C_DOUBLE), INTENT(OUT) :: vec(*)
     END FUNCTION
+    ! transform tiles timed on this handle (optional; results do not depend on them)
+    INTEGER(C_INT) FUNCTION chgpu_autotune(h) BIND(C, name="chgpu_autotune")
+      IMPORT :: C_INT, C_PTR
+      TYPE(C_PTR), VALUE :: h
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION chgpu_set_step_halves(h, halves) BIND(C, name="chgpu_set_step_halves")
+      IMPORT :: C_INT, C_PTR
+      TYPE(C_PTR), VALUE :: h
+      INTEGER(C_INT), VALUE :: halves
+    END FUNCTION
     TYPE(C_PTR) FUNCTION chgpu_last_error(h) BIND(C, name="chgpu_last_error")
       IMPORT :: C_PTR
       TYPE(C_PTR), VALUE :: h

@@ -70,3 +70,27 @@ def test_driver_rejects_mismatched_restart(gpu_lib, tmp_path):
     r = subprocess.run([str(build.DRIVER), "--quiet"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
     assert r.returncode == 1
     assert "mismatch in metadata" in r.stderr
+
+
+@pytest.mark.parametrize("flag,tol", [("--fp64dd", 1e-10), ("--mixed", 1e-4)])
+def test_driver_precision_flags(gpu_lib, tmp_path, flag, tol):
+    """The driver's --fp64dd and --mixed runs give the FP64 run's
+    Runtimedata to their precision (wall shear, flow rate, CFL*dt)."""
+    from channel_gb300 import build, dnsin, fields, initial
+
+    p = dnsin.workload("small")
+    p.nstep = 4
+    runs = {}
+    for f in ("", flag):
+        d = tmp_path / (f.strip("-") or "fp64")
+        d.mkdir()
+        dnsin.write(d / "dns.in", p)
+        initial.write_initial(d / "Dati.cart.out", p, 0.01, 0)
+        r = subprocess.run([str(build.DRIVER), "--quiet"] + ([f] if f else []), cwd=d, capture_output=True, text=True,
+                           timeout=300)
+        assert r.returncode == 0, r.stdout + r.stderr
+        runs[f] = fields.parse_runtimedata(d / "Runtimedata")
+    a, b = runs[flag], runs[""]
+    assert a.shape == b.shape == (5, 11)
+    for col in (1, 2, 5, 9):
+        assert np.abs(a[:, col] - b[:, col]).max() <= tol * np.abs(b[:, col]).max(), col
