@@ -657,7 +657,11 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
 
 int chgpu_destroy(chgpu_handle* h) {
   if (!h) return 0;
+  // work in flight on any of the handle's streams (a snapshot copy into the
+  // pinned buffer, a half of the split step) ends before anything is freed
   if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->stream2) cudaStreamSynchronize(h->stream2);
+  if (h->snap_stream) cudaStreamSynchronize(h->snap_stream);
   release(h);
   delete h;
   return 0;
