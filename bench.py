@@ -350,6 +350,47 @@ def cpu_baseline(p, V0, max_seconds=20.0):
                       f"(reference Fortran/MPI/FFTW not buildable here), OpenMP over planes and modes"}
 
 
+def run_long(args):
+    """FP64, FP64DD and mixed stepped side by side from the same field for
+    --steps steps: the largest deviation from FP64 over the run of the wall
+    shear, the pressure gradient and the time step, and the final mean and
+    rms profiles (the statistics the correctness statement names)."""
+    from channel_gb300 import Channel, dnsin, initial
+
+    p = dnsin.workload(args.workload)
+    V0 = initial.perturbed_laminar(p, AMPLITUDE[args.workload], seed=0)
+    runs = {}
+    for prec in ("fp64", "fp64dd", "mixed"):
+        g = tuned(Channel(p, prec), prec)
+        g.upload(V0)
+        lines = [g.start()]
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            lines.append(g.step())
+        wall = time.perf_counter() - t0
+        runs[prec] = {"lines": np.array(lines), "V": g.download(), "s": wall}
+        g.close()
+    ref = runs["fp64"]
+    U64, r64 = profiles(ref["V"])
+    out = {"mode": "long", "workload": workload_desc(p, "FP64"), "steps": args.steps,
+           "time_units": float(ref["lines"][-1][0] - ref["lines"][0][0])}
+    for prec in ("fp64dd", "mixed"):
+        L, R = runs[prec]["lines"], ref["lines"]
+
+        def dev(cols):
+            return float(np.max(np.abs(L[:, cols] - R[:, cols])) / np.max(np.abs(R[:, cols])))
+
+        U, rr = profiles(runs[prec]["V"])
+        out[prec] = {"wall_shear_max_rel": dev([1, 2]), "dpdx_max_rel": dev([6]), "dt_max_rel": dev([10]),
+                     "mean_U_final": rel(U, U64), "rms_u_final": rel(rr[0], r64[0]), "rms_v_final": rel(rr[1], r64[1]),
+                     "rms_w_final": rel(rr[2], r64[2]), "fields_final": [rel(runs[prec]["V"][c], ref["V"][c])
+                                                                          for c in range(3)],
+                     "wall_s": runs[prec]["s"]}
+    out["fp64_wall_s"] = ref["s"]
+    out["wall_shear_fp64_first_last"] = [float(ref["lines"][0][1]), float(ref["lines"][-1][1])]
+    print(json.dumps(out), flush=True)
+
+
 def run_ours(args):
     from channel_gb300 import dnsin, initial
 
@@ -539,8 +580,9 @@ def main():
                     help="fixed transform tiles instead of autotuning, e.g. fp64:8,4,2,256,256/mixed:8,4,3,256,192 "
                          "(z columns, x rows, x-row variant, z threads, x threads; for reproducible profiler "
                          "captures)")
-    ap.add_argument("--mode", default="full", choices=["full", "timed"],
-                    help="timed: only the FP64 and mixed timed runs (for profiler captures)")
+    ap.add_argument("--mode", default="full", choices=["full", "timed", "long"],
+                    help="timed: only the three timed runs (for profiler captures); long: --steps steps of FP64, "
+                         "FP64DD and mixed from one field, Runtimedata and profile errors against FP64 over the run")
     args = ap.parse_args()
     for item in filter(None, args.tiles.split("/")):
         prec, t = item.split(":")
@@ -551,7 +593,10 @@ def main():
 
     if args.impl == "ours":
         b.build()
-        run_ours(args)
+        if args.mode == "long":
+            run_long(args)
+        else:
+            run_ours(args)
     else:
         run_reference(args)
 
