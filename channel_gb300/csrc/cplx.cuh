@@ -108,6 +108,15 @@ template <int SIGN, typename V> __device__ __forceinline__ void dft4(V& a0, V& a
   a2 = t0 - t2;
   a3 = t1 - t3;
 }
+// double-float: the first-level sums feed only the second level, so they
+// skip the renormalisation; the outputs are normalised
+template <int SIGN> __device__ __forceinline__ void dft4(cdd& a0, cdd& a1, cdd& a2, cdd& a3) {
+  const cdd t0 = add_nr(a0, a2), t1 = sub_nr(a0, a2), t2 = add_nr(a1, a3), t3 = mul_is<SIGN>(sub_nr(a1, a3));
+  a0 = t0 + t2;
+  a1 = t1 + t3;
+  a2 = t0 - t2;
+  a3 = t1 - t3;
+}
 
 template <int R, typename V> struct Dft;
 template <typename V> struct Dft<2, V> {

@@ -46,6 +46,15 @@ __device__ __forceinline__ dd operator+(dd a, dd b) {
   const float e = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
   return fast_two_sum(s.hi, e);
 }
+// Addition without the final renormalisation (8 FP32 operations): the high
+// parts summed error-free, the low parts and the error in FP32.  For
+// intermediate sums that only feed further arithmetic: the pair's low part
+// may exceed half an ulp of its high part by a few ulps, which the next
+// error-free sum of the high parts absorbs.
+__device__ __forceinline__ dd add_nr(dd a, dd b) {
+  const dd s = two_sum(a.hi, b.hi);
+  return dd(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
 __device__ __forceinline__ dd operator-(dd a) { return dd(-a.hi, -a.lo); }
 __device__ __forceinline__ dd operator-(dd a, dd b) { return a + (-b); }
 __device__ __forceinline__ dd operator*(dd a, dd b) {
@@ -86,6 +95,8 @@ struct __align__(16) cdd {
 __device__ __forceinline__ cdd cmul(cdd a, cdd b) { return cdd{dd_dot2(a.x, b.x, -a.y, b.y), dd_dot2(a.x, b.y, a.y, b.x)}; }
 __device__ __forceinline__ cdd operator+(cdd a, cdd b) { return cdd{a.x + b.x, a.y + b.y}; }
 __device__ __forceinline__ cdd operator-(cdd a, cdd b) { return cdd{a.x - b.x, a.y - b.y}; }
+__device__ __forceinline__ cdd add_nr(cdd a, cdd b) { return cdd{add_nr(a.x, b.x), add_nr(a.y, b.y)}; }
+__device__ __forceinline__ cdd sub_nr(cdd a, cdd b) { return cdd{add_nr(a.x, -b.x), add_nr(a.y, -b.y)}; }
 
 // FP64 -> double-float with integer operations only: conversions between
 // FP64 and FP32 run at the FP64 rate on GB300 (measured ~580 G/s against
