@@ -108,6 +108,18 @@ template <int SIGN, typename V> __device__ __forceinline__ void dft4(V& a0, V& a
   a2 = t0 - t2;
   a3 = t1 - t3;
 }
+// radix-4 butterfly whose outputs feed only further arithmetic inside a
+// larger register DFT: for double-float no sum is renormalised
+template <int SIGN, typename V> __device__ __forceinline__ void dft4_inner(V& a0, V& a1, V& a2, V& a3) {
+  dft4<SIGN>(a0, a1, a2, a3);
+}
+template <int SIGN> __device__ __forceinline__ void dft4_inner(cdd& a0, cdd& a1, cdd& a2, cdd& a3) {
+  const cdd t0 = add_nr(a0, a2), t1 = sub_nr(a0, a2), t2 = add_nr(a1, a3), t3 = mul_is<SIGN>(sub_nr(a1, a3));
+  a0 = add_nr(t0, t2);
+  a1 = add_nr(t1, t3);
+  a2 = sub_nr(t0, t2);
+  a3 = sub_nr(t1, t3);
+}
 // double-float: the first-level sums feed only the second level, so they
 // skip the renormalisation; the outputs are normalised
 template <int SIGN> __device__ __forceinline__ void dft4(cdd& a0, cdd& a1, cdd& a2, cdd& a3) {
@@ -146,8 +158,8 @@ template <typename V> struct Dft<8, V> {
     using T = decltype(V::x);
     const T r2 = Num<T>::sqrt1_2();
     const T sr2 = SIGN > 0 ? r2 : -r2;
-    dft4<SIGN>(a[0], a[2], a[4], a[6]);
-    dft4<SIGN>(a[1], a[3], a[5], a[7]);
+    dft4_inner<SIGN>(a[0], a[2], a[4], a[6]);
+    dft4_inner<SIGN>(a[1], a[3], a[5], a[7]);
     a[3] = cmul(a[3], mk<V>(r2, sr2));   // w8^1
     a[5] = mul_is<SIGN>(a[5]);           // w8^2
     a[7] = cmul(a[7], mk<V>(-r2, sr2));  // w8^3
@@ -168,7 +180,7 @@ template <typename V> struct Dft<16, V> {
     const T c = Num<T>::cos_pi8(), s = Num<T>::sin_pi8(), r2 = Num<T>::sqrt1_2();
     const T ss = SIGN > 0 ? s : -s, sc = SIGN > 0 ? c : -c, sr2 = SIGN > 0 ? r2 : -r2;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) dft4<SIGN>(a[q], a[q + 4], a[q + 8], a[q + 12]);
+    for (int q = 0; q < 4; ++q) dft4_inner<SIGN>(a[q], a[q + 4], a[q + 8], a[q + 12]);
     // b[r2][k1] sits in a[r2 + 4 k1]
     a[1 + 4] = cmul(a[1 + 4], mk<V>(c, ss));      // w^1
     a[1 + 8] = cmul(a[1 + 8], mk<V>(r2, sr2));    // w^2
