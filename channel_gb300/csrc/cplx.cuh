@@ -70,6 +70,14 @@ template <int SIGN, typename V> __device__ __forceinline__ V cmul_s(V a, V w) {
 template <int SIGN> __device__ __forceinline__ cdd cmul_s(cdd a, cdd w) {
   return SIGN < 0 ? cmul(a, w) : cdd{dd_dot2(a.x, w.x, a.y, w.y), dd_dot2(a.y, w.x, -a.x, w.y)};
 }
+// products that feed only further sums inside a register DFT: for
+// double-float without the final renormalisation
+template <typename V> __device__ __forceinline__ V cmul_inner(V a, V b) { return cmul(a, b); }
+__device__ __forceinline__ cdd cmul_inner(cdd a, cdd b) { return cmul_nr(a, b); }
+template <int SIGN, typename V> __device__ __forceinline__ V cmul_s_inner(V a, V w) { return cmul_s<SIGN>(a, w); }
+template <int SIGN> __device__ __forceinline__ cdd cmul_s_inner(cdd a, cdd w) {
+  return SIGN < 0 ? cmul_nr(a, w) : cdd{dd_dot2_nr(a.x, w.x, a.y, w.y), dd_dot2_nr(a.y, w.x, -a.x, w.y)};
+}
 
 // w_N^m = exp(SIGN 2 pi i m / N) for N dividing 24 (m fixed at compile
 // time after unrolling), from the constants of the type: angles are
@@ -160,9 +168,9 @@ template <typename V> struct Dft<8, V> {
     const T sr2 = SIGN > 0 ? r2 : -r2;
     dft4_inner<SIGN>(a[0], a[2], a[4], a[6]);
     dft4_inner<SIGN>(a[1], a[3], a[5], a[7]);
-    a[3] = cmul(a[3], mk<V>(r2, sr2));   // w8^1
+    a[3] = cmul_inner(a[3], mk<V>(r2, sr2));   // w8^1
     a[5] = mul_is<SIGN>(a[5]);           // w8^2
-    a[7] = cmul(a[7], mk<V>(-r2, sr2));  // w8^3
+    a[7] = cmul_inner(a[7], mk<V>(-r2, sr2));  // w8^3
     V y[8];
 #pragma unroll
     for (int k1 = 0; k1 < 4; ++k1) {
@@ -182,15 +190,15 @@ template <typename V> struct Dft<16, V> {
 #pragma unroll
     for (int q = 0; q < 4; ++q) dft4_inner<SIGN>(a[q], a[q + 4], a[q + 8], a[q + 12]);
     // b[r2][k1] sits in a[r2 + 4 k1]
-    a[1 + 4] = cmul(a[1 + 4], mk<V>(c, ss));      // w^1
-    a[1 + 8] = cmul(a[1 + 8], mk<V>(r2, sr2));    // w^2
-    a[1 + 12] = cmul(a[1 + 12], mk<V>(s, sc));    // w^3
-    a[2 + 4] = cmul(a[2 + 4], mk<V>(r2, sr2));    // w^2
+    a[1 + 4] = cmul_inner(a[1 + 4], mk<V>(c, ss));      // w^1
+    a[1 + 8] = cmul_inner(a[1 + 8], mk<V>(r2, sr2));    // w^2
+    a[1 + 12] = cmul_inner(a[1 + 12], mk<V>(s, sc));    // w^3
+    a[2 + 4] = cmul_inner(a[2 + 4], mk<V>(r2, sr2));    // w^2
     a[2 + 8] = mul_is<SIGN>(a[2 + 8]);            // w^4
-    a[2 + 12] = cmul(a[2 + 12], mk<V>(-r2, sr2));  // w^6
-    a[3 + 4] = cmul(a[3 + 4], mk<V>(s, sc));      // w^3
-    a[3 + 8] = cmul(a[3 + 8], mk<V>(-r2, sr2));   // w^6
-    a[3 + 12] = cmul(a[3 + 12], mk<V>(-c, -ss));  // w^9
+    a[2 + 12] = cmul_inner(a[2 + 12], mk<V>(-r2, sr2));  // w^6
+    a[3 + 4] = cmul_inner(a[3 + 4], mk<V>(s, sc));      // w^3
+    a[3 + 8] = cmul_inner(a[3 + 8], mk<V>(-r2, sr2));   // w^6
+    a[3 + 12] = cmul_inner(a[3 + 12], mk<V>(-c, -ss));  // w^9
     V y[16];
 #pragma unroll
     for (int k1 = 0; k1 < 4; ++k1) {
@@ -276,7 +284,7 @@ __device__ __forceinline__ void stockham_stage(const V* __restrict__ src, V* __r
     if (Ns > 1) {
       const V* w = twst + k * (R - 1);
 #pragma unroll
-      for (int r = 1; r < R; ++r) a[r] = cmul_s<SIGN>(a[r], ldg_v(w + r - 1));
+      for (int r = 1; r < R; ++r) a[r] = cmul_s_inner<SIGN>(a[r], ldg_v(w + r - 1));
     }
     Dft<R, V>::template run<SIGN>(a);
     const int dbase = t * n + (j - k) * R + k;

@@ -87,12 +87,30 @@ __device__ __forceinline__ dd dd_dot2(dd x1, dd y1, dd x2, dd y2) {
   return fast_two_sum(s.hi, s.lo);
 }
 
+// the same without the final renormalisation, for products that feed only
+// further sums
+__device__ __forceinline__ dd dd_dot2_nr(dd x1, dd y1, dd x2, dd y2) {
+  const float p1 = __fmul_rn(x1.hi, y1.hi);
+  float e1 = __fmaf_rn(x1.hi, y1.hi, -p1);
+  e1 = __fmaf_rn(x1.hi, y1.lo, e1);
+  e1 = __fmaf_rn(x1.lo, y1.hi, e1);
+  const float p2 = __fmul_rn(x2.hi, y2.hi);
+  float e2 = __fmaf_rn(x2.hi, y2.hi, -p2);
+  e2 = __fmaf_rn(x2.hi, y2.lo, e2);
+  e2 = __fmaf_rn(x2.lo, y2.hi, e2);
+  const dd s = two_sum(p1, p2);
+  return dd(s.hi, __fadd_rn(s.lo, __fadd_rn(e1, e2)));
+}
+
 // complex double-float: 16 bytes, like double2
 struct __align__(16) cdd {
   dd x, y;
 };
 // complex product in two fused dot products (38 FP32 operations instead of 68)
 __device__ __forceinline__ cdd cmul(cdd a, cdd b) { return cdd{dd_dot2(a.x, b.x, -a.y, b.y), dd_dot2(a.x, b.y, a.y, b.x)}; }
+__device__ __forceinline__ cdd cmul_nr(cdd a, cdd b) {
+  return cdd{dd_dot2_nr(a.x, b.x, -a.y, b.y), dd_dot2_nr(a.x, b.y, a.y, b.x)};
+}
 __device__ __forceinline__ cdd operator+(cdd a, cdd b) { return cdd{a.x + b.x, a.y + b.y}; }
 __device__ __forceinline__ cdd operator-(cdd a, cdd b) { return cdd{a.x - b.x, a.y - b.y}; }
 __device__ __forceinline__ cdd add_nr(cdd a, cdd b) { return cdd{add_nr(a.x, b.x), add_nr(a.y, b.y)}; }
