@@ -451,6 +451,7 @@ void fill_stats(const chgpu_handle* h, chgpu_stats* st) {
 int pull_scalars(chgpu_handle* h) {
   CK(h, cudaMemcpyAsync(h->sc_host, h->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->stream));
   CK(h, cudaStreamSynchronize(h->stream));
+  if (h->sc_host->error & 2) return fail(h, CHGPU_E_CUDA, "a bulk copy into shared memory did not complete in time");
   if (h->sc_host->error & 1) return fail(h, CHGPU_E_NONFINITE, "non-finite CFL or statistics (flow field blew up)");
   return 0;
 }

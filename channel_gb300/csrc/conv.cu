@@ -190,12 +190,49 @@ __global__ void __launch_bounds__(256, MINB) k_xrow(const typename C2<T>::t* __r
   }
 }
 
+// ---------------------------------------------------------------------------
+// bulk asynchronous copy global -> shared through the TMA unit, completed on
+// an mbarrier (cp.async.bulk with complete_tx); every wait is bounded
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+// true once phase `parity` of the barrier has completed; false after
+// `limit` polls
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, int limit) {
+  for (int i = 0; i < limit; ++i) {
+    unsigned done = 0;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+constexpr int kBulkWaitPolls = 1 << 22;  // each try_wait itself waits a while: seconds in all
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_zfwd(const typename C2<T>::t* __restrict__ Pb, typename C2<T>::t* __restrict__ VV,
                                               const typename C2<T>::t* __restrict__ twz, Dims d, RadixDev rz,
-                                              int nb_cols, int plane0) {
+                                              int nb_cols, int plane0, DevScalars* __restrict__ sc) {
   using V2 = typename C2<T>::t;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) unsigned long long bar;
   const int nzd = d.nzd, nz = d.nz, nxp = d.nx + 1, nzt = d.nzt;
   V2* bufA = reinterpret_cast<V2*>(smem_raw);
   V2* bufB = bufA + pad32_size(nb_cols * nzd);
@@ -205,7 +242,19 @@ __global__ void __launch_bounds__(256) k_zfwd(const typename C2<T>::t* __restric
   const int nb = min(nb_cols, nxp - ix0);
   const size_t colbase = ((size_t)p * d.nplanes + plane) * nxp;
   const V2* in = Pb + (colbase + ix0) * nzd;
-  for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) bufA[pad32(idx)] = in[idx];
+  // the block's columns are one contiguous run of Pb (nzd even: 16-byte
+  // aligned, a multiple of 16 bytes): one bulk copy into the scratch buffer,
+  // then into the padded transform layout
+  const unsigned bytes = (unsigned)((size_t)nb * nzd * sizeof(V2));
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  if (threadIdx.x == 0) bulk_copy_g2s(bufB, in, bytes, &bar);
+  if (!mbar_wait(&bar, 0, kBulkWaitPolls)) {
+    if (threadIdx.x == 0) atomicOr(&sc->error, 2);
+    mbar_wait(&bar, 0, kBulkWaitPolls);  // the copy in flight, once more
+    return;
+  }
+  for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) bufA[pad32(idx)] = bufB[idx];
   __syncthreads();
   V2* res = fft_block<-1>(bufA, bufB, nb, rz, twz);
   const FastDiv by_nzt(nzt);
@@ -243,7 +292,8 @@ void launch_convolutions(const ConvLaunch& L, cudaStream_t s, int stage) {
   if (stage == 2) {
     dim3 grid((nxp + L.zcols - 1) / L.zcols, L.nplanes, 6);
     size_t sm = conv_z_smem(L.zcols, d.nzd, sizeof(V2));
-    k_zfwd<T><<<grid, L.zthreads, sm, s>>>((const V2*)L.Pb, (V2*)L.VV, (const V2*)L.twz, d, L.rz, L.zcols, L.plane0);
+    k_zfwd<T><<<grid, L.zthreads, sm, s>>>((const V2*)L.Pb, (V2*)L.VV, (const V2*)L.twz, d, L.rz, L.zcols, L.plane0,
+                                           L.sc);
   }
 }
 

@@ -57,7 +57,9 @@ struct RadixDev {
 // whole warp on one bank; with it every warp access needs only the minimum
 // number of wavefronts for 8- and 16-byte elements.
 __device__ __forceinline__ int pad32(int i) { return i + (i >> 5); }
-__host__ __device__ constexpr int pad32_size(int n) { return n + (n >> 5) + 1; }
+// even, so that a buffer placed after one of 8-byte elements starts on a
+// 16-byte boundary (what bulk copies into it need)
+__host__ __device__ constexpr int pad32_size(int n) { return (n + (n >> 5) + 2) & ~1; }
 
 // a * (SIGN * i)
 template <int SIGN, typename V> __device__ __forceinline__ V mul_is(V a) {
