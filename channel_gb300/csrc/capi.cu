@@ -540,7 +540,7 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
   // shared-memory budget (two ping-pong buffers; nine row buffers)
   const size_t ts = tsize(h);
   h->zcols = 8;
-  while (h->zcols > 1 && conv_z_smem(h->zcols, nzd, ts) > 100 * 1024) --h->zcols;
+  while (h->zcols > 1 && conv_zinv_smem(h->zcols, nzd, d.nzt, ts) > 100 * 1024) --h->zcols;
   // rows per x block: the most that keep two resident blocks per SM (228 KB
   // of shared memory per SM, 1 KB reserved per block); chgpu_autotune may
   // choose otherwise by timing
@@ -548,7 +548,7 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
   h->xrows = 1;
   while (h->xrows < 4 && conv_x_smem(2 * h->xrows, nxd, ts) <= xbudget && nzd % (2 * h->xrows) == 0)
     h->xrows *= 2;
-  if (conv_x_smem(h->xrows, nxd, ts) > 227 * 1024 || conv_z_smem(1, nzd, ts) > 227 * 1024) {
+  if (conv_x_smem(h->xrows, nxd, ts) > 227 * 1024 || conv_zinv_smem(1, nzd, d.nzt, ts) > 227 * 1024) {
     delete h;
     return fail(nullptr, CHGPU_E_PARAM, "transform length too large for one thread block");
   }
@@ -1050,7 +1050,7 @@ int chgpu_autotune(chgpu_handle* h) {
   };
   h->zthreads = 256;
   for (int zc = 1; zc <= 8; zc *= 2) {
-    if (conv_z_smem(zc, nzd, ts) > lim) break;
+    if (conv_zinv_smem(zc, nzd, h->d.nzt, ts) > lim) break;
     h->zcols = zc;
     if (int rc = time_z(&ms)) return rc;
     if (ms < best) {
@@ -1114,7 +1114,7 @@ int chgpu_set_tiles(chgpu_handle* h, const int tiles[CHGPU_NTILES]) {
   const size_t ts = tsize(h), lim = (size_t)optin - 1024;
   const int zc = tiles[0], xr = tiles[1], xb = tiles[2], zt = tiles[3], xt = tiles[4];
   auto threads_ok = [](int t) { return t >= 64 && t <= 256 && t % 32 == 0; };
-  if (zc < 1 || zc > 8 || conv_z_smem(zc, h->d.nzd, ts) > lim || (xr != 1 && xr != 2 && xr != 4) ||
+  if (zc < 1 || zc > 8 || conv_zinv_smem(zc, h->d.nzd, h->d.nzt, ts) > lim || (xr != 1 && xr != 2 && xr != 4) ||
       h->d.nzd % xr != 0 || conv_x_smem(xr, h->d.nxd, ts) > lim || xb < 1 || xb > 3 || !threads_ok(zt) ||
       !threads_ok(xt))
     return fail(h, CHGPU_E_PARAM, "chgpu_set_tiles: tiles outside what this handle's sizes allow");

@@ -17,6 +17,7 @@
 // T is the arithmetic type: double (plain FP64 step) or float (mixed step).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <type_traits>
 
@@ -25,40 +26,6 @@
 #include "kernels.cuh"
 
 namespace chgpu {
-
-template <typename T>
-__global__ void __launch_bounds__(256) k_zinv(const double2* __restrict__ V, typename C2<T>::t* __restrict__ Zb,
-                                              const typename C2<T>::t* __restrict__ twz, Dims d, RadixDev rz,
-                                              int nb_cols, int plane0, int ix_lo, int ix_hi) {
-  using V2 = typename C2<T>::t;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int nzd = d.nzd, nz = d.nz, nxp = d.nx + 1;
-  V2* bufA = reinterpret_cast<V2*>(smem_raw);
-  V2* bufB = bufA + pad32_size(nb_cols * nzd);
-  const int c = blockIdx.z;
-  const int plane = plane0 + blockIdx.y;
-  const int ix0 = ix_lo + blockIdx.x * nb_cols;
-  const int nb = min(nb_cols, ix_hi - ix0);
-  const size_t colbase = ((size_t)c * d.nplanes + plane) * nxp;
-  const FastDiv by_nzd(nzd);
-  for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) {
-    const int b = by_nzd.div(idx);
-    const int jz = idx - b * nzd;
-    V2 val = czero<V2>();
-    int izp = -1;
-    if (jz <= nz) izp = nz + jz;
-    else if (jz >= nzd - nz) izp = jz - nzd + nz;
-    if (izp >= 0) {
-      double2 x = V[(colbase + ix0 + b) * d.nzt + izp];
-      val = mk<V2>(Num<T>::from_double(x.x), Num<T>::from_double(x.y));
-    }
-    bufA[pad32(idx)] = val;
-  }
-  __syncthreads();
-  V2* res = fft_block<+1>(bufA, bufB, nb, rz, twz);
-  V2* out = Zb + (colbase + ix0) * nzd;
-  for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) out[idx] = res[pad32(idx)];
-}
 
 __device__ __forceinline__ void block_max_atomic(double v, double* target) {
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -226,6 +193,56 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
 }
 constexpr int kBulkWaitPolls = 1 << 22;  // each try_wait itself waits a while: seconds in all
 
+// z-inverse of u, v, w per (plane, column group).  The block's columns of V
+// are one contiguous run of complex doubles: one bulk copy brings them into
+// the scratch buffer (sized for the raw columns when T is 8 bytes), the
+// conversion pass places them with the 3/2 zero band in the padded layout.
+template <typename T>
+__global__ void __launch_bounds__(256) k_zinv(const double2* __restrict__ V, typename C2<T>::t* __restrict__ Zb,
+                                              const typename C2<T>::t* __restrict__ twz, Dims d, RadixDev rz,
+                                              int nb_cols, int plane0, int ix_lo, int ix_hi,
+                                              DevScalars* __restrict__ sc) {
+  using V2 = typename C2<T>::t;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) unsigned long long bar;
+  const int nzd = d.nzd, nz = d.nz, nxp = d.nx + 1, nzt = d.nzt;
+  V2* bufA = reinterpret_cast<V2*>(smem_raw);
+  V2* bufB = bufA + pad32_size(nb_cols * nzd);
+  const double2* raw = reinterpret_cast<const double2*>(bufB);
+  const int c = blockIdx.z;
+  const int plane = plane0 + blockIdx.y;
+  const int ix0 = ix_lo + blockIdx.x * nb_cols;
+  const int nb = min(nb_cols, ix_hi - ix0);
+  const size_t colbase = ((size_t)c * d.nplanes + plane) * nxp;
+  const unsigned bytes = (unsigned)((size_t)nb * nzt * sizeof(double2));
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  if (threadIdx.x == 0) bulk_copy_g2s(const_cast<double2*>(raw), V + (colbase + ix0) * nzt, bytes, &bar);
+  if (!mbar_wait(&bar, 0, kBulkWaitPolls)) {
+    if (threadIdx.x == 0) atomicOr(&sc->error, 2);
+    mbar_wait(&bar, 0, kBulkWaitPolls);  // the copy in flight, once more
+    return;
+  }
+  const FastDiv by_nzd(nzd);
+  for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) {
+    const int b = by_nzd.div(idx);
+    const int jz = idx - b * nzd;
+    V2 val = czero<V2>();
+    int izp = -1;
+    if (jz <= nz) izp = nz + jz;
+    else if (jz >= nzd - nz) izp = jz - nzd + nz;
+    if (izp >= 0) {
+      const double2 x = raw[b * nzt + izp];
+      val = mk<V2>(Num<T>::from_double(x.x), Num<T>::from_double(x.y));
+    }
+    bufA[pad32(idx)] = val;
+  }
+  __syncthreads();
+  V2* res = fft_block<+1>(bufA, bufB, nb, rz, twz);
+  V2* out = Zb + (colbase + ix0) * nzd;
+  for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) out[idx] = res[pad32(idx)];
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_zfwd(const typename C2<T>::t* __restrict__ Pb, typename C2<T>::t* __restrict__ VV,
                                               const typename C2<T>::t* __restrict__ twz, Dims d, RadixDev rz,
@@ -268,6 +285,10 @@ __global__ void __launch_bounds__(256) k_zfwd(const typename C2<T>::t* __restric
 }
 
 size_t conv_z_smem(int zcols, int nzd, size_t ts) { return 2 * (size_t)pad32_size(zcols * nzd) * ts; }
+size_t conv_zinv_smem(int zcols, int nzd, int nzt, size_t ts) {
+  const size_t buf = (size_t)pad32_size(zcols * nzd) * ts;
+  return buf + std::max(buf, (size_t)zcols * nzt * sizeof(double2));
+}
 size_t conv_x_smem(int xrows, int nxd, size_t ts) { return 3 * (size_t)pad32_size(3 * xrows * nxd) * ts; }
 
 template <typename T>
@@ -278,9 +299,9 @@ void launch_convolutions(const ConvLaunch& L, cudaStream_t s, int stage) {
   if (stage == 0) {
     const int ncol = L.ix_hi - L.ix_lo;
     dim3 grid((ncol + L.zcols - 1) / L.zcols, L.nplanes, 3);
-    size_t sm = conv_z_smem(L.zcols, d.nzd, sizeof(V2));
+    size_t sm = conv_zinv_smem(L.zcols, d.nzd, d.nzt, sizeof(V2));
     k_zinv<T><<<grid, L.zthreads, sm, s>>>(L.V, (V2*)L.Zb, (const V2*)L.twz, d, L.rz, L.zcols, L.plane0, L.ix_lo,
-                                           L.ix_hi);
+                                           L.ix_hi, L.sc);
   }
   if (stage == 1) {
     dim3 grid(d.nzd / L.xrows, L.nplanes);

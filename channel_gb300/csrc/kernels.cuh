@@ -53,7 +53,8 @@ struct ConvLaunch {
 template <typename T> void launch_convolutions(const ConvLaunch& L, cudaStream_t s, int stage);
 cudaError_t conv_set_smem_limits();
 // dynamic shared memory of the z-transform and x-row kernels (padded buffers)
-size_t conv_z_smem(int zcols, int nzd, size_t ts);
+size_t conv_z_smem(int zcols, int nzd, size_t ts);                     // z-forward
+size_t conv_zinv_smem(int zcols, int nzd, int nzt, size_t ts);         // z-inverse (raw field copy)
 size_t conv_x_smem(int xrows, int nxd, size_t ts);
 
 struct SolveLaunch {
