@@ -24,6 +24,7 @@
 #include "chgpu_internal.h"
 #include "cplx.cuh"
 #include "kernels.cuh"
+#include "async.cuh"
 
 namespace chgpu {
 
@@ -157,41 +158,6 @@ __global__ void __launch_bounds__(256, MINB) k_xrow(const typename C2<T>::t* __r
   }
 }
 
-// ---------------------------------------------------------------------------
-// bulk asynchronous copy global -> shared through the TMA unit, completed on
-// an mbarrier (cp.async.bulk with complete_tx); every wait is bounded
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ unsigned smem_addr(const void* p) {
-  return static_cast<unsigned>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
-      "l"(src), "r"(bytes), "r"(smem_addr(bar))
-      : "memory");
-}
-// true once phase `parity` of the barrier has completed; false after
-// `limit` polls
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, int limit) {
-  for (int i = 0; i < limit; ++i) {
-    unsigned done = 0;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-constexpr int kBulkWaitPolls = 1 << 22;  // each try_wait itself waits a while: seconds in all
 
 // z-inverse of u, v, w per (plane, column group).  The block's columns of V
 // are one contiguous run of complex doubles: one bulk copy brings them into

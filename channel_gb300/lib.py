@@ -60,6 +60,7 @@ EXPORT_PART = {"all": 0, "large": 1, "small": 2}
 
 _P = C.c_void_p
 _DP = C.POINTER(C.c_double)
+_FP = C.POINTER(C.c_float)
 SIGNATURES = {
     "chgpu_create": (C.c_int, [C.POINTER(Params), C.POINTER(C.c_void_p)]),
     "chgpu_destroy": (C.c_int, [_P]),
@@ -102,6 +103,19 @@ SIGNATURES = {
     "chgpu_snapshot_wait": (C.c_int, [_P, C.POINTER(_DP)]),
     "chgpu_linsolve_noalloc": (C.c_int, [C.POINTER(Params), C.c_double, C.c_void_p, _DP, C.c_void_p,
                                          C.c_char_p, C.c_size_t]),
+    # include/chgpu_closure.h
+    "chgpu_mlp_create": (C.c_int, [C.c_ulonglong, C.POINTER(C.c_void_p)]),
+    "chgpu_mlp_destroy": (C.c_int, [_P]),
+    "chgpu_mlp_last_error": (C.c_char_p, [_P]),
+    "chgpu_mlp_set_params": (C.c_int, [_P, _FP]),
+    "chgpu_mlp_get_params": (C.c_int, [_P, _FP]),
+    "chgpu_mlp_set_norm": (C.c_int, [_P, C.c_void_p]),
+    "chgpu_mlp_get_norm": (C.c_int, [_P, C.c_void_p]),
+    "chgpu_mlp_set_data": (C.c_int, [_P, _FP, _FP, C.c_longlong]),
+    "chgpu_mlp_data_size": (C.c_longlong, [_P]),
+    "chgpu_mlp_gradient": (C.c_int, [_P, C.c_longlong, C.c_longlong, _FP, _DP]),
+    "chgpu_mlp_train": (C.c_int, [_P, C.c_int, C.c_longlong, C.c_float, _DP]),
+    "chgpu_mlp_predict": (C.c_int, [_P, _FP, C.c_longlong, _FP]),
 }
 NKINDS = 6
 
