@@ -20,8 +20,10 @@
 #include <vector>
 
 #include "../../include/chgpu.h"
+#include "../../include/chgpu_closure.h"
 #include "chgpu_internal.h"
 #include "kernels.cuh"
+#include "mlp.cuh"
 
 using namespace chgpu;
 
@@ -101,6 +103,20 @@ struct chgpu_handle {
   size_t ex_out_cap = 0;  // doubles
   int ex_chunk = 0, ex_zcols = 0, ex_xpairs = 0;
   RadixDev ex_rz{}, ex_rx{};
+  // learned closure: gradient spectra [9][plane][mode], their z-inverse
+  // [9][plane][kx][z] and physical values [9][plane][z][x] (FP32, x pairs
+  // packed), the stresses [6][plane][z][x], wall distance per plane, FP32
+  // transform tables
+  chgpu_mlp* cl_mlp = nullptr;
+  bool cl_on = false;     // the network evaluates tau in every convolution pass
+  bool cl_fixed = false;  // a prescribed tau (chgpu_closure_set_tau)
+  double2* cl_G = nullptr;
+  float2* cl_Z = nullptr;
+  float2* cl_P = nullptr;
+  float2* cl_tau = nullptr;
+  float* cl_wd = nullptr;
+  void *cl_twz = nullptr, *cl_twx = nullptr, *cl_twh = nullptr;
+  int nsm = 0;
   // per-kernel timing
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -324,6 +340,18 @@ SolveLaunch solve_launch(chgpu_handle* h, const double* ode) {
   return L;
 }
 
+// the closure's stresses for the current field: velocity gradients ->
+// physical -> network -> tau at the points of the planes iy = 1..ny-1
+void enqueue_closure(chgpu_handle* h) {
+  const Dims& d = h->d;
+  launch_gradients(h->V, h->cl_G, h->der, h->d0lu, h->bc, d, h->stream);
+  launch_physical_fields(h->cl_G, 9, h->cl_Z, h->cl_P, (const float2*)h->cl_twz, (const float2*)h->cl_twx,
+                         (const float2*)h->cl_twh, d, h->rz, h->rx, h->zcols, h->xrows, h->sc, h->stream);
+  launch_mlp_closure(h->cl_mlp, reinterpret_cast<const float*>(h->cl_P), reinterpret_cast<float*>(h->cl_tau),
+                     h->cl_wd, (long long)d.nzd * 2 * d.nxd, d.nplanes, d.ny, &h->sc->error, 4, h->nsm, h->stream);
+  h->launches += 4;
+}
+
 void run_convolutions(chgpu_handle* h, int compute_cfl, int products, int plane0, int nplanes, int stage_lo = 0,
                       int stage_hi = 3, int ix_lo = 0, int ix_hi = -1) {
   ConvLaunch L = conv_launch(h, compute_cfl, products, plane0, nplanes);
@@ -331,6 +359,8 @@ void run_convolutions(chgpu_handle* h, int compute_cfl, int products, int plane0
     L.ix_lo = ix_lo;
     L.ix_hi = ix_hi;
   }
+  if (products && (h->cl_on || h->cl_fixed)) L.tau = h->cl_tau;
+  if (products && h->cl_on && stage_lo == 0) enqueue_closure(h);
   const int nst = products ? 3 : 2;
   for (int stage = stage_lo; stage < std::min(nst, stage_hi); ++stage) {
     timed(h, stage, [&] {
@@ -400,7 +430,7 @@ void run_outstats(chgpu_handle* h) {
 // both; so does the end of the step.  Nothing half B's kernels read is
 // written by half A's (the mean-mode scalars are read only for the mean mode).
 void enqueue_step(chgpu_handle* h) {
-  const bool split = h->halves == 2 && !h->profiling && h->d.nx >= 1;
+  const bool split = h->halves == 2 && !h->profiling && h->d.nx >= 1 && !h->cl_on && !h->cl_fixed;
   const int KA = (h->d.nx + 1 + 1) / 2, nxp = h->d.nx + 1;
   const int mA = KA * h->d.nzt, qA = KA * (h->d.nz + 1);
   for (int k = 0; k < 3; ++k) {
@@ -452,6 +482,7 @@ int pull_scalars(chgpu_handle* h) {
   CK(h, cudaMemcpyAsync(h->sc_host, h->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->stream));
   CK(h, cudaStreamSynchronize(h->stream));
   if (h->sc_host->error & 2) return fail(h, CHGPU_E_CUDA, "a bulk copy into shared memory did not complete in time");
+  if (h->sc_host->error & 4) return fail(h, CHGPU_E_CUDA, "a tensor-core completion wait of the closure ran out");
   if (h->sc_host->error & 1) return fail(h, CHGPU_E_NONFINITE, "non-finite CFL or statistics (flow field blew up)");
   return 0;
 }
@@ -464,7 +495,8 @@ void release(chgpu_handle* h) {
   }
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   void* bufs[] = {h->V, h->F, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->derT, h->derL, h->cst, h->d0lu, h->nud, h->lindd, h->yint, h->dy,
-                  h->twz, h->twx, h->twh, h->sc, h->ex_W, h->ex_P, h->ex_out, h->ex_twz, h->ex_twx};
+                  h->twz, h->twx, h->twh, h->sc, h->ex_W, h->ex_P, h->ex_out, h->ex_twz, h->ex_twx,
+                  h->cl_G, h->cl_Z, h->cl_P, h->cl_tau, h->cl_wd, h->cl_twz, h->cl_twx, h->cl_twh};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (h->sc_host) cudaFreeHost(h->sc_host);
@@ -1369,5 +1401,181 @@ int chgpu_snapshot_wait(chgpu_handle* h, const double** V) {
 void* chgpu_stream(chgpu_handle* h) { return h ? (void*)h->stream : nullptr; }
 
 long long chgpu_launch_count(const chgpu_handle* h) { return h ? h->launches : 0; }
+
+// ---------------------------------------------------------------------------
+// learned closure (include/chgpu_closure.h)
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+long long closure_plane_pts(const chgpu_handle* h) { return (long long)h->d.nzd * 2 * h->d.nxd; }
+
+void drop_graph(chgpu_handle* h) {  // the captured step holds the old launch sequence
+  if (h->graph) {
+    cudaStreamSynchronize(h->stream);
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  ++h->version;
+}
+
+// buffers and FP32 tables of the closure, on first use
+int closure_alloc(chgpu_handle* h) {
+  if (h->cl_G) return 0;
+  const Dims& d = h->d;
+  const size_t np = d.nplanes, nm = d.nmodes, nxp = d.nx + 1;
+  const size_t phys = (size_t)9 * np * d.nzd * d.nxd * sizeof(float2);
+  // cl_P also stages host spectra (up to 9 fields, complex128) for chgpu_closure_physical
+  const size_t stage = (size_t)9 * np * nm * sizeof(double2);
+  int dev = 0;
+  CK(h, cudaGetDevice(&dev));
+  CK(h, cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, dev));
+  if (mlp_set_smem_limits() != 0) return fail(h, CHGPU_E_CUDA, "closure: shared-memory limit refused");
+  auto alloc = [&](void** ptr, size_t bytes) -> int {
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    return e == cudaSuccess ? 0 : fail(h, CHGPU_E_NOMEM, "closure: device allocation failed");
+  };
+  if (int rc = alloc((void**)&h->cl_G, (size_t)9 * np * nm * sizeof(double2))) return rc;
+  if (int rc = alloc((void**)&h->cl_Z, (size_t)9 * np * nxp * d.nzd * sizeof(float2))) return rc;
+  if (int rc = alloc((void**)&h->cl_P, std::max(phys, stage))) return rc;
+  if (int rc = alloc((void**)&h->cl_tau, (size_t)6 * np * d.nzd * d.nxd * sizeof(float2))) return rc;
+  if (int rc = alloc((void**)&h->cl_wd, np * sizeof(float))) return rc;
+  CK(h, cudaMemset(h->cl_tau, 0, (size_t)6 * np * d.nzd * d.nxd * sizeof(float2)));
+  std::vector<float> wd(np);
+  for (size_t k = 0; k < np; ++k) {
+    const double y = h->tab.y[k];
+    wd[k] = (float)std::min(y - h->p.ymin, h->p.ymax - y);
+  }
+  CK(h, cudaMemcpy(h->cl_wd, wd.data(), np * sizeof(float), cudaMemcpyHostToDevice));
+  if (int rc = upload_stage_twiddles<float2>(h, &h->cl_twz, h->rz)) return rc;
+  if (int rc = upload_stage_twiddles<float2>(h, &h->cl_twx, h->rx)) return rc;
+  return upload_pack_roots<float2>(h, &h->cl_twh, 2 * d.nxd, 1.0L);
+}
+
+// interior planes (iy = 1..ny-1) of ncomp physical fields in cl_P -> out[ncomp][npts]
+int copy_closure_points(chgpu_handle* h, int ncomp, float* out) {
+  const long long pp = closure_plane_pts(h), n = (long long)(h->d.ny - 1) * pp;
+  const float* P = reinterpret_cast<const float*>(h->cl_P);
+  for (int c = 0; c < ncomp; ++c)
+    CK(h, cudaMemcpyAsync(out + (size_t)c * n, P + ((size_t)c * h->d.nplanes + 2) * pp, sizeof(float) * n,
+                          cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+template <typename V2>
+__global__ void k_to_double2(const V2* __restrict__ in, double2* __restrict__ out, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = make_double2((double)in[i].x, (double)in[i].y);
+}
+
+}  // namespace
+
+extern "C" {
+
+int chgpu_closure_dims(chgpu_handle* h, int dims[3]) {
+  if (!h || !dims) return fail(h, CHGPU_E_PARAM, "chgpu_closure_dims: null argument");
+  dims[0] = 2 * h->d.nxd;
+  dims[1] = h->d.nzd;
+  dims[2] = h->d.ny - 1;
+  return 0;
+}
+
+int chgpu_closure_attach(chgpu_handle* h, chgpu_mlp* m, int enable) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "chgpu_closure_attach: null handle");
+  if (enable && !m) return fail(h, CHGPU_E_PARAM, "chgpu_closure_attach: enable needs a network");
+  if (int rc = closure_alloc(h)) return rc;
+  h->cl_mlp = m;
+  const bool on = enable && m;
+  if (on != h->cl_on) {
+    h->cl_on = on;
+    drop_graph(h);
+  }
+  return 0;
+}
+
+int chgpu_closure_set_tau(chgpu_handle* h, const float* tau) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "chgpu_closure_set_tau: null handle");
+  if (int rc = closure_alloc(h)) return rc;
+  const long long pp = closure_plane_pts(h), n = (long long)(h->d.ny - 1) * pp;
+  float* T = reinterpret_cast<float*>(h->cl_tau);
+  CK(h, cudaStreamSynchronize(h->stream));
+  CK(h, cudaMemset(T, 0, sizeof(float) * 6 * h->d.nplanes * pp));
+  if (tau)
+    for (int o = 0; o < 6; ++o)
+      CK(h, cudaMemcpy(T + ((size_t)o * h->d.nplanes + 2) * pp, tau + (size_t)o * n, sizeof(float) * n,
+                       cudaMemcpyHostToDevice));
+  const bool fixed = tau != nullptr;
+  if (fixed != h->cl_fixed) {
+    h->cl_fixed = fixed;
+    drop_graph(h);
+  }
+  return 0;
+}
+
+int chgpu_closure_features(chgpu_handle* h, float* feat) {
+  if (!h || !feat) return fail(h, CHGPU_E_PARAM, "chgpu_closure_features: null argument");
+  if (!h->field_set) return fail(h, CHGPU_E_STATE, "chgpu_closure_features: upload the field first");
+  if (int rc = closure_alloc(h)) return rc;
+  const Dims& d = h->d;
+  launch_gradients(h->V, h->cl_G, h->der, h->d0lu, h->bc, d, h->stream);
+  launch_physical_fields(h->cl_G, 9, h->cl_Z, h->cl_P, (const float2*)h->cl_twz, (const float2*)h->cl_twx,
+                         (const float2*)h->cl_twh, d, h->rz, h->rx, h->zcols, h->xrows, h->sc, h->stream);
+  h->launches += 3;
+  CK(h, cudaGetLastError());
+  if (int rc = copy_closure_points(h, 9, feat)) return rc;
+  if (int rc = pull_scalars(h)) return rc;
+  const long long pp = closure_plane_pts(h), n = (long long)(d.ny - 1) * pp;
+  float* w = feat + (size_t)9 * n;
+  for (int iy = 1; iy <= d.ny - 1; ++iy) {
+    const double y = h->tab.y[iy + 1];
+    const float v = (float)std::min(y - h->p.ymin, h->p.ymax - y);
+    std::fill(w + (size_t)(iy - 1) * pp, w + (size_t)iy * pp, v);
+  }
+  return 0;
+}
+
+int chgpu_closure_physical(chgpu_handle* h, const double* spec, int ncomp, float* out) {
+  if (!h || !spec || !out) return fail(h, CHGPU_E_PARAM, "chgpu_closure_physical: null argument");
+  if (ncomp != 3 && ncomp != 6 && ncomp != 9) return fail(h, CHGPU_E_PARAM, "chgpu_closure_physical: ncomp must be 3, 6 or 9");
+  if (int rc = closure_alloc(h)) return rc;
+  const Dims& d = h->d;
+  const size_t n = (size_t)ncomp * d.nplanes * d.nmodes;
+  double2* stage = reinterpret_cast<double2*>(h->cl_P);
+  CK(h, cudaMemcpyAsync(stage, spec, sizeof(double2) * n, cudaMemcpyHostToDevice, h->stream));
+  launch_transpose(stage, h->cl_G, d.nmodes, d.nplanes, ncomp, h->stream);
+  launch_physical_fields(h->cl_G, ncomp, h->cl_Z, h->cl_P, (const float2*)h->cl_twz, (const float2*)h->cl_twx,
+                         (const float2*)h->cl_twh, d, h->rz, h->rx, h->zcols, h->xrows, h->sc, h->stream);
+  h->launches += 3;
+  CK(h, cudaGetLastError());
+  if (int rc = copy_closure_points(h, ncomp, out)) return rc;
+  return pull_scalars(h);
+}
+
+int chgpu_products(chgpu_handle* h, double* out) {
+  if (!h || !out) return fail(h, CHGPU_E_PARAM, "chgpu_products: null argument");
+  if (!h->field_set) return fail(h, CHGPU_E_STATE, "chgpu_products: upload the field first");
+  if (int rc = closure_alloc(h)) return rc;
+  const Dims& d = h->d;
+  const bool on = h->cl_on, fixed = h->cl_fixed;
+  h->cl_on = h->cl_fixed = false;  // the resolved products alone
+  run_convolutions(h, 0, 1, 0, d.nplanes);
+  h->cl_on = on;
+  h->cl_fixed = fixed;
+  const size_t n = (size_t)6 * d.nplanes * d.nmodes;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  if (h->prec == CHGPU_MIXED) k_to_double2<float2><<<blocks, 256, 0, h->stream>>>((const float2*)h->VV, h->cl_G, n);
+  else if (h->prec == CHGPU_FP64DD)
+    k_to_double2<cdd><<<blocks, 256, 0, h->stream>>>((const cdd*)h->VV, h->cl_G, n);
+  else CK(h, cudaMemcpyAsync(h->cl_G, h->VV, sizeof(double2) * n, cudaMemcpyDeviceToDevice, h->stream));
+  double2* stage = reinterpret_cast<double2*>(h->cl_P);
+  launch_transpose(h->cl_G, stage, d.nplanes, d.nmodes, 6, h->stream);
+  h->launches += 2;
+  CK(h, cudaGetLastError());
+  CK(h, cudaMemcpyAsync(out, stage, sizeof(double2) * n, cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return pull_scalars(h);
+}
 
 }  // extern "C"

@@ -67,7 +67,8 @@ struct DevScalars {
   double line[11];
   double runtime_global;
   long long istep;
-  int error;  // bit 0: non-finite CFL or statistics; bit 1: a bulk-copy wait ran out
+  int error;  // bit 0: non-finite CFL or statistics; bit 1: a bulk-copy wait ran out;
+              // bit 2: a tensor-core completion wait of the closure ran out
   int pad;
 };
 

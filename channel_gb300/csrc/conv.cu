@@ -42,14 +42,22 @@ __device__ __forceinline__ void block_max_atomic(double v, double* target) {
   }
 }
 
+// an FP32 pair of the closure's stresses in the transform type
+template <typename V2> __device__ __forceinline__ V2 tau2(float2 t);
+template <> __device__ __forceinline__ double2 tau2<double2>(float2 t) { return make_double2(t.x, t.y); }
+template <> __device__ __forceinline__ float2 tau2<float2>(float2 t) { return t; }
+template <> __device__ __forceinline__ cdd tau2<cdd>(float2 t) { return cdd{dd(t.x), dd(t.y)}; }
+
 // MINB: resident 256-thread blocks per SM the register allocation is capped
 // for (the autotuner picks the variant and the rows per block together)
-template <typename T, int MINB>
+// TAU: the closure's subgrid stresses tau[p][plane][jz][x] (FP32, physical,
+// x pairs packed like the transform) are added to the six products.
+template <typename T, int MINB, bool TAU = false>
 __global__ void __launch_bounds__(256, MINB) k_xrow(const typename C2<T>::t* __restrict__ Zb, typename C2<T>::t* __restrict__ Pb,
                                               const typename C2<T>::t* __restrict__ twx,
                                               const typename C2<T>::t* __restrict__ twh, const T* __restrict__ cst,
                                               Dims d, RadixDev rx, int nrows, int plane0, int compute_cfl,
-                                              DevScalars* sc) {
+                                              DevScalars* sc, const float2* __restrict__ tau) {
   using V2 = typename C2<T>::t;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int M = d.nxd, nx = d.nx, nxp = nx + 1, nzd = d.nzd;
@@ -106,9 +114,16 @@ __global__ void __launch_bounds__(256, MINB) k_xrow(const typename C2<T>::t* __r
       cfl = N::max(cfl, N::max(c0, c1));
       bad = bad || !N::finite(c0) || !N::finite(c1);
     }
-    Cb[pad32((0 * nrows + r) * M + m)] = mk<V2>(u.x * u.x, u.y * u.y);
-    Cb[pad32((1 * nrows + r) * M + m)] = mk<V2>(v.x * v.x, v.y * v.y);
-    Cb[pad32((2 * nrows + r) * M + m)] = mk<V2>(w.x * w.x, w.y * w.y);
+    V2 puu = mk<V2>(u.x * u.x, u.y * u.y), pvv = mk<V2>(v.x * v.x, v.y * v.y), pww = mk<V2>(w.x * w.x, w.y * w.y);
+    if constexpr (TAU) {
+      const size_t tb = ((size_t)plane * nzd + jz0 + r) * M + m, ts = (size_t)d.nplanes * nzd * M;
+      puu = puu + tau2<V2>(tau[tb]);
+      pvv = pvv + tau2<V2>(tau[tb + ts]);
+      pww = pww + tau2<V2>(tau[tb + 2 * ts]);
+    }
+    Cb[pad32((0 * nrows + r) * M + m)] = puu;
+    Cb[pad32((1 * nrows + r) * M + m)] = pvv;
+    Cb[pad32((2 * nrows + r) * M + m)] = pww;
   }
   if (bad) cfl = T((float)INFINITY);  // a non-finite velocity shows up as an infinite CFL
   if (compute_cfl) block_max_atomic(Num<T>::to_double(cfl), &sc->cfl);
@@ -120,9 +135,16 @@ __global__ void __launch_bounds__(256, MINB) k_xrow(const typename C2<T>::t* __r
         V2 u = U[pad32((0 * nrows + r) * M + m)];
         V2 v = U[pad32((1 * nrows + r) * M + m)];
         V2 w = U[pad32((2 * nrows + r) * M + m)];
-        Cb[pad32((0 * nrows + r) * M + m)] = mk<V2>(u.x * v.x, u.y * v.y);
-        Cb[pad32((1 * nrows + r) * M + m)] = mk<V2>(v.x * w.x, v.y * w.y);
-        Cb[pad32((2 * nrows + r) * M + m)] = mk<V2>(u.x * w.x, u.y * w.y);
+        V2 puv = mk<V2>(u.x * v.x, u.y * v.y), pvw = mk<V2>(v.x * w.x, v.y * w.y), puw = mk<V2>(u.x * w.x, u.y * w.y);
+        if constexpr (TAU) {
+          const size_t tb = ((size_t)plane * nzd + jz0 + r) * M + m, ts = (size_t)d.nplanes * nzd * M;
+          puv = puv + tau2<V2>(tau[tb + 3 * ts]);
+          pvw = pvw + tau2<V2>(tau[tb + 4 * ts]);
+          puw = puw + tau2<V2>(tau[tb + 5 * ts]);
+        }
+        Cb[pad32((0 * nrows + r) * M + m)] = puv;
+        Cb[pad32((1 * nrows + r) * M + m)] = pvw;
+        Cb[pad32((2 * nrows + r) * M + m)] = puw;
       }
       __syncthreads();
     }
@@ -158,6 +180,56 @@ __global__ void __launch_bounds__(256, MINB) k_xrow(const typename C2<T>::t* __r
   }
 }
 
+
+// x-inverse alone: the physical rows of ncomp fields after their z-inverse
+// (the c2r of k_xrow), for the closure's velocity gradients.  Blocks:
+// (groups of nrows z rows, planes, groups of 3 fields).  Writes
+// out[c][plane][jz][m], the pairs x = 2m, 2m+1 packed as in the transform.
+template <typename T>
+__global__ void __launch_bounds__(256) k_xphys(const typename C2<T>::t* __restrict__ Zb, typename C2<T>::t* __restrict__ out,
+                                               const typename C2<T>::t* __restrict__ twx,
+                                               const typename C2<T>::t* __restrict__ twh, Dims d, RadixDev rx,
+                                               int nrows, int plane0) {
+  using V2 = typename C2<T>::t;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int M = d.nxd, nx = d.nx, nxp = nx + 1, nzd = d.nzd;
+  const int plane = plane0 + blockIdx.y;
+  const int jz0 = blockIdx.x * nrows;
+  const int c0 = 3 * blockIdx.z;
+  const int S = 3 * nrows * M;
+  const int lgr = __ffs(nrows) - 1;
+  const FastDiv by_M(M);
+  V2* A = reinterpret_cast<V2*>(smem_raw);
+  V2* B = A + pad32_size(S);
+  V2* Cb = B + pad32_size(S);
+  for (int idx = threadIdx.x; idx < S; idx += blockDim.x) {
+    const int r = idx & (nrows - 1);
+    const int ck = idx >> lgr;
+    const int c = by_M.div(ck);
+    const int k = ck - c * M;
+    V2 val = czero<V2>();
+    if (k <= nx) val = Zb[(((size_t)(c0 + c) * d.nplanes + plane) * nxp + k) * nzd + jz0 + r];
+    Cb[pad32((c * nrows + r) * M + k)] = val;
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < S; idx += blockDim.x) {
+    const int cr = by_M.div(idx);
+    const int k = idx - cr * M;
+    V2 xk = Cb[pad32(cr * M + k)];
+    V2 xm = czero<V2>();
+    if (k == 0) xk.y = T();
+    else xm = conjg(Cb[pad32(cr * M + M - k)]);
+    V2 e = xk + xm, o = cmul_s<+1>(xk - xm, twh[k]);
+    A[pad32(idx)] = e + mul_is<+1>(o);
+  }
+  __syncthreads();
+  V2* U = fft_block<+1, V2, true>(A, B, 3 * nrows, rx, twx);
+  for (int idx = threadIdx.x; idx < S; idx += blockDim.x) {
+    const int cr = by_M.div(idx), m = idx - cr * M;
+    const int c = cr >> lgr, r = cr & (nrows - 1);
+    out[(((size_t)(c0 + c) * d.nplanes + plane) * nzd + jz0 + r) * M + m] = U[pad32(idx)];
+  }
+}
 
 // z-inverse of u, v, w per (plane, column group).  The block's columns of V
 // are one contiguous run of complex doubles: one bulk copy brings them into
@@ -272,9 +344,9 @@ void launch_convolutions(const ConvLaunch& L, cudaStream_t s, int stage) {
   if (stage == 1) {
     dim3 grid(d.nzd / L.xrows, L.nplanes);
     size_t sm = conv_x_smem(L.xrows, d.nxd, sizeof(V2));
-    auto kern = L.xminb == 1 ? k_xrow<T, 1> : L.xminb == 3 ? k_xrow<T, 3> : k_xrow<T, 2>;
+    auto kern = L.tau ? k_xrow<T, 2, true> : L.xminb == 1 ? k_xrow<T, 1> : L.xminb == 3 ? k_xrow<T, 3> : k_xrow<T, 2>;
     kern<<<grid, L.xthreads, sm, s>>>((const V2*)L.Zb, (V2*)L.Pb, (const V2*)L.twx, (const V2*)L.twh, (const T*)L.cst, d, L.rx,
-                               L.xrows, L.plane0, L.compute_cfl, L.sc);
+                               L.xrows, L.plane0, L.compute_cfl, L.sc, L.tau);
   }
   if (stage == 2) {
     dim3 grid((nxp + L.zcols - 1) / L.zcols, L.nplanes, 6);
@@ -282,6 +354,19 @@ void launch_convolutions(const ConvLaunch& L, cudaStream_t s, int stage) {
     k_zfwd<T><<<grid, L.zthreads, sm, s>>>((const V2*)L.Pb, (V2*)L.VV, (const V2*)L.twz, d, L.rz, L.zcols, L.plane0,
                                            L.sc);
   }
+}
+
+// z-inverse and x-inverse of ncomp (a multiple of 3) fields in the field
+// layout, FP32, all planes: src [c][plane][mode] -> zb -> out [c][plane][jz][m]
+void launch_physical_fields(const double2* src, int ncomp, float2* zb, float2* out, const float2* twz,
+                            const float2* twx, const float2* twh, const Dims& d, const RadixDev& rz,
+                            const RadixDev& rx, int zcols, int xrows, DevScalars* sc, cudaStream_t s) {
+  const int nxp = d.nx + 1;
+  dim3 gz((nxp + zcols - 1) / zcols, d.nplanes, ncomp);
+  k_zinv<float><<<gz, 256, conv_zinv_smem(zcols, d.nzd, d.nzt, sizeof(float2)), s>>>(src, zb, twz, d, rz, zcols, 0, 0,
+                                                                                      nxp, sc);
+  dim3 gx(d.nzd / xrows, d.nplanes, ncomp / 3);
+  k_xphys<float><<<gx, 256, conv_x_smem(xrows, d.nxd, sizeof(float2)), s>>>(zb, out, twx, twh, d, rx, xrows, 0);
 }
 
 template void launch_convolutions<double>(const ConvLaunch&, cudaStream_t, int);
@@ -318,6 +403,11 @@ cudaError_t conv_set_smem_limits() {
   if ((e = allow_max_smem(k_xrow<float, 3>, optin))) return e;
   if ((e = allow_max_smem(k_xrow<dd, 1>, optin))) return e;
   if ((e = allow_max_smem(k_xrow<dd, 2>, optin))) return e;
+  if ((e = allow_max_smem(k_xrow<dd, 3>, optin))) return e;
+  if ((e = allow_max_smem(k_xrow<double, 2, true>, optin))) return e;
+  if ((e = allow_max_smem(k_xrow<float, 2, true>, optin))) return e;
+  if ((e = allow_max_smem(k_xrow<dd, 2, true>, optin))) return e;
+  if ((e = allow_max_smem(k_xphys<float>, optin))) return e;
   return allow_max_smem(k_xrow<dd, 3>, optin);
 }
 

@@ -47,6 +47,7 @@ struct ConvLaunch {
   int plane0, nplanes;
   int compute_cfl;
   int products;  // 0: stop after the x pass (the start-up CFL pass)
+  const float2* tau;  // closure stresses added to the products, or null
 };
 
 // stage 0: z-inverse, 1: x rows, 2: z-forward
@@ -56,6 +57,12 @@ cudaError_t conv_set_smem_limits();
 size_t conv_z_smem(int zcols, int nzd, size_t ts);                     // z-forward
 size_t conv_zinv_smem(int zcols, int nzd, int nzt, size_t ts);         // z-inverse (raw field copy)
 size_t conv_x_smem(int xrows, int nxd, size_t ts);
+void launch_physical_fields(const double2* src, int ncomp, float2* zb, float2* out, const float2* twz,
+                            const float2* twx, const float2* twh, const Dims& d, const RadixDev& rz,
+                            const RadixDev& rx, int zcols, int xrows, DevScalars* sc, cudaStream_t s);
+// the closure's velocity gradients: G[3c + {0,1,2}] = d/dx, d/dy, d/dz of V[c]
+void launch_gradients(const double2* V, double2* G, const double* der, const double* d0lu, const BcRows& bc,
+                      const Dims& d, cudaStream_t s);
 
 struct SolveLaunch {
   Dims d;

@@ -389,13 +389,41 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train(const unsigned char* __res
 // ---------------------------------------------------------------------------
 // inference
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_mlp_infer(const unsigned char* __restrict__ packed,
-                                                   const float* __restrict__ feat, long long n, Norm nm,
-                                                   float* __restrict__ out, int* __restrict__ err) {
+// point sources and sinks: structure-of-arrays feat[10][n] -> out[6][n] ...
+struct SoaIO {
+  const float* feat;
+  float* out;
+  long long n;
+  __device__ long long count() const { return n; }
+  __device__ void load(long long idx, const Norm& nm, float (&f)[NIN]) const { load_features(feat, n, idx, nm, f); }
+  __device__ void store(long long idx, int o, float v) const { out[(long long)o * n + idx] = v; }
+};
+// ... or the closure points of a channel handle: the planes iy = 1..ny-1 of
+// the physical gradient fields phys[9][plane][z][x] and the wall distance of
+// each plane -> tau[6][plane][z][x] (the interior planes are contiguous)
+struct PlaneIO {
+  const float* phys;
+  float* tau;
+  const float* wd;
+  long long plane_pts, comp_stride, n;
+  __device__ long long count() const { return n; }
+  __device__ void load(long long idx, const Norm& nm, float (&f)[NIN]) const {
+    const long long off = idx + 2 * plane_pts;
+#pragma unroll
+    for (int k = 0; k < NIN - 1; ++k) f[k] = (phys[k * comp_stride + off] - nm.mu_in[k]) * nm.isd_in[k];
+    f[NIN - 1] = (wd[off / plane_pts] - nm.mu_in[NIN - 1]) * nm.isd_in[NIN - 1];
+  }
+  __device__ void store(long long idx, int o, float v) const { tau[o * comp_stride + idx + 2 * plane_pts] = v; }
+};
+
+template <typename IO>
+__global__ void __launch_bounds__(128) k_mlp_infer(const unsigned char* __restrict__ packed, IO io,
+                                                   const Norm* __restrict__ nmp, int* __restrict__ err, int errbit) {
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ __align__(8) unsigned long long bar;
   __shared__ unsigned tbase_s;
   const int p = threadIdx.x, warp = p >> 5;
+  const Norm nm = *nmp;
   if (p == 0) mbar_init(&bar, 1);
   if (warp == 0) tm_alloc(&tbase_s, kInferCols);
   tm_fence_before();
@@ -410,11 +438,12 @@ __global__ void __launch_bounds__(128) k_mlp_infer(const unsigned char* __restri
   const float* bias = reinterpret_cast<const float*>(sm + P_BIAS);
   unsigned char *X = sm + S_X, *PA = sm + S_PA, *PB = sm + S_PB;
   constexpr unsigned i64 = idesc_bf16(128, 64), i16 = idesc_bf16(128, 16);
+  const long long n = io.count();
   const long long tiles = (n + 127) / 128;
   for (long long t = blockIdx.x; ok && t < tiles; t += gridDim.x) {
     const long long idx = t * 128 + p;
     float f[NIN];
-    if (idx < n) load_features(feat, n, idx, nm, f);
+    if (idx < n) io.load(idx, nm, f);
     else
       for (int k = 0; k < NIN; ++k) f[k] = 0.0f;
     write_input_row(X, nullptr, p, f);
@@ -432,10 +461,10 @@ __global__ void __launch_bounds__(128) k_mlp_infer(const unsigned char* __restri
     float v[16];
     tm_ld16(tl + I_Y, v);
     if (idx < n)
-      for (int o = 0; o < NOUT; ++o) out[(long long)o * n + idx] = (v[o] + bias[128 + o]) * nm.sd_out[o] + nm.mu_out[o];
+      for (int o = 0; o < NOUT; ++o) io.store(idx, o, (v[o] + bias[128 + o]) * nm.sd_out[o] + nm.mu_out[o]);
   }
   if (!ok) {
-    if (p == 0) atomicOr(err, 1);
+    if (p == 0) atomicOr(err, errbit);
     mbar_wait(&bar, phase ^ 1u, kBulkWaitPolls);
   }
   tm_fence_before();
@@ -461,14 +490,36 @@ __global__ void k_adam(float* __restrict__ theta, float* __restrict__ g, float* 
 
 }  // namespace mlp
 
+}  // namespace chgpu
+
+struct chgpu_mlp {
+  float *theta = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr;
+  unsigned char* packed = nullptr;
+  float *feat = nullptr, *targ = nullptr;
+  long long n = 0, cursor = 0;
+  double* loss = nullptr;  // per-step losses of the current train call
+  int loss_cap = 0;
+  int* err = nullptr;
+  int adam_t = 0, nsm = 0;
+  chgpu_mlp_norm user{};
+  chgpu::mlp::Norm nm{};
+  chgpu::mlp::Norm* nm_dev = nullptr;  // the same on the device (read by captured closure launches)
+  cudaStream_t stream = nullptr;
+  std::string msg;
+};
+
+namespace chgpu {
+
 // ---------------------------------------------------------------------------
 // launches (also used by the closure inside the coarse solver)
 // ---------------------------------------------------------------------------
 int mlp_set_smem_limits() {
   if (cudaFuncSetAttribute(mlp::k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::S_END) != cudaSuccess)
     return -1;
-  if (cudaFuncSetAttribute(mlp::k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::S_INFER_END) !=
-      cudaSuccess)
+  if (cudaFuncSetAttribute(mlp::k_mlp_infer<mlp::SoaIO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           mlp::S_INFER_END) != cudaSuccess ||
+      cudaFuncSetAttribute(mlp::k_mlp_infer<mlp::PlaneIO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           mlp::S_INFER_END) != cudaSuccess)
     return -1;
   return 0;
 }
@@ -481,11 +532,19 @@ void launch_mlp_train(const unsigned char* packed, const float* feat, const floa
   const int grid = tiles < nsm ? tiles : nsm;
   mlp::k_mlp_train<<<grid, 128, mlp::S_END, s>>>(packed, feat, targ, n, first, tiles, nm, gscale, grad, loss, err);
 }
-void launch_mlp_infer(const unsigned char* packed, const float* feat, long long n, const mlp::Norm& nm, float* out,
+void launch_mlp_infer(const unsigned char* packed, const float* feat, long long n, const mlp::Norm* nm, float* out,
                       int* err, int nsm, cudaStream_t s) {
   const long long tiles = (n + 127) / 128;
   const int grid = (int)(tiles < 2LL * nsm ? tiles : 2LL * nsm);
-  if (grid > 0) mlp::k_mlp_infer<<<grid, 128, mlp::S_INFER_END, s>>>(packed, feat, n, nm, out, err);
+  if (grid > 0) mlp::k_mlp_infer<<<grid, 128, mlp::S_INFER_END, s>>>(packed, mlp::SoaIO{feat, out, n}, nm, err, 1);
+}
+void launch_mlp_closure(const chgpu_mlp* m, const float* phys, float* tau, const float* wd, long long plane_pts,
+                        int nplanes, int ny, int* err, int errbit, int nsm, cudaStream_t s) {
+  const long long n = (long long)(ny - 1) * plane_pts;
+  const long long tiles = (n + 127) / 128;
+  const int grid = (int)(tiles < 2LL * nsm ? tiles : 2LL * nsm);
+  mlp::PlaneIO io{phys, tau, wd, plane_pts, (long long)nplanes * plane_pts, n};
+  if (grid > 0) mlp::k_mlp_infer<<<grid, 128, mlp::S_INFER_END, s>>>(m->packed, io, m->nm_dev, err, errbit);
 }
 void launch_adam(float* theta, float* g, float* m1, float* m2, int n, float lr, int t, cudaStream_t s) {
   const float b1 = 0.9f, b2 = 0.999f;
@@ -499,21 +558,6 @@ void launch_adam(float* theta, float* g, float* m1, float* m2, int n, float lr, 
 // C ABI
 // ---------------------------------------------------------------------------
 using namespace chgpu;
-
-struct chgpu_mlp {
-  float *theta = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr;
-  unsigned char* packed = nullptr;
-  float *feat = nullptr, *targ = nullptr;
-  long long n = 0, cursor = 0;
-  double* loss = nullptr;  // per-step losses of the current train call
-  int loss_cap = 0;
-  int* err = nullptr;
-  int adam_t = 0, nsm = 0;
-  chgpu_mlp_norm user{};
-  mlp::Norm nm{};
-  cudaStream_t stream = nullptr;
-  std::string msg;
-};
 
 namespace {
 
@@ -591,7 +635,8 @@ int chgpu_mlp_create(unsigned long long seed, chgpu_mlp** out) {
   if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaMalloc(&m->theta, pb) != cudaSuccess || cudaMalloc(&m->grad, pb) != cudaSuccess ||
       cudaMalloc(&m->m1, pb) != cudaSuccess || cudaMalloc(&m->m2, pb) != cudaSuccess ||
-      cudaMalloc(&m->packed, mlp::PACKED_BYTES) != cudaSuccess || cudaMalloc(&m->err, sizeof(int)) != cudaSuccess) {
+      cudaMalloc(&m->packed, mlp::PACKED_BYTES) != cudaSuccess || cudaMalloc(&m->err, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&m->nm_dev, sizeof(mlp::Norm)) != cudaSuccess) {
     chgpu_mlp_destroy(m);
     return mfail(nullptr, CHGPU_E_NOMEM, "chgpu_mlp_create: device allocation failed");
   }
@@ -615,6 +660,7 @@ int chgpu_mlp_create(unsigned long long seed, chgpu_mlp** out) {
   for (int o = 0; o < mlp::NOUT; ++o) id.sd_out[o] = 1.0f;
   set_norm(m, id);
   *out = m;
+  if (int rc = chgpu_mlp_set_norm(m, &id)) return rc;
   return chgpu_mlp_set_params(m, th.data());
 }
 
@@ -630,6 +676,7 @@ int chgpu_mlp_destroy(chgpu_mlp* m) {
   cudaFree(m->targ);
   cudaFree(m->loss);
   cudaFree(m->err);
+  cudaFree(m->nm_dev);
   if (m->stream) cudaStreamDestroy(m->stream);
   delete m;
   return 0;
@@ -658,7 +705,8 @@ int chgpu_mlp_set_norm(chgpu_mlp* m, const chgpu_mlp_norm* nm) {
     if (!(nm->sd_out[o] > 0.0f) || !std::isfinite(nm->mu_out[o]))
       return mfail(m, CHGPU_E_PARAM, "chgpu_mlp_set_norm: sd_out must be positive and mu_out finite");
   set_norm(m, *nm);
-  return 0;
+  MCK(m, cudaMemcpyAsync(m->nm_dev, &m->nm, sizeof(mlp::Norm), cudaMemcpyHostToDevice, m->stream));
+  return finish(m);
 }
 
 int chgpu_mlp_get_norm(chgpu_mlp* m, chgpu_mlp_norm* nm) {
@@ -759,7 +807,7 @@ int chgpu_mlp_predict(chgpu_mlp* m, const float* feat, long long n, float* out) 
   }
   cudaError_t e = cudaMemcpyAsync(df, feat, (size_t)n * mlp::NIN * sizeof(float), cudaMemcpyHostToDevice, m->stream);
   if (e == cudaSuccess) {
-    launch_mlp_infer(m->packed, df, n, m->nm, dout, m->err, m->nsm, m->stream);
+    launch_mlp_infer(m->packed, df, n, m->nm_dev, dout, m->err, m->nsm, m->stream);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess)

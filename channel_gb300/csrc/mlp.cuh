@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+struct chgpu_mlp;
+
 namespace chgpu {
 namespace mlp {
 
@@ -63,8 +65,12 @@ void launch_mlp_pack(const float* theta, unsigned char* packed, cudaStream_t s);
 void launch_mlp_train(const unsigned char* packed, const float* feat, const float* targ, long long n, long long first,
                       int tiles, const mlp::Norm& nm, float gscale, float* grad, double* loss, int* err, int nsm,
                       cudaStream_t s);
-void launch_mlp_infer(const unsigned char* packed, const float* feat, long long n, const mlp::Norm& nm, float* out,
+void launch_mlp_infer(const unsigned char* packed, const float* feat, long long n, const mlp::Norm* nm, float* out,
                       int* err, int nsm, cudaStream_t s);
+// tau at the closure points (planes iy = 1..ny-1) of phys[9][plane][plane_pts]
+// -> tau[6][plane][plane_pts]; a wait that runs out ors errbit into *err
+void launch_mlp_closure(const chgpu_mlp* m, const float* phys, float* tau, const float* wd, long long plane_pts,
+                        int nplanes, int ny, int* err, int errbit, int nsm, cudaStream_t s);
 void launch_adam(float* theta, float* g, float* m1, float* m2, int n, float lr, int t, cudaStream_t s);
 
 }  // namespace chgpu

@@ -116,6 +116,12 @@ SIGNATURES = {
     "chgpu_mlp_gradient": (C.c_int, [_P, C.c_longlong, C.c_longlong, _FP, _DP]),
     "chgpu_mlp_train": (C.c_int, [_P, C.c_int, C.c_longlong, C.c_float, _DP]),
     "chgpu_mlp_predict": (C.c_int, [_P, _FP, C.c_longlong, _FP]),
+    "chgpu_closure_dims": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "chgpu_closure_attach": (C.c_int, [_P, _P, C.c_int]),
+    "chgpu_closure_set_tau": (C.c_int, [_P, _FP]),
+    "chgpu_closure_features": (C.c_int, [_P, _FP]),
+    "chgpu_closure_physical": (C.c_int, [_P, _DP, C.c_int, _FP]),
+    "chgpu_products": (C.c_int, [_P, _DP]),
 }
 NKINDS = 6
 
@@ -325,6 +331,52 @@ class Channel:
         self._check(self.lib.chgpu_snapshot_wait(self.h, C.byref(ptr)))
         n = int(np.prod(self.shape))
         return np.ctypeslib.as_array(ptr, shape=(2 * n,)).view(np.complex128).reshape(self.shape).copy()
+
+    # ---- learned closure (include/chgpu_closure.h) ----
+    def closure_dims(self) -> tuple[int, int, int]:
+        """(2 nxd, nzd, ny-1): the closure points, x fastest."""
+        d = (C.c_int * 3)()
+        self._check(self.lib.chgpu_closure_dims(self.h, d))
+        return tuple(d)
+
+    def closure_points(self) -> int:
+        a, b, c = self.closure_dims()
+        return a * b * c
+
+    def products(self) -> np.ndarray:
+        """The six product spectra of the current field, (6, nx+1, 2nz+1, ny+3) complex128."""
+        out = np.empty((6,) + self.shape[1:], dtype=np.complex128)
+        self._check(self.lib.chgpu_products(self.h, _dp(out.view(np.float64))))
+        return out
+
+    def closure_features(self) -> np.ndarray:
+        out = np.empty((10, self.closure_points()), dtype=np.float32)
+        self._check(self.lib.chgpu_closure_features(self.h, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def closure_physical(self, spec: np.ndarray) -> np.ndarray:
+        """Physical values at the closure points of (3|6|9, nx+1, 2nz+1, ny+3) spectra."""
+        a = np.ascontiguousarray(spec, dtype=np.complex128)
+        if a.shape[1:] != self.shape[1:] or a.shape[0] not in (3, 6, 9):
+            raise ValueError(f"spectra shape {a.shape}")
+        out = np.empty((a.shape[0], self.closure_points()), dtype=np.float32)
+        self._check(self.lib.chgpu_closure_physical(self.h, _dp(a.view(np.float64)), a.shape[0],
+                                                    out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def closure_set_tau(self, tau: np.ndarray | None):
+        if tau is None:
+            self._check(self.lib.chgpu_closure_set_tau(self.h, None))
+            return
+        t = np.ascontiguousarray(tau, dtype=np.float32)
+        if t.shape != (6, self.closure_points()):
+            raise ValueError(f"tau shape {t.shape}")
+        self._check(self.lib.chgpu_closure_set_tau(self.h, t.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def closure_attach(self, mlp, enable: bool = True):
+        """Evaluate the network in every convolution pass (enable=False: the plain solver)."""
+        self._closure_mlp = mlp  # keeps the network alive while attached
+        self._check(self.lib.chgpu_closure_attach(self.h, mlp.h if mlp is not None else None, int(enable)))
 
     @property
     def launches(self) -> int:

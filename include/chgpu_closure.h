@@ -75,6 +75,44 @@ int chgpu_mlp_train(chgpu_mlp* m, int steps, long long batch, float lr, double* 
 /* Network outputs in physical units: out[CHGPU_MLP_OUT][n] from feat[CHGPU_MLP_IN][n]. */
 int chgpu_mlp_predict(chgpu_mlp* m, const float* feat, long long n, float* out);
 
+/* ---- the closure inside a channel handle ---- */
+
+/* Closure points of a handle: the physical grid of its convolutions (the
+ * 3/2-padded x and z points, dnsdata.f90:110-114) on the planes iy = 1..ny-1:
+ * dims = {2 nxd, nzd, ny-1}; npts = their product, x fastest, then z, then y. */
+int chgpu_closure_dims(chgpu_handle* h, int dims[3]);
+
+/* Attach a network: with enable = 1 every convolution pass of the step
+ * evaluates the network at the closure points of the current field and adds
+ * tau_ij to the six products there (walls and ghost planes get none);
+ * enable = 0 detaches it -- the plain under-resolved solver, the fallback.
+ * The handle keeps the pointer: the network must outlive the attachment.
+ * The next step is captured anew. */
+int chgpu_closure_attach(chgpu_handle* h, chgpu_mlp* m, int enable);
+
+/* A prescribed tau instead of the network: tau[6][npts] (FP32) added to the
+ * products at the closure points in every convolution pass; NULL removes it.
+ * An attached, enabled network takes precedence. */
+int chgpu_closure_set_tau(chgpu_handle* h, const float* tau);
+
+/* The network's inputs for the current field: feat[10][npts] -- the nine
+ * velocity gradients (d/dx, d/dz spectral; d/dy the compact derivative of
+ * COMPLEXderiv, dnsdata.f90:339-373) transformed to the closure points in
+ * FP32, and the wall distance min(y - ymin, ymax - y). */
+int chgpu_closure_features(chgpu_handle* h, float* feat);
+
+/* Physical values at the closure points of ncomp (3, 6 or 9) spectral fields
+ * of this handle's size, given in the restart-field layout
+ * [ncomp][nx+1][2nz+1][ny+3] complex128: out[ncomp][npts] (FP32 transforms). */
+int chgpu_closure_physical(chgpu_handle* h, const double* spec, int ncomp, float* out);
+
+/* The six product spectra uu vv ww uv vw uw of the current field, as the
+ * convolutions pass computes them (dnsdata.f90:487-602; no closure term), in
+ * the restart-field layout [6][nx+1][2nz+1][ny+3] complex128.  The subgrid
+ * stresses of a coarse field are the fine products at the coarse modes minus
+ * the coarse products of the truncated field. */
+int chgpu_products(chgpu_handle* h, double* out);
+
 #ifdef __cplusplus
 }
 #endif

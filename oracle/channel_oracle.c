@@ -167,6 +167,7 @@ struct orc_state {
   cplx* newrhs_eta;
   cplx* newrhs_d2v;
   cplx* F;       /* body force, V's layout, or NULL */
+  double* tau;   /* closure stresses [6][iy=1..ny-1][nzd][2nxd], or NULL */
   double* k2;    /* k2[ix*(2nz+1)+iz+nz] */
   fftplan pz_f, pz_b, px_f, px_b;
   /* module scalars */
@@ -424,6 +425,7 @@ void orc_destroy(orc_state* s) {
   free(s->V); free(s->old_eta); free(s->old_d2v); free(s->newrhs_eta); free(s->newrhs_d2v);
   free(s->VV);
   free(s->F);
+  free(s->tau);
   fftplan_free(&s->pz_f); fftplan_free(&s->pz_b); fftplan_free(&s->px_f); fftplan_free(&s->px_b);
   free(s);
 }
@@ -534,6 +536,12 @@ static double convolve_plane(orc_state* s, int iy, int compute_cfl, cplx* out, c
       *v = Vv * Vv * f;
       *ww = W * W * f;
     }
+  /* a prescribed subgrid stress enters with the products it belongs to */
+  if (s->tau && iy >= 1 && iy <= s->ny - 1) {
+    const size_t pp = (size_t)nzd * n2, np = (size_t)(s->ny - 1) * pp;
+    for (int c = 0; c < 6; ++c)
+      for (size_t q = 0; q < pp; ++q) w->xr[(size_t)c * pp + q] += s->tau[(size_t)c * np + (size_t)(iy - 1) * pp + q] * f;
+  }
   /* HFT, xTOz, FFT (dnsdata.f90:585-590) */
   for (int c = 0; c < 6; ++c) {
     for (int jz = 0; jz < nzd; ++jz) {
@@ -574,6 +582,17 @@ void orc_set_body_force(orc_state* s, const double* F) {
   }
   if (!s->F) s->F = (cplx*)malloc(sizeof(cplx) * (size_t)orc_field_len(s));
   memcpy(s->F, F, sizeof(cplx) * (size_t)orc_field_len(s));
+}
+
+void orc_set_tau(orc_state* s, const double* tau) {
+  const size_t n = (size_t)6 * (s->ny - 1) * s->nzd * 2 * s->nxd;
+  if (!tau) {
+    free(s->tau);
+    s->tau = NULL;
+    return;
+  }
+  if (!s->tau) s->tau = (double*)malloc(sizeof(double) * n);
+  memcpy(s->tau, tau, sizeof(double) * n);
 }
 
 /* dnsdata.f90:617-628: F(-1:0)=0, then F(-1) = -D4(F)/d4(-2) at iy=1; same at the top */

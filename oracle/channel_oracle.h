@@ -107,6 +107,12 @@ void orc_start(orc_state* s, orc_line* line);
  * (dnsdata.f90:617-628) and adds F's terms to the explicit parts. */
 void orc_set_body_force(orc_state* s, const double* F);
 
+/* A subgrid stress tau[6][iy=1..ny-1][nzd][2nxd] (physical, the order of
+ * the products uu vv ww uv vw uw) added to the products of the planes
+ * iy = 1..ny-1 before their forward transforms -- the closure's insertion
+ * point (no counterpart in the reference); NULL switches it off. */
+void orc_set_tau(orc_state* s, const double* tau);
+
 /* COMPLEXderiv followed by LeftLU5divStep2(D0mat) on one y-line
  * (dnsdata.f90:339-373): f0, f1 hold ny+3 complex values (iy=-1..ny+1). */
 void orc_deriv(const orc_state* s, const double* f0, double* f1);

@@ -43,8 +43,8 @@ class Scalars(C.Structure):
 
 
 def build(force: bool = False) -> Path:
-    if force or not LIB.exists():
-        subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    # make rebuilds when the sources are newer than the library
+    subprocess.run(["make", "-s", "-C", str(HERE)] + (["-B"] if force else []), check=True)
     return LIB
 
 
@@ -60,6 +60,7 @@ def lib():
         D = C.POINTER(C.c_double)
         L.orc_create.restype = P
         L.orc_create.argtypes = [C.POINTER(Params), C.c_int]
+        L.orc_sizes.argtypes = [C.POINTER(Params), C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.orc_destroy.argtypes = [P]
         L.orc_set_field.argtypes = [P, D]
         L.orc_get_field.argtypes = [P, D]
@@ -83,6 +84,7 @@ def lib():
         L.orc_fft.argtypes = [C.c_int, C.c_int, C.c_int, D]
         L.orc_deriv.argtypes = [P, D, D]
         L.orc_set_body_force.argtypes = [P, D]
+        L.orc_set_tau.argtypes = [P, D]
         L.orc_fftfit.restype = C.c_int
         L.orc_fftfit.argtypes = [C.c_int]
         _lib = L
@@ -122,6 +124,9 @@ class Oracle:
         if not self.h:
             raise ValueError("oracle rejected the parameters")
         self.shape = (3, p.nx + 1, 2 * p.nz + 1, p.ny + 3)
+        nxd, nzd = C.c_int(), C.c_int()
+        lib().orc_sizes(C.byref(self._cp), C.byref(nxd), C.byref(nzd))
+        self.nxd, self.nzd = nxd.value, nzd.value
 
     def close(self):
         if self.h:
@@ -178,6 +183,15 @@ class Oracle:
         a = np.ascontiguousarray(F, dtype=np.complex128)
         assert a.shape == self.shape
         lib().orc_set_body_force(self.h, _dp(a.view(np.float64)))
+
+    def set_tau(self, tau):
+        """tau (6, ny-1, nzd, 2nxd) added to the products, or None."""
+        if tau is None:
+            lib().orc_set_tau(self.h, None)
+            return
+        a = np.ascontiguousarray(tau, dtype=np.float64)
+        assert a.shape == (6, self.p.ny - 1, self.nzd, 2 * self.nxd), a.shape
+        lib().orc_set_tau(self.h, _dp(a))
 
     def deriv(self, f: np.ndarray) -> np.ndarray:
         """Compact first y-derivative of a complex y-line (iy=-1..ny+1)."""
