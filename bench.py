@@ -569,6 +569,75 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_closure(args):
+    """The learned closure on the Re_tau 180 grid: FP64 DNS 127x192x127 from a
+    seeded broadband field, coarse solver 47x192x47 (the x and z modes of the
+    47x96x47 closure grid on the DNS's y grid), training on the tensor cores,
+    explained variance on held-out snapshots and the coarse solver's error
+    against the filtered DNS with and without the network; then the training
+    kernel's throughput and the cost of the closure in the coarse step."""
+    import dataclasses
+
+    import torch
+    from channel_gb300 import Channel, dnsin, initial
+    from channel_gb300 import closure as cl
+
+    pf = dnsin.workload("retau180")
+    net, rep = cl.pipeline(pf, 47, 47, amp=0.002, kmax=48, spinup=150, every=15, nsnap=12, nval=3,
+                           points=400_000, steps=20_000, horizons=(10, 40))
+    # training throughput: Adam steps of 152 x 128 points on resident data
+    m = cl.Mlp(1)
+    rng = np.random.default_rng(0)
+    n = 1 << 21
+    m.set_data(rng.normal(size=(10, n)).astype(np.float32), rng.normal(size=(6, n)).astype(np.float32))
+    batch = 152 * 128
+    m.train(50, batch, 1e-3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    steps = 2000
+    m.train(steps, batch, 1e-3)
+    dt_train = (time.perf_counter() - t0) / steps
+    feat = rng.normal(size=(10, n)).astype(np.float32)
+    m.predict(feat)
+    t0 = time.perf_counter()
+    for _ in range(5):
+        m.predict(feat)
+    dt_pred = (time.perf_counter() - t0) / 5
+    # MMA work issued per point (padded shapes): forward 11 264 and backward
+    # 35 840 multiply-adds
+    fl_train = 2.0 * (11264 + 35840) * batch / dt_train
+    m.close()
+    # the closure's share of the coarse step
+    pc = dataclasses.replace(pf, nx=47, nz=47)
+    V0 = cl.restrict(initial.perturbed_laminar(pf, 0.002, 0, kmax=48), 47, 47)
+    step_ms = {}
+    probe = cl.Mlp(2) if net is None else net
+    for name, on in (("plain", False), ("closure", True)):
+        with Channel(pc, "fp64") as c:
+            c.upload(V0)
+            if on:
+                c.closure_attach(probe, True)
+            c.start()
+            for _ in range(3):
+                c.step(sync=False)
+            c.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(20):
+                c.step(sync=False)
+            c.synchronize()
+            step_ms[name] = 1e3 * (time.perf_counter() - t0) / 20
+    out = {"mode": "closure", **rep,
+           "training_kernel": {"batch": batch, "ms_per_adam_step": 1e3 * dt_train,
+                               "points_per_s": batch / dt_train, "mma_tflops_issued": fl_train / 1e12,
+                               "arithmetic": "tcgen05.mma kind::f16, BF16 operands, FP32 accumulators in TMEM"},
+           "inference_points_per_s": n / dt_pred,
+           "coarse_step_ms": step_ms,
+           "data": "synthetic: seeded broadband field (initial.perturbed_laminar, modes up to kmax), FP64 DNS"}
+    print(json.dumps(out), flush=True)
+    if net is not None:
+        net.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -580,9 +649,10 @@ def main():
                     help="fixed transform tiles instead of autotuning, e.g. fp64:8,4,2,256,256/mixed:8,4,3,256,192 "
                          "(z columns, x rows, x-row variant, z threads, x threads; for reproducible profiler "
                          "captures)")
-    ap.add_argument("--mode", default="full", choices=["full", "timed", "long"],
+    ap.add_argument("--mode", default="full", choices=["full", "timed", "long", "closure"],
                     help="timed: only the three timed runs (for profiler captures); long: --steps steps of FP64, "
-                         "FP64DD and mixed from one field, Runtimedata and profile errors against FP64 over the run")
+                         "FP64DD and mixed from one field, Runtimedata and profile errors against FP64 over the run; "
+                         "closure: the learned closure trained and judged against the FP64 DNS")
     args = ap.parse_args()
     for item in filter(None, args.tiles.split("/")):
         prec, t = item.split(":")
@@ -595,6 +665,8 @@ def main():
         b.build()
         if args.mode == "long":
             run_long(args)
+        elif args.mode == "closure":
+            run_closure(args)
         else:
             run_ours(args)
     else:
