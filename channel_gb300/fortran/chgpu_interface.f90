@@ -1,5 +1,6 @@
 !==============================================================!
-! Fortran 2008 interface to libchgpu.so (include/chgpu.h).    !
+! Fortran 2008 interface to libchgpu.so (include/chgpu.h and !
+! include/chgpu_closure.h).                                   !
 ! Lets a Fortran driver shaped like channel.f90 call the GB300 !
 ! time step through iso_c_binding.  Compile with the driver    !
 ! and link -lchgpu (channel_gb300/_build/libchgpu.so).        !
@@ -44,6 +45,12 @@ MODULE chgpu_interface
     INTEGER(C_INT)       :: fluct_only, part, z_threshold
     REAL(C_FLOAT)        :: undersample
   END TYPE chgpu_export_opts
+
+  ! Mirrors chgpu_mlp_norm (include/chgpu_closure.h).
+  INTEGER(C_INT), PARAMETER :: CHGPU_MLP_NPARAMS = 9734
+  TYPE, BIND(C) :: chgpu_mlp_norm
+    REAL(C_FLOAT)        :: mu_in(10), sd_in(10), mu_out(6), sd_out(6)
+  END TYPE chgpu_mlp_norm
 
   INTERFACE
     INTEGER(C_INT) FUNCTION chgpu_create(p, h) BIND(C, name="chgpu_create")
@@ -160,6 +167,33 @@ MODULE chgpu_interface
     TYPE(C_PTR) FUNCTION chgpu_last_error(h) BIND(C, name="chgpu_last_error")
       IMPORT :: C_PTR
       TYPE(C_PTR), VALUE :: h
+    END FUNCTION
+    ! ---- learned closure (include/chgpu_closure.h) ----
+    INTEGER(C_INT) FUNCTION chgpu_mlp_create(seed, m) BIND(C, name="chgpu_mlp_create")
+      IMPORT :: C_INT, C_LONG_LONG, C_PTR
+      INTEGER(C_LONG_LONG), VALUE :: seed
+      TYPE(C_PTR), INTENT(OUT) :: m
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION chgpu_mlp_destroy(m) BIND(C, name="chgpu_mlp_destroy")
+      IMPORT :: C_INT, C_PTR
+      TYPE(C_PTR), VALUE :: m
+    END FUNCTION
+    ! theta(CHGPU_MLP_NPARAMS): W1(16,64) W2(64,64) b2(64) W3(64,64) b3(64) W4(64,6) b4(6), column-major view of W[o][i]
+    INTEGER(C_INT) FUNCTION chgpu_mlp_set_params(m, theta) BIND(C, name="chgpu_mlp_set_params")
+      IMPORT :: C_INT, C_PTR, C_FLOAT
+      TYPE(C_PTR), VALUE :: m
+      REAL(C_FLOAT), INTENT(IN) :: theta(*)
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION chgpu_mlp_set_norm(m, nm) BIND(C, name="chgpu_mlp_set_norm")
+      IMPORT :: C_INT, C_PTR, chgpu_mlp_norm
+      TYPE(C_PTR), VALUE :: m
+      TYPE(chgpu_mlp_norm), INTENT(IN) :: nm
+    END FUNCTION
+    ! enable = 1: the network's stresses enter every convolution pass; 0: the plain solver
+    INTEGER(C_INT) FUNCTION chgpu_closure_attach(h, m, enable) BIND(C, name="chgpu_closure_attach")
+      IMPORT :: C_INT, C_PTR
+      TYPE(C_PTR), VALUE :: h, m
+      INTEGER(C_INT), VALUE :: enable
     END FUNCTION
   END INTERFACE
 
