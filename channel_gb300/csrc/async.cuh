@@ -21,6 +21,18 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsign
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
 }
+// several bulk copies completing one phase: announce their total once, then
+// issue each copy without an arrival of its own
+__device__ __forceinline__ void mbar_arrive_expect(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s_noarrive(void* dst, const void* src, unsigned bytes,
+                                                       unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
 // true once phase `parity` of the barrier has completed; false after
 // `limit` polls
 __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, int limit) {

@@ -349,7 +349,7 @@ void enqueue_closure(chgpu_handle* h) {
                          (const float2*)h->cl_twh, d, h->rz, h->rx, h->zcols, h->xrows, h->sc, h->stream);
   launch_mlp_closure(h->cl_mlp, reinterpret_cast<const float*>(h->cl_P), reinterpret_cast<float*>(h->cl_tau),
                      h->cl_wd, (long long)d.nzd * 2 * d.nxd, d.nplanes, d.ny, &h->sc->error, 4, h->nsm, h->stream);
-  h->launches += 4;
+  h->launches += 5;
 }
 
 void run_convolutions(chgpu_handle* h, int compute_cfl, int products, int plane0, int nplanes, int stage_lo = 0,
@@ -1522,7 +1522,7 @@ int chgpu_closure_features(chgpu_handle* h, float* feat) {
   launch_gradients(h->V, h->cl_G, h->der, h->d0lu, h->bc, d, h->stream);
   launch_physical_fields(h->cl_G, 9, h->cl_Z, h->cl_P, (const float2*)h->cl_twz, (const float2*)h->cl_twx,
                          (const float2*)h->cl_twh, d, h->rz, h->rx, h->zcols, h->xrows, h->sc, h->stream);
-  h->launches += 3;
+  h->launches += 4;
   CK(h, cudaGetLastError());
   if (int rc = copy_closure_points(h, 9, feat)) return rc;
   if (int rc = pull_scalars(h)) return rc;

@@ -1,7 +1,8 @@
 // Velocity gradients of the coarse field for the learned closure.
 //
-// k_grad: one thread per (mode, velocity component c).  d/dx and d/dz are
-// the products with i alfa0 kx and i beta0 kz; d/dy is the compact
+// k_grad_xz: d/dx and d/dz, the products with i alfa0 kx and i beta0 kz,
+// one thread per value.  k_grad: one thread per (mode, velocity component
+// c), d/dy by the compact
 // derivative COMPLEXderiv (dnsdata.f90:339-373): the d1 stencil with the
 // one-sided wall values d140/d14m1/d14n/d14np1 folded in, then the two
 // sweeps of the D0mat factorisation (LeftLU5divStep1 bottom-up,
@@ -23,20 +24,28 @@ __device__ __forceinline__ double2 operator-(double2 a, double2 b) { return make
 __device__ __forceinline__ double2 operator+(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 rm(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
 
+// d/dx and d/dz: one thread per (component, plane, mode)
+__global__ void k_grad_xz(const double2* __restrict__ V, double2* __restrict__ G, Dims d) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t per_c = (size_t)d.nplanes * d.nmodes;
+  if (t >= 3 * per_c) return;
+  const int c = (int)(t / per_c);
+  const size_t r = t - c * per_c;
+  const int m = (int)(r % d.nmodes);
+  const int ix = m / d.nzt, kz = m - ix * d.nzt - d.nz;
+  const double ka = d.alfa0 * ix, kb = d.beta0 * kz;
+  const double2 v = V[t];
+  G[(size_t)(3 * c) * per_c + r] = make_double2(-ka * v.y, ka * v.x);
+  G[(size_t)(3 * c + 2) * per_c + r] = make_double2(-kb * v.y, kb * v.x);
+}
+
+// d/dy: one thread per (mode, component), the two sweeps along y
 __global__ void k_grad(const double2* __restrict__ V, double2* __restrict__ G, const double* __restrict__ der,
                        const double* __restrict__ d0lu, BcRows bc, Dims d) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 3 * d.nmodes) return;
   const int c = t / d.nmodes, m = t - c * d.nmodes;
-  const int ix = m / d.nzt, kz = m - ix * d.nzt - d.nz;
-  const double ka = d.alfa0 * ix, kb = d.beta0 * kz;
   const int ny = d.ny;
-  // d/dx, d/dz on every plane
-  for (int iy = -1; iy <= ny + 1; ++iy) {
-    const double2 v = V[gidx(d, c, iy, m)];
-    G[gidx(d, 3 * c, iy, m)] = make_double2(-ka * v.y, ka * v.x);
-    G[gidx(d, 3 * c + 2, iy, m)] = make_double2(-kb * v.y, kb * v.x);
-  }
   // d/dy: wall values, then Step1 bottom-up parked in the d/dy slot, then Step2
   auto dot5 = [&](int iy0, const double* w) {
     double2 a = rm(w[0], V[gidx(d, c, iy0, m)]);
@@ -85,8 +94,10 @@ __global__ void k_grad(const double2* __restrict__ V, double2* __restrict__ G, c
 
 void launch_gradients(const double2* V, double2* G, const double* der, const double* d0lu, const BcRows& bc,
                       const Dims& d, cudaStream_t s) {
+  const size_t nxz = (size_t)3 * d.nplanes * d.nmodes;
+  k_grad_xz<<<(unsigned)((nxz + 255) / 256), 256, 0, s>>>(V, G, d);
   const int n = 3 * d.nmodes;
-  k_grad<<<(n + 127) / 128, 128, 0, s>>>(V, G, der, d0lu, bc, d);
+  k_grad<<<(n + 63) / 64, 64, 0, s>>>(V, G, der, d0lu, bc, d);
 }
 
 }  // namespace chgpu

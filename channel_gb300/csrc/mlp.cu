@@ -423,7 +423,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer(const unsigned char* __restri
   __shared__ __align__(8) unsigned long long bar;
   __shared__ unsigned tbase_s;
   const int p = threadIdx.x, warp = p >> 5;
-  const Norm nm = *nmp;
+  const Norm& nm = *nmp;  // read through the cache where used
   if (p == 0) mbar_init(&bar, 1);
   if (warp == 0) tm_alloc(&tbase_s, kInferCols);
   tm_fence_before();
@@ -432,11 +432,15 @@ __global__ void __launch_bounds__(128) k_mlp_infer(const unsigned char* __restri
   const unsigned tbase = tbase_s;
   const unsigned tl = tbase + ((unsigned)(32 * warp) << 16);
   unsigned phase = 0;
-  if (p == 0) bulk_copy_g2s(sm, packed, PACKED_BYTES, &bar);
+  if (p == 0) {  // forward operands and biases: two bulk copies, one phase
+    mbar_arrive_expect(&bar, P_W4T + (PACKED_BYTES - P_BIAS));
+    bulk_copy_g2s_noarrive(sm, packed, P_W4T, &bar);
+    bulk_copy_g2s_noarrive(sm + SI_BIAS, packed + P_BIAS, PACKED_BYTES - P_BIAS, &bar);
+  }
   bool ok = __syncthreads_and(mbar_wait(&bar, phase, kBulkWaitPolls));
   phase ^= 1u;
-  const float* bias = reinterpret_cast<const float*>(sm + P_BIAS);
-  unsigned char *X = sm + S_X, *PA = sm + S_PA, *PB = sm + S_PB;
+  const float* bias = reinterpret_cast<const float*>(sm + SI_BIAS);
+  unsigned char *X = sm + SI_X, *H = sm + SI_H;
   constexpr unsigned i64 = idesc_bf16(128, 64), i16 = idesc_bf16(128, 16);
   const long long n = io.count();
   const long long tiles = (n + 127) / 128;
@@ -449,17 +453,17 @@ __global__ void __launch_bounds__(128) k_mlp_infer(const unsigned char* __restri
     write_input_row(X, nullptr, p, f);
     ok = stage(&bar, phase, [&] { mma_chain(tbase + I_Z, X, 256, sm + P_W1, 256, 1, i64, false); });
     if (!ok) break;
-    hidden_epilogue(tl + I_Z, nullptr, PA, nullptr, p);
-    ok = stage(&bar, phase, [&] { mma_chain(tbase + I_Z, PA, 1024, sm + P_W2, 1024, 4, i64, false); });
+    hidden_epilogue(tl + I_Z, nullptr, H, nullptr, p);
+    ok = stage(&bar, phase, [&] { mma_chain(tbase + I_Z, H, 1024, sm + P_W2, 1024, 4, i64, false); });
     if (!ok) break;
-    hidden_epilogue(tl + I_Z, bias, PB, nullptr, p);
-    ok = stage(&bar, phase, [&] { mma_chain(tbase + I_Z, PB, 1024, sm + P_W3, 1024, 4, i64, false); });
+    hidden_epilogue(tl + I_Z, bias, H, nullptr, p);
+    ok = stage(&bar, phase, [&] { mma_chain(tbase + I_Z, H, 1024, sm + P_W3, 1024, 4, i64, false); });
     if (!ok) break;
-    hidden_epilogue(tl + I_Z, bias + 64, PA, nullptr, p);
-    ok = stage(&bar, phase, [&] { mma_chain(tbase + I_Y, PA, 1024, sm + P_W4, 1024, 4, i16, false); });
+    hidden_epilogue(tl + I_Z, bias + 64, H, nullptr, p);
+    ok = stage(&bar, phase, [&] { mma_chain(tbase + I_Z, H, 1024, sm + P_W4, 1024, 4, i16, false); });
     if (!ok) break;
     float v[16];
-    tm_ld16(tl + I_Y, v);
+    tm_ld16(tl + I_Z, v);
     if (idx < n)
       for (int o = 0; o < NOUT; ++o) io.store(idx, o, (v[o] + bias[128 + o]) * nm.sd_out[o] + nm.mu_out[o]);
   }
@@ -535,14 +539,14 @@ void launch_mlp_train(const unsigned char* packed, const float* feat, const floa
 void launch_mlp_infer(const unsigned char* packed, const float* feat, long long n, const mlp::Norm* nm, float* out,
                       int* err, int nsm, cudaStream_t s) {
   const long long tiles = (n + 127) / 128;
-  const int grid = (int)(tiles < 2LL * nsm ? tiles : 2LL * nsm);
+  const int grid = (int)(tiles < 4LL * nsm ? tiles : 4LL * nsm);
   if (grid > 0) mlp::k_mlp_infer<<<grid, 128, mlp::S_INFER_END, s>>>(packed, mlp::SoaIO{feat, out, n}, nm, err, 1);
 }
 void launch_mlp_closure(const chgpu_mlp* m, const float* phys, float* tau, const float* wd, long long plane_pts,
                         int nplanes, int ny, int* err, int errbit, int nsm, cudaStream_t s) {
   const long long n = (long long)(ny - 1) * plane_pts;
   const long long tiles = (n + 127) / 128;
-  const int grid = (int)(tiles < 2LL * nsm ? tiles : 2LL * nsm);
+  const int grid = (int)(tiles < 4LL * nsm ? tiles : 4LL * nsm);
   mlp::PlaneIO io{phys, tau, wd, plane_pts, (long long)nplanes * plane_pts, n};
   if (grid > 0) mlp::k_mlp_infer<<<grid, 128, mlp::S_INFER_END, s>>>(m->packed, io, m->nm_dev, err, errbit);
 }

@@ -45,13 +45,20 @@ constexpr int S_T = S_DY + 4096;    // transposed operands: rows x 128 points, 2
 constexpr int G_XT = 0, G_H1T = 2, G_ONE1 = 10, G_H2T = 11, G_ONE2 = 19, G_H3T = 20, G_ONE3 = 28;
 constexpr int G_DYT = 29, G_DZ3T = 31, G_DZ2T = 39, G_DZ1T = 47, G_END = 55;
 constexpr int S_END = S_T + G_END * 2048;  // 193 536 bytes
-constexpr int S_INFER_END = S_DY;          // weights, input tile, ping, pong
+// shared memory of the inference kernel: the forward operands W1..W4 (the
+// first P_W4T bytes of the packed block), the biases, the input tile and one
+// activation tile (each layer's epilogue overwrites the operand its product
+// has finished reading)
+constexpr int SI_BIAS = P_W4T;                 // 20480
+constexpr int SI_X = 21504;                    // [128 x 16]
+constexpr int SI_H = SI_X + 4096;              // [128 x 64]
+constexpr int S_INFER_END = SI_H + 16384;      // 41 984 bytes
 
 // tensor-memory columns (FP32, 128 lanes)
 constexpr unsigned C_Z1 = 0, C_Z2 = 64, C_Z3 = 128, C_Y4 = 192, C_DH = 208;
 constexpr unsigned C_DW1 = 272, C_DW2 = 336, C_DW3 = 400, C_DW4 = 464;
 constexpr unsigned kTrainCols = 512;
-constexpr unsigned I_Z = 0, I_Y = 64, kInferCols = 128;
+constexpr unsigned I_Z = 0, kInferCols = 64;  // every layer's accumulator in the same 64 columns
 
 struct Norm {
   float mu_in[NIN], isd_in[NIN];
