@@ -1420,9 +1420,26 @@ void drop_graph(chgpu_handle* h) {  // the captured step holds the old launch se
   ++h->version;
 }
 
-// buffers and FP32 tables of the closure, on first use
+void closure_free(chgpu_handle* h) {
+  void** bufs[] = {(void**)&h->cl_G, (void**)&h->cl_Z, (void**)&h->cl_P, (void**)&h->cl_tau, (void**)&h->cl_wd,
+                   &h->cl_twz, &h->cl_twx, &h->cl_twh};
+  for (void** b : bufs) {
+    if (*b) cudaFree(*b);
+    *b = nullptr;
+  }
+}
+
+int closure_alloc_all(chgpu_handle* h);
+
+// buffers and FP32 tables of the closure, on first use; all or nothing
 int closure_alloc(chgpu_handle* h) {
-  if (h->cl_G) return 0;
+  if (h->cl_twh) return 0;  // the last one made
+  const int rc = closure_alloc_all(h);
+  if (rc) closure_free(h);
+  return rc;
+}
+
+int closure_alloc_all(chgpu_handle* h) {
   const Dims& d = h->d;
   const size_t np = d.nplanes, nm = d.nmodes, nxp = d.nx + 1;
   const size_t phys = (size_t)9 * np * d.nzd * d.nxd * sizeof(float2);

@@ -173,3 +173,54 @@ def test_network_steps_run_in_the_graph(gpu_lib):
     g.closure_attach(m, False)
     g.step()
     assert np.all(np.isfinite(g.download()))
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64dd", 1e-12), ("mixed", 2e-5)])
+def test_products_of_every_precision(gpu_lib, prec, tol):
+    """chgpu_products converts the double-float and FP32 product spectra to
+    complex128: against the oracle within the precision of each path."""
+    import pyoracle
+
+    p, V0, g = setup(prec)
+    o = pyoracle.Oracle(p)
+    o.set_field(V0)
+    P = g.products()
+    for iy in (0, 5, p.ny // 2, p.ny):
+        ref, _ = o.convolve_plane(iy)
+        assert np.abs(P[:, :, :, iy + 1] - ref).max() <= tol * np.abs(ref).max(), iy
+
+
+@pytest.mark.parametrize("ncomp", [3, 9])
+def test_physical_transform_component_counts(gpu_lib, ncomp):
+    from channel_gb300 import dnsin
+
+    p, V0, g = setup("mixed")
+    nxd, nzd = dnsin.padded_sizes(p.nx, p.nz)
+    rng = np.random.default_rng(ncomp)
+    S = (rng.normal(size=(ncomp,) + V0.shape[1:]) + 1j * rng.normal(size=(ncomp,) + V0.shape[1:])) * 0.1
+    got = g.closure_physical(S).reshape(ncomp, p.ny - 1, nzd, 2 * nxd)
+    ref = physical(S, nxd, nzd)
+    assert np.abs(got - ref).max() / np.abs(ref).max() < 2e-6
+    with pytest.raises(Exception):
+        g.closure_physical(S[:2])
+
+
+def test_network_in_a_mixed_coarse_step(gpu_lib):
+    """The closure in the FP32-transform path: the network's stresses enter
+    as in the FP64 path (prescribed equivalence, bit for bit)."""
+    from channel_gb300 import lib
+    from channel_gb300.closure import Mlp
+
+    p, V0, g = setup("mixed", amp=0.1)
+    m = Mlp(8)
+    feat = g.closure_features()
+    m.norm = {"mu_in": feat.mean(1), "sd_in": feat.std(1) + 1e-6, "mu_out": np.zeros(6), "sd_out": np.full(6, 1e-3)}
+    tau = m.predict(feat)
+    g.start(deltat=1e-3)
+    g.closure_attach(m, True)
+    g.buildrhs(lib.RK[1], False)
+    g2 = setup("mixed", amp=0.1)[2]
+    g2.start(deltat=1e-3)
+    g2.closure_set_tau(tau)
+    g2.buildrhs(lib.RK[1], False)
+    assert np.array_equal(g.download(), g2.download())

@@ -266,3 +266,35 @@ def test_two_half_step_is_identical(gpu_lib, prec):
     assert np.array_equal(lg, lt)
     g.close()
     t.close()
+
+
+# uneven sizes: odd and even mode counts, ny-1 not a multiple of the row
+# groups, transform lengths 24 / 48 / 32 / 96 (2^a and 3*2^a)
+UNEVEN = [(11, 20, 13), (24, 33, 9), (40, 50, 31)]
+
+
+@pytest.mark.parametrize("nx,ny,nz", UNEVEN)
+@pytest.mark.parametrize("prec", ["fp64", "fp64dd", "mixed"])
+def test_uneven_sizes_match_oracle(gpu_lib, nx, ny, nz, prec):
+    import pyoracle
+    from channel_gb300 import Channel, dnsin, initial
+
+    p = dnsin.DnsIn(nx=nx, ny=ny, nz=nz, alfa0=1.3, beta0=2.1, re=3000.0, a=1.6, ymin=0.0, ymax=2.0,
+                    meanflowx=4.0 / 3.0, deltat=0.003, cflmax=0.0, nstep=3)
+    V0 = initial.perturbed_laminar(p, 0.02, 3, kmax=min(nx, nz, 6))
+    o = pyoracle.Oracle(p)
+    o.set_field(V0)
+    g = Channel(p, prec)
+    g.upload(V0)
+    o.start()
+    g.start()
+    for _ in range(3):
+        lo, lg = o.step(), g.step()
+    e = per_field_rel(g.download(), o.field())
+    if prec == "mixed":  # FP32 transforms: the statistics bar is 1e-4; fields stay far inside it
+        assert max(e) <= 1e-5, e
+    else:
+        assert max(e) <= TOL1 * 10, e
+        ok, err = line_close(lg, lo, 1e-10)
+        assert ok, (err, lg, lo)
+    g.close()
