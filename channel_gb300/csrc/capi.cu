@@ -56,6 +56,12 @@ struct chgpu_handle {
   // GPU emptier than they overlap (mixed path 10.0 -> 11.2 ms at 127x192x127),
   // at 147 456 the overlap gains ~1%.
   int halves = 1;
+  // the banded solves as two kernels (factorisation, then one thread per
+  // mode and system) below 65 536 pairs: at 16 384 the fused kernel has ~7
+  // warps per SM and the split is 14-17% faster; at 147 456 the fused kernel
+  // hides its latency and the split is 4-19% slower (extra factor traffic,
+  // half the warps idle during v')
+  bool split_solve = false;
   cudaStream_t stream2 = nullptr;
   cudaEvent_t ev_vv = nullptr, ev_solved = nullptr;
   // device buffers
@@ -409,8 +415,9 @@ void run_linsolve(chgpu_handle* h, double ode1, double lambda, int from_dt, bool
     L.rhs_plane_off = -1;
   }
   if (!s) s = h->stream;
+  L.split_solve = h->split_solve ? 1 : 0;
   timed(h, 4, [&] { launch_linsolve(L, s); });
-  h->launches += 1;
+  h->launches += h->split_solve ? 2 : 1;
 }
 
 void run_outstats(chgpu_handle* h) {
@@ -564,6 +571,7 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
   Radix rz = make_radix(nzd, false), rx = make_radix(nxd, h->prec == CHGPU_MIXED);
   if (rz.nst < 0 || rx.nst < 0) { delete h; return fail(nullptr, CHGPU_E_PARAM, "unsupported FFT length"); }
   h->halves = d.npairs >= 65536 ? 2 : 1;
+  h->split_solve = d.npairs < 65536;
   h->rz.n = rz.n; h->rz.nst = rz.nst; std::memcpy(h->rz.r, rz.r, sizeof rz.r);
   h->rx.n = rx.n; h->rx.nst = rx.nst; std::memcpy(h->rx.r, rx.r, sizeof rx.r);
   set_twiddle_offsets(h->rz);
@@ -606,7 +614,11 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
     if ((rc = dev_alloc(&h->Pb, std::max(ts * 6 * nplanes * nxp * nzd, sizeof(double2) * 3 * nplanes * nmodes),
                         "x work buffer"))) break;
     if ((rc = dev_alloc((void**)&h->rhs, sizeof(double2) * 2 * (p->ny - 1) * nmodes, "rhs"))) break;
-    if ((rc = dev_alloc((void**)&h->fac, sizeof(double) * 4 * (p->ny - 1) * (size_t)d.npairs, "factors"))) break;
+    if ((rc = dev_alloc((void**)&h->fac,
+                        sizeof(double) * (h->split_solve ? kFacPerRow : kFacPerRowFused) * (p->ny - 1) *
+                            (size_t)d.npairs,
+                        "factors")))
+      break;
     if ((rc = dev_alloc((void**)&h->der, sizeof(double) * t.der.size(), "der"))) break;
     if ((rc = dev_alloc((void**)&h->d0lu, sizeof(double) * t.d0lu.size(), "D0mat"))) break;
     if ((rc = dev_alloc((void**)&h->yint, sizeof(double) * std::max<size_t>(3, t.yint.size()), "yint"))) break;

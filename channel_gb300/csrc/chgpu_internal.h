@@ -66,6 +66,7 @@ struct DevScalars {
   double u0, uN;
   double line[11];
   double runtime_global;
+  double wallrhs[8];  // the mean mode's wall-velocity terms of the eta right-hand side, rows 1, 2, ny-2, ny-1
   long long istep;
   int error;  // bit 0: non-finite CFL or statistics; bit 1: a bulk-copy wait ran out;
               // bit 2: a tensor-core completion wait of the closure ran out

@@ -64,6 +64,11 @@ void launch_physical_fields(const double2* src, int ncomp, float2* zb, float2* o
 void launch_gradients(const double2* V, double2* G, const double* der, const double* d0lu, const BcRows& bc,
                       const Dims& d, cudaStream_t s);
 
+// factor doubles per y row and (kx, +-kz) pair: the fused solve keeps l2, l1
+// of the v and eta matrices; the split solve (k_factor + k_solve) l2, l1,
+// 1/d, u1, u2 of both
+constexpr int kFacPerRowFused = 4, kFacPerRow = 10;
+
 struct SolveLaunch {
   Dims d;
   BcRows bc;
@@ -90,6 +95,7 @@ struct SolveLaunch {
   const double* nud;  // per y row: -ni d4 (5), -ni d2 (5); null: formed in the kernel
   int m_lo, m_hi;     // modes of k_rhs (all: 0, nmodes); a range of whole kx columns
   int q_lo, q_hi;     // (kx, +-kz) pairs of k_linsolve (all: 0, npairs)
+  int split_solve;    // 0: the fused k_linsolve; 1: k_factor then k_solve (fac holds kFacPerRow per row)
 };
 
 template <typename T> void launch_rhs(const SolveLaunch& L, cudaStream_t s);

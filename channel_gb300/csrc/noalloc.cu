@@ -5,7 +5,7 @@
 // code that runs inside a fixed memory arena handed out by its framework, a
 // driver that reserved the GPU's memory at start-up, or a caller that must
 // not trigger an allocation between launches.  They cannot let a library call
-// cudaMalloc.  This entry point runs the same solve kernel as
+// cudaMalloc.  This entry point runs the fused solve kernel of
 // chgpu_linsolve on the caller's field buffer, and keeps everything else it
 // needs -- the pentadiagonal factors (the kernel's scratch), the
 // wall-normal tables and the mean-flow scalars -- in the file-scope device
@@ -98,7 +98,7 @@ extern "C" int chgpu_linsolve_noalloc(const chgpu_params* p, double lambda, doub
   if (p->nx < 1 || p->nz < 1 || p->ny < 8 || p->ny > StaticTables::kMaxNy)
     return error(CHGPU_E_PARAM, "chgpu_linsolve_noalloc: need nx>=1, nz>=1, 8<=ny<=1024");
   const size_t npairs = (size_t)(p->nx + 1) * (p->nz + 1);
-  const size_t need = 4 * (size_t)(p->ny - 1) * npairs;
+  const size_t need = chgpu::kFacPerRowFused * (size_t)(p->ny - 1) * npairs;
   if (need > kFactorDoubles) {
     if (err && errlen)
       std::snprintf(err, errlen,

@@ -18,6 +18,11 @@
 //   pass C (iy=ny-1..1): COMPLEXderiv of v with LeftLU5divStep1(D0mat) (dnsdata.f90:339-373)
 //   pass D (iy=-1..ny+1): LeftLU5divStep2(D0mat) and u,w recovery (linsolve_blocking.inc:99-103)
 // The recurrences of each mode are sequential in y; parallelism is across modes.
+// k_factor + k_solve : the same solve for grids with fewer than 65 536 pairs:
+//              pass A's factorisation alone (two threads per pair, factors to
+//              global memory), then Step1, Step2, walls, mean flow, v' and
+//              u, w with one thread per (system, mode) -- twice the threads
+//              of the fused kernel where it has too few to hide latency.
 #include <cuda_runtime.h>
 
 #include <type_traits>
@@ -744,11 +749,255 @@ __global__ void __launch_bounds__(64, 8) k_linsolve(double2* __restrict__ V, con
   else deriv_uw<double>(V, der, d0lu, lindd, bc, d, mm[role], ka, (role == 0 ? 1.0 : -1.0) * kb, k2);
 }
 
+// The same solves in two kernels, for grids with few pairs (the fused kernel
+// has too few warps per SM there to hide its recurrences' latency):
+//
+// k_factor: two threads per pair (kx, +-kz), whose matrices are equal because
+// k^2 is: role 0 the v system (D2vmat), role 1 the eta system (etamat).
+// Bottom-up (iy = ny-1..1): assemble, fold the boundary rows, LU5decompStep
+// row; each row's factors go to fac[iy-1][5 role + {l2, l1, 1/d, u1, u2}][q]
+// (l2, l1 the scaled lower entries LeftLU5divStep2 reads, 1/d, u1, u2 the
+// reciprocal pivot and upper entries LeftLU5divStep1 reads).  The eta thread
+// of the mean mode also stores the wall-velocity terms of its right-hand side
+// (rows 1, 2, ny-2, ny-1; linsolve_blocking.inc:26-27,40-41).
+// Registers capped for 8 resident 64-thread blocks per SM.
+__global__ void __launch_bounds__(64, 8) k_factor(double* __restrict__ fac, const double* __restrict__ der,
+                                                  BcRows bc, Dims d, double lambda_in, double ode1,
+                                                  int lambda_from_dt, DevScalars* __restrict__ sc,
+                                                  const double* __restrict__ nud, int q_lo, int q_hi) {
+  const int lane = threadIdx.x & 31, role = threadIdx.x >> 5;
+  const int q = q_lo + blockIdx.x * 32 + lane;
+  if (q >= q_hi) return;
+  const int ny = d.ny, nz = d.nz;
+  const int ix = q / (nz + 1);
+  const int a = q - ix * (nz + 1);
+  const bool is00 = (ix == 0 && a == 0);
+  const double ka = ix * d.alfa0, kb = a * d.beta0;
+  const double k2 = ka * ka + kb * kb;
+  const double lambda = lambda_from_dt ? ode1 / sc->deltat : lambda_in;
+  const size_t P = d.npairs;
+  double bot[5], botm1[5], top[5], topp1[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    bot[j] = role ? bc.eta0bc[j] : bc.v0bc[j];
+    botm1[j] = role ? bc.eta0m1bc[j] : bc.v0m1bc[j];
+    top[j] = role ? bc.etanbc[j] : bc.vnbc[j];
+    topp1[j] = role ? bc.etanp1bc[j] : bc.vnp1bc[j];
+  }
+  const bool wallrhs = role == 1 && is00;  // the packed wall velocity U+iW (channel.f90:122-124)
+  const double bval0 = wallrhs ? sc->u0 : 0.0, bvaln = wallrhs ? sc->uN : 0.0;
+  const AsmCoef ac = asm_coef(lambda, k2, d.ni);
+  double L1[2] = {0, 0}, L2[2] = {0, 0};
+  for (int iy = ny - 1; iy >= 1; --iy) {
+    const double* dr = der + (size_t)iy * 20;
+    // warp-uniform: each warp assembles only its own matrix; the products
+    // -ni d4 and -ni d2, the same for every mode, come from the per-row
+    // table nud when there is one
+    double A[5];
+    if (role) {
+#pragma unroll
+      for (int j = 0; j < 5; ++j) {
+        const double p2 = nud ? __ldg(nud + (size_t)iy * 10 + 5 + j) : ac.ce2 * __ldg(dr + 10 + j);
+        A[j] = fma(ac.ce0, __ldg(dr + j), p2);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 5; ++j) {
+        const double p4 = nud ? __ldg(nud + (size_t)iy * 10 + j) : ac.cv4 * __ldg(dr + 15 + j);
+        A[j] = fma(ac.cv0, __ldg(dr + j), fma(ac.cv2, __ldg(dr + 10 + j), p4));
+      }
+    }
+    if (iy == ny - 1) bc_top1(A, top, topp1);
+    if (iy == ny - 2) bc_top2(A, top);
+    if (iy == 1) bc_bot1(A, bot, botm1);
+    if (iy == 2) bc_bot2(A, bot);
+    if (wallrhs) {  // subtracted from the right-hand side of these rows by k_solve
+      if (iy == 1) { sc->wallrhs[0] = A[1] * bval0 / bot[1]; sc->wallrhs[1] = A[1] * 0.0 / bot[1]; }
+      if (iy == 2) { sc->wallrhs[2] = A[0] * bval0 / bot[1]; sc->wallrhs[3] = A[0] * 0.0 / bot[1]; }
+      if (iy == ny - 2) { sc->wallrhs[4] = A[4] * bvaln / top[3]; sc->wallrhs[5] = A[4] * 0.0 / top[3]; }
+      if (iy == ny - 1) { sc->wallrhs[6] = A[3] * bvaln / top[3]; sc->wallrhs[7] = A[3] * 0.0 / top[3]; }
+    }
+    if (iy == ny - 1) { A[3] = 0; A[4] = 0; }  // rbparmat_blocking.f90:29
+    if (iy == ny - 2) A[4] = 0;
+    lu_row(A, L1, L2);
+    L2[0] = L1[0]; L2[1] = L1[1];
+    L1[0] = A[0]; L1[1] = A[1];
+    if (iy == 1) { A[0] = 0; A[1] = 0; }  // rbparmat_blocking.f90:45
+    if (iy == 2) A[0] = 0;
+    double* f = fac + ((size_t)(iy - 1) * kFacPerRow + 5 * role) * P + q;
+    f[0] = A[0];
+    f[P] = A[1];
+    f[2 * P] = A[2];
+    f[3 * P] = A[3];
+    f[4 * P] = A[4];
+  }
+}
+
+// k_solve: four threads per pair, one per (system, mode): warp 0 (v, +kz),
+// warp 1 (v, -kz), warp 2 (eta, +kz), warp 3 (eta, -kz).  The (eta, -kz)
+// thread of the mean pair, whose mode does not exist, solves the mean
+// mode's unit-forcing response instead.  Each: LeftLU5divStep1 bottom-up and
+// LeftLU5divStep2 top-down with the factors of k_factor (rbparmat_blocking.f90:
+// 57-100), then the wall and ghost values (linsolve_blocking.inc:50-61).
+// After a block barrier the mean pair's eta thread makes the mean-flow
+// correction (:62-97), and warps 0 and 1 take v' and the u, w recovery of
+// the +kz and -kz modes (:99-103).
+__global__ void __launch_bounds__(128, 4) k_solve(double2* __restrict__ V, const double2* rhs, size_t rcs, int roff,
+                                                  const double* __restrict__ fac, const double* __restrict__ der,
+                                                  const double* __restrict__ d0lu, const double* __restrict__ yint,
+                                                  BcRows bc, Dims d, DevScalars* __restrict__ sc,
+                                                  const dd* __restrict__ lindd, int q_lo, int q_hi) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int sys = w >> 1, t = w & 1;
+  const int q = q_lo + blockIdx.x * 32 + lane;
+  const bool active = q < q_hi;
+  const int ny = d.ny, nz = d.nz;
+  const int ix = active ? q / (nz + 1) : 0;
+  const int a = active ? q - ix * (nz + 1) : 0;
+  const int nm = (a == 0) ? 1 : 2;
+  int mm[2];
+  mm[0] = ix * d.nzt + nz + a;
+  mm[1] = ix * d.nzt + nz - a;
+  const bool is00 = (ix == 0 && a == 0);
+  const double ka = ix * d.alfa0, kb = a * d.beta0;
+  const double k2 = ka * ka + kb * kb;
+  const double ni = d.ni;
+  const size_t P = d.npairs;
+  const bool ucor = active && is00 && sys == 1 && t == 1;  // unit-forcing response (linsolve_blocking.inc:62-68)
+  const bool mine = active && t < nm;
+  const int m = mm[ucor ? 0 : t];
+  const int vc = ucor ? 2 : (sys == 0 ? 1 : 0);  // field slot written
+  const bool wallrhs = mine && sys == 1 && is00;
+  double bot[5], botm1[5], top[5], topp1[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    bot[j] = sys ? bc.eta0bc[j] : bc.v0bc[j];
+    botm1[j] = sys ? bc.eta0m1bc[j] : bc.v0m1bc[j];
+    top[j] = sys ? bc.etanbc[j] : bc.vnbc[j];
+    topp1[j] = sys ? bc.etanp1bc[j] : bc.vnp1bc[j];
+  }
+  const double bval0 = wallrhs ? sc->u0 : 0.0, bvaln = wallrhs ? sc->uN : 0.0;
+  if (mine || ucor) {
+    const double* fs = fac + (size_t)5 * sys * P + q;  // this system's factors of row 1
+    const size_t frow = (size_t)kFacPerRow * P;
+    // ---- Step1 bottom-up: x = (b - u1 x(+1) - u2 x(+2)) / d ----
+    const double2* rsrc = rhs + (sys == 0 ? rcs : 0);
+    double2 x1 = cz(), x2 = cz();
+    double2 bn = ucor ? make_double2(1.0, 0.0) : rsrc[(size_t)(ny - 1 + roff) * d.nmodes + m];
+    const double* f = fs + (size_t)(ny - 2) * frow;
+    double dn = f[2 * P], u1n = f[3 * P], u2n = f[4 * P];
+    for (int iy = ny - 1; iy >= 1; --iy) {
+      double2 b = bn;
+      const double dv = dn, u1 = u1n, u2 = u2n;
+      if (iy > 1) {  // one row ahead (global-load latency)
+        if (!ucor) bn = rsrc[(size_t)(iy - 1 + roff) * d.nmodes + m];
+        f -= frow;
+        dn = f[2 * P];
+        u1n = f[3 * P];
+        u2n = f[4 * P];
+      }
+      if (wallrhs) {
+        if (iy == 1) b = b - make_double2(sc->wallrhs[0], sc->wallrhs[1]);
+        if (iy == 2) b = b - make_double2(sc->wallrhs[2], sc->wallrhs[3]);
+        if (iy == ny - 2) b = b - make_double2(sc->wallrhs[4], sc->wallrhs[5]);
+        if (iy == ny - 1) b = b - make_double2(sc->wallrhs[6], sc->wallrhs[7]);
+      }
+      double2 sacc = rmul(u1, x1);
+      sacc = sacc + rmul(u2, x2);
+      const double2 x = rmul(dv, b - sacc);
+      x2 = x1;
+      x1 = x;
+      V[vidx(d, vc, iy, m)] = x;
+    }
+    // ---- Step2 top-down: v = x - l2 v(-2) - l1 v(-1); rows 1..3 and ny-3..ny-1 kept ----
+    double2 lo[3], hi[3];
+    double2 m2 = cz(), m1 = cz();
+    f = fs;
+    double l2n = f[0], l1n = f[P];
+    double2 vn = V[vidx(d, vc, 1, m)];
+    for (int iy = 1; iy <= ny - 1; ++iy) {
+      const double l2 = l2n, l1 = l1n;
+      const double2 vcur = vn;
+      if (iy < ny - 1) {
+        f += frow;
+        l2n = f[0];
+        l1n = f[P];
+        vn = V[vidx(d, vc, iy + 1, m)];
+      }
+      const double2 nv = step2(vcur, l2, l1, m2, m1);
+      V[vidx(d, vc, iy, m)] = nv;
+      m2 = m1;
+      m1 = nv;
+      if (iy == 1) lo[0] = nv;
+      if (iy == 2) lo[1] = nv;
+      if (iy == 3) lo[2] = nv;
+      if (iy == ny - 3) hi[0] = nv;
+      if (iy == ny - 2) hi[1] = nv;
+      if (iy == ny - 1) hi[2] = nv;
+    }
+    // wall and ghost values (linsolve_blocking.inc:50-61)
+    const double2 w0 = cdivr(make_double2(bval0, 0.0) - dot3(lo, bot + 2), bot[1]);
+    const double2 rb[4] = {w0, lo[0], lo[1], lo[2]};
+    const double2 wm1 = cdivr(cz() - dot4(rb, botm1 + 1), botm1[0]);
+    const double2 wn = cdivr(make_double2(bvaln, 0.0) - dot3(hi, top), top[3]);
+    const double2 rt[4] = {hi[0], hi[1], hi[2], wn};
+    const double2 wn1 = cdivr(cz() - dot4(rt, topp1), topp1[4]);
+    V[vidx(d, vc, -1, m)] = wm1;
+    V[vidx(d, vc, 0, m)] = w0;
+    V[vidx(d, vc, ny, m)] = wn;
+    V[vidx(d, vc, ny + 1, m)] = wn1;
+  }
+  __syncthreads();  // v, eta (and the unit response) of this block's pairs are in V
+  if (wallrhs) {  // mean flow (linsolve_blocking.inc:62-97)
+    // flow rates by the non-uniform Simpson rule (dnsdata.f90:312-324)
+    double fu = 0.0, fw = 0.0, fc = 0.0;
+    for (int iy = 1, k = 0; iy <= ny - 1; iy += 2, ++k) {
+      const double a1 = yint[3 * k], a2 = yint[3 * k + 1], a3 = yint[3 * k + 2];
+      const double2 e0 = V[vidx(d, 0, iy - 1, m)], e1 = V[vidx(d, 0, iy, m)], e2 = V[vidx(d, 0, iy + 1, m)];
+      const double2 u0 = V[vidx(d, 2, iy - 1, m)], u1 = V[vidx(d, 2, iy, m)], u2 = V[vidx(d, 2, iy + 1, m)];
+      fu = fu + a1 * e0.x + a2 * e1.x + a3 * e2.x;
+      fw = fw + a1 * e0.y + a2 * e1.y + a3 * e2.y;
+      fc = fc + a1 * u0.x + a2 * u1.x + a3 * u2.x;
+    }
+    double corrpx = sc->corrpx, corrpz = sc->corrpz;
+    const bool cx = fabs(d.meanflowx) > 1.0e-7 && !d.cpi;
+    const bool cz_ = fabs(d.meanflowz) > 1.0e-7 && !d.cpi;
+    if (cx) corrpx = (d.meanflowx - fu) / fc;
+    if (cz_) corrpz = (d.meanflowz - fw) / fc;
+    for (int iy = -1; iy <= ny + 1; ++iy) {
+      const double2 et = V[vidx(d, 0, iy, m)];
+      const double uc = V[vidx(d, 2, iy, m)].x;
+      double U = et.x, W = et.y;
+      if (cx) U = U + corrpx * uc;
+      if (cz_) W = W + corrpz * uc;
+      V[vidx(d, 0, iy, m)] = make_double2(U, 0.0);
+      V[vidx(d, 2, iy, m)] = make_double2(W, 0.0);
+    }
+    sc->fr[0] = fu; sc->fr[1] = fw; sc->fr[2] = fc;
+    sc->corrpx = corrpx; sc->corrpz = corrpz;
+    if (d.cpi) {
+      if (d.cpi_type == 0) sc->meanpx = (1 - d.gamma) * 6 * ni / fu;
+      else sc->meanpx = (1.5 / d.gamma) * fu * ni;
+    }
+  }
+  if (!active || is00 || sys != 0 || t >= nm) return;
+  if (lindd) deriv_uw<dd>(V, der, d0lu, lindd, bc, d, mm[t], ka, (t == 0 ? 1.0 : -1.0) * kb, k2);
+  else deriv_uw<double>(V, der, d0lu, lindd, bc, d, mm[t], ka, (t == 0 ? 1.0 : -1.0) * kb, k2);
+}
+
 void launch_linsolve(const SolveLaunch& L, cudaStream_t s) {
   if (L.q_hi <= L.q_lo) return;
-  dim3 grid((L.q_hi - L.q_lo + 31) / 32);
-  k_linsolve<<<grid, 64, 0, s>>>(L.V, L.rhs_src, L.rhs_cstride, L.rhs_plane_off, L.fac, L.der, L.d0lu, L.yint, L.bc, L.d, L.lambda, L.ode[0],
-                                  L.lambda_from_dt, L.sc, (const dd*)L.lindd, L.nud, L.q_lo, L.q_hi);
+  const unsigned grid = (unsigned)((L.q_hi - L.q_lo + 31) / 32);
+  if (!L.split_solve) {
+    k_linsolve<<<grid, 64, 0, s>>>(L.V, L.rhs_src, L.rhs_cstride, L.rhs_plane_off, L.fac, L.der, L.d0lu, L.yint, L.bc,
+                                   L.d, L.lambda, L.ode[0], L.lambda_from_dt, L.sc, (const dd*)L.lindd, L.nud, L.q_lo,
+                                   L.q_hi);
+    return;
+  }
+  k_factor<<<grid, 64, 0, s>>>(L.fac, L.der, L.bc, L.d, L.lambda, L.ode[0], L.lambda_from_dt, L.sc, L.nud, L.q_lo,
+                               L.q_hi);
+  k_solve<<<grid, 128, 0, s>>>(L.V, L.rhs_src, L.rhs_cstride, L.rhs_plane_off, L.fac, L.der, L.d0lu, L.yint, L.bc,
+                               L.d, L.sc, (const dd*)L.lindd, L.q_lo, L.q_hi);
 }
 
 // ---------------------------------------------------------------------------
