@@ -119,6 +119,18 @@ class Mlp:
         self._check(self.lib.chgpu_mlp_train(self.h, steps, batch, C.c_float(lr), out.ctypes.data_as(_DP)))
         return out[:steps]
 
+    def save(self, path):
+        """Parameters and normalisation to an .npz file."""
+        np.savez(path, theta=self.params, **self.norm)
+
+    @classmethod
+    def load(cls, path) -> "Mlp":
+        with np.load(path) as z:
+            m = cls()
+            m.params = z["theta"]
+            m.norm = {k: z[k] for k in ("mu_in", "sd_in", "mu_out", "sd_out")}
+        return m
+
     def predict(self, feat) -> np.ndarray:
         f = _f32(feat)
         if f.ndim != 2 or f.shape[0] != NIN:

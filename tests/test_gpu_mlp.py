@@ -124,3 +124,18 @@ def test_bad_arguments_are_rejected(gpu_lib):
     bad["sd_in"] = np.zeros(10)
     with pytest.raises(ChannelError):
         m.norm = bad
+
+
+def test_save_and_load(gpu_lib, tmp_path):
+    from channel_gb300.closure import Mlp
+
+    m = make(9)
+    m.params = mo.init(21).astype(np.float32)
+    path = tmp_path / "net.npz"
+    m.save(path)
+    m2 = Mlp.load(path)
+    assert np.array_equal(m2.params, m.params)
+    for k, v in m.norm.items():
+        assert np.array_equal(m2.norm[k], v)
+    feat, _ = data(512, 2)
+    assert np.array_equal(m2.predict(feat), m.predict(feat))
