@@ -833,6 +833,13 @@ __global__ void __launch_bounds__(64, 8) k_factor(double* __restrict__ fac, cons
   }
 }
 
+// L1 prefetch of a line the thread will load some rows later (no register
+// is held for it); every address passed is inside its buffer
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+constexpr int kSolvePrefetch = 6;  // rows ahead
+
 // k_solve: four threads per pair, one per (system, mode): warp 0 (v, +kz),
 // warp 1 (v, -kz), warp 2 (eta, +kz), warp 3 (eta, -kz).  The (eta, -kz)
 // thread of the mean pair, whose mode does not exist, solves the mean
@@ -896,6 +903,13 @@ __global__ void __launch_bounds__(128, 4) k_solve(double2* __restrict__ V, const
         u1n = f[3 * P];
         u2n = f[4 * P];
       }
+      if (iy - kSolvePrefetch >= 1) {  // and the lines of a row further down
+        const double* fp = f - (size_t)(kSolvePrefetch - 1) * frow;
+        prefetch_l1(fp + 2 * P);
+        prefetch_l1(fp + 3 * P);
+        prefetch_l1(fp + 4 * P);
+        if (!ucor) prefetch_l1(rsrc + (size_t)(iy - kSolvePrefetch + roff) * d.nmodes + m);
+      }
       if (wallrhs) {
         if (iy == 1) b = b - make_double2(sc->wallrhs[0], sc->wallrhs[1]);
         if (iy == 2) b = b - make_double2(sc->wallrhs[2], sc->wallrhs[3]);
@@ -923,6 +937,12 @@ __global__ void __launch_bounds__(128, 4) k_solve(double2* __restrict__ V, const
         l2n = f[0];
         l1n = f[P];
         vn = V[vidx(d, vc, iy + 1, m)];
+      }
+      if (iy + kSolvePrefetch <= ny - 1) {
+        const double* fp = f + (size_t)(kSolvePrefetch - 1) * frow;
+        prefetch_l1(fp);
+        prefetch_l1(fp + P);
+        prefetch_l1(&V[vidx(d, vc, iy + kSolvePrefetch, m)]);
       }
       const double2 nv = step2(vcur, l2, l1, m2, m1);
       V[vidx(d, vc, iy, m)] = nv;
