@@ -652,7 +652,7 @@ def main():
     ap.add_argument("--mode", default="full", choices=["full", "timed", "long", "closure"],
                     help="timed: only the three timed runs (for profiler captures); long: --steps steps of FP64, "
                          "FP64DD and mixed from one field, Runtimedata and profile errors against FP64 over the run; "
-                         "closure: the learned closure trained and judged against the FP64 DNS")
+                         "closure: the learned closure trained and evaluated against the FP64 DNS")
     args = ap.parse_args()
     for item in filter(None, args.tiles.split("/")):
         prec, t = item.split(":")
