@@ -169,3 +169,20 @@ def test_create_without_gpu_reports_error():
     with pytest.raises(ChannelError) as e:
         Channel(dnsin.workload("small"))
     assert e.value.code in (-2, -3)
+
+
+def test_fortran_interface_binds_declared_symbols():
+    """Every BIND(C, name=...) of the Fortran interface module names a
+    function the headers declare (the module is not compiled here: no
+    gfortran), and the mirrored struct types list the C fields in order."""
+    f90 = (ROOT / "channel_gb300" / "fortran" / "chgpu_interface.f90").read_text()
+    bound = set(re.findall(r'BIND\(C,\s*name="(chgpu_\w+)"\)', f90))
+    assert len(bound) >= 20
+    assert bound <= set(header_functions()), bound - set(header_functions())
+    text = (ROOT / "include" / "chgpu.h").read_text()
+    body = re.search(r"typedef struct chgpu_params \{(.*?)\} chgpu_params;", text, re.S).group(1)
+    c_fields = re.findall(r"\b(\w+)\s*[;,]", re.sub(r"/\*.*?\*/", "", body, flags=re.S))
+    ftype = re.search(r"TYPE, BIND\(C\) :: chgpu_params(.*?)END TYPE", f90, re.S).group(1)
+    f_fields = re.findall(r"::\s*([\w, ]+)", ftype)
+    f_fields = [x.strip() for grp in f_fields for x in grp.split(",")]
+    assert [c.lower() for c in c_fields] == [f.lower() for f in f_fields], (c_fields, f_fields)
