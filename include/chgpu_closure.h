@@ -86,8 +86,10 @@ int chgpu_closure_dims(chgpu_handle* h, int dims[3]);
  * evaluates the network at the closure points of the current field and adds
  * tau_ij to the six products there (walls and ghost planes get none);
  * enable = 0 detaches it -- the plain under-resolved solver, the fallback.
- * The handle keeps the pointer: the network must outlive the attachment.
- * The next step is captured anew. */
+ * The handle keeps the pointer: the network must outlive the attachment,
+ * and must not be trained (chgpu_mlp_train / _set_params / _set_norm) while
+ * an attached handle's steps are in flight -- they read its weights on the
+ * handle's stream.  The next step is captured anew. */
 int chgpu_closure_attach(chgpu_handle* h, chgpu_mlp* m, int enable);
 
 /* A prescribed tau instead of the network: tau[6][npts] (FP32) added to the
