@@ -1,12 +1,13 @@
 """Benchmark of the channel RK3/CN time step on GB300.
 
-Headline: RK3 steps/s of the plain FP64 step on the Re_tau~180 channel
-(127x192x127 modes, 384x193x384 physical grid after 3/2 padding), with the
-mixed-precision step measured side by side from the same seeded field and its
-statistics error against FP64.  One JSON line on stdout (rank 0).
+Headline: RK3 steps/s of the plain FP64 step on the Re_tau~550 channel
+(383x384x383 modes, 1536x385x1536 physical grid after 3/2 padding), with the
+double-float and mixed-precision steps measured side by side from the same
+seeded field and their statistics error against FP64.  One JSON line on
+stdout (rank 0).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload retau180|small|retau550|coarse]
+                  [--workload retau550|retau180|small|coarse]
 
 --impl reference times the reference algorithm on the host cores.  The
 reference itself (Fortran 2008 + MPI + FFTW3) cannot be built on these
@@ -47,6 +48,19 @@ def workload_desc(p, prec: str) -> str:
     return (f"channel {p.nx}x{p.ny}x{p.nz} modes (physical {2 * p.nxd}x{p.ny + 1}x{p.nzd} with 3/2 padding), "
             f"alfa0={p.alfa0} beta0={p.beta0} Re={p.re} a={p.a}, "
             + (f"cflmax={p.cflmax} (adaptive dt)" if p.cflmax > 0 else f"fixed dt={p.deltat}") + f", {prec}")
+
+
+def bench_config(p, ws: int) -> dict:
+    """The `config` object of the JSON line, identical in both arms."""
+    field_mb = 3 * (p.nx + 1) * (2 * p.nz + 1) * (p.ny + 3) * 16 / 1e6
+    return {"workload": workload_desc(p, "FP64"), "grid_points": p.grid_points(),
+            "spectral_points": p.spectral_points(),
+            "l2": f"inputs larger than L2 (field {field_mb:.0f} MB + product spectra per step)",
+            "parallelism": f"replicas x{ws}"}
+
+
+def bench_data(seed: int, amp: float) -> str:
+    return f"synthetic: seeded perturbed-laminar field (numpy default_rng({seed}), amplitude {amp})"
 
 
 # ---------------------------------------------------------------------------
@@ -331,6 +345,11 @@ def rel(a, b):
 
 
 def cpu_baseline(p, V0, max_seconds=20.0):
+    """The oracle (the reference's algorithm restated in C, OpenMP over planes
+    and modes, every host thread) on a bounded sample of the same workload:
+    whole RK3 substeps (buildrhs over every plane, linsolve over every mode,
+    in the reference's order) after the start-up pass, until about
+    max_seconds of work; steps/s = substeps / 3 / time."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import pyoracle
 
@@ -339,15 +358,23 @@ def cpu_baseline(p, V0, max_seconds=20.0):
     o.set_field(V0)
     o.start()
     n, t = 0, 0.0
-    while n == 0 or (t + t / n <= max_seconds and n < 50):
+    while n == 0 or (t + t / n <= max_seconds and n < 150):
+        k = n % 3
         t0 = time.perf_counter()
-        o.step()
+        s = o.scalars()
+        s.time = s.time + 2.0 / pyoracle.RK[k][0] * s.deltat
+        o.set_scalars(s)
+        o.buildrhs(pyoracle.RK[k], k == 2)
+        o.linsolve(pyoracle.RK[k][0] / s.deltat)
+        if k == 2:
+            o.outstats()
         t += time.perf_counter() - t0
         n += 1
     o.close()
-    return {"value": n / t, "unit": "steps/s", "cores": threads, "kind": "port",
-            "sample": f"{n} RK3 step(s) of the same workload after start-up, oracle C restatement "
-                      f"(reference Fortran/MPI/FFTW not buildable here), OpenMP over planes and modes"}
+    return {"value": n / 3.0 / t, "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": f"{n} RK3 substep(s) (buildrhs over all {p.ny + 3} planes + linsolve over all modes) of the "
+                      f"same workload after start-up, {t:.1f} s; oracle C restatement (reference "
+                      f"Fortran/MPI/FFTW not buildable here), OpenMP over planes and modes"}
 
 
 def run_long(args):
@@ -433,11 +460,14 @@ def run_ours(args):
                 "wall_shear": float(abs(r["line"][1] - r64["line"][1]) / abs(r64["line"][1])),
                 "fields": [rel(r["V"][c], r64["V"][c]) for c in range(3)], "after_steps": W + K}
 
+    from channel_gb300.lib import measure_peaks
+
+    in_run_peaks = measure_peaks()
     peaks = measured_peaks()
     hbm_peak = peaks.get("hbm_gbs")
-    peak_src = "measured" if hbm_peak else "fallback"
+    peak_src = "measured (MEASURED_PEAKS.json)" if hbm_peak else "fallback (6.8 TB/s, no MEASURED_PEAKS.json)"
     hbm_peak = hbm_peak or 6800.0
-    fp64_peak_tflops = 1.196  # FP64 FMA throughput of GB300, measured with an FMA loop (8 chains per thread)
+    fp64_peak_tflops = in_run_peaks["fp64_tflops"]
     nprof = max(2, min(K, 10))
 
     def attribution(prec, mixed):
@@ -454,25 +484,26 @@ def run_ours(args):
     dom, per, gbs, tfl, kin64 = attribution("fp64", False)
     domd, perd, gbsd, tfld, kindd = attribution("fp64dd", False)
     domm, perm, gbsm, tflm, kinmx = attribution("mixed", True)
-    traffic = None
     tf = ROOT / "profiles" / "traffic.json"
-    if tf.exists():
-        try:
-            traffic = json.loads(tf.read_text()).get(f"{args.workload}:fp64:{dom}")
-        except Exception:
-            traffic = None
+    try:
+        traffic_tab = json.loads(tf.read_text()) if tf.exists() else {}
+    except Exception:
+        traffic_tab = {}
+
+    def traffic_of(prec, kernel):
+        return traffic_tab.get(f"{args.workload}:{prec}:{kernel}")
     e2e = e2e_run(p, V0, "fp64", min(K, 10), 2)
     ens = ensemble_run()
     cpu = cpu_baseline(p, V0) if rank == 0 else None
 
-    def variant(r, dom_, per_, gbs_, tfl_, kin_, what):
+    def variant(r, dom_, per_, gbs_, tfl_, kin_, what, prec):
         msv = r["ms"] / K
         return {"value": whole_job_steps_per_s(r["ms"], K, ws), "unit": "steps/s", "ms_per_step": msv,
                 "ns_per_pt_step": msv * 1e6 / gpts, "ns_per_spectral_pt_step": msv * 1e6 / p.spectral_points(),
                 "speedup_vs_fp64": ms64 / msv, "arithmetic": what,
                 "stats_err_vs_fp64": stats_err(r), "dominant_kernel": dom_, "kernels": kin_,
                 "roofline": {"bound": "hbm", "kernel": dom_, "achieved": gbs_, "peak": hbm_peak, "unit": "GB/s",
-                             "frac": gbs_ / hbm_peak, "traffic": None, "launch_ms": per_ * 1e3,
+                             "frac": gbs_ / hbm_peak, "traffic": traffic_of(prec, dom_), "launch_ms": per_ * 1e3,
                              "flops_tflops": tfl_}}
 
     line = {
@@ -487,27 +518,28 @@ def run_ours(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": f"synthetic: seeded perturbed-laminar field (numpy default_rng({rank}), amplitude {amp})",
-        "config": {"workload": workload_desc(p, "FP64"), "grid_points": gpts, "spectral_points": p.spectral_points(),
-                   "l2": "inputs larger than L2 (field " + f"{V0.nbytes / 1e6:.0f} MB" + " + product spectra per step)",
-                   "parallelism": f"replicas x{ws}",
-                   "tiles": {k: {"z_cols": t[0], "x_rows": t[1], "x_variant": t[2], "z_threads": t[3],
-                                 "x_threads": t[4]} for k, t in TILES.items()},
-                   "tiles_from": "--tiles" if args.tiles else "chgpu_autotune on the first handle of each precision"},
+        "data": bench_data(rank, amp),
+        "config": bench_config(p, ws),
+        "tiles": {k: {"z_cols": t[0], "x_rows": t[1], "x_variant": t[2], "z_threads": t[3],
+                      "x_threads": t[4]} for k, t in TILES.items()},
+        "tiles_from": "--tiles" if args.tiles else "chgpu_autotune on the first handle of each precision",
         "ns_per_pt_step": ms64 * 1e6 / gpts,
         "ns_per_spectral_pt_step": ms64 * 1e6 / p.spectral_points(),
         "fp64dd": variant(rdd, domd, perd, gbsd, tfld, kindd,
                           "transforms, products and nonlinear stencils in double-float (2 x FP32, ~48 bits) on the "
-                          "FP32 pipes; linear terms, banded solves, walls and mean flow FP64; meets the FP64 parity bars"),
+                          "FP32 pipes; linear terms, banded solves, walls and mean flow FP64; meets the FP64 parity bars",
+                          "fp64dd"),
         "mixed": variant(rmx, domm, perm, gbsm, tflm, kinmx,
                          "transforms, products and nonlinear stencils FP32; linear terms double-float; banded "
-                         "solves, walls and mean flow FP64"),
+                         "solves, walls and mean flow FP64", "mixed"),
         "ensemble": ens,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": gbs / hbm_peak, "traffic": traffic, "peak_source": peak_src,
+                     "frac": gbs / hbm_peak, "traffic": traffic_of("fp64", dom), "peak_source": peak_src,
                      "launch_ms": per * 1e3,
                      "fp64": {"achieved": tfl, "peak": fp64_peak_tflops, "unit": "TFLOP/s", "frac": tfl / fp64_peak_tflops,
+                              "peak_source": "measured in this run (chgpu_measure_peaks: FP64 FMA loop, CUDA events)",
                               "note": "the FP64 pipe binds this kernel; the HBM fraction is low by design"}},
+        "peaks_in_run": in_run_peaks,
         "kernels": kin64,
         "e2e": {"value": min(K, 10) / e2e["s"] * ws, "unit": "steps/s", "h2d_bytes_per_step": e2e["h2d"],
                 "d2h_bytes_per_step": e2e["d2h"]},
@@ -524,6 +556,12 @@ def run_ours(args):
 
 
 def run_reference(args):
+    """The reference arm: the oracle (the reference's algorithm restated in
+    C; the reference's Fortran/MPI/FFTW build is impossible on these
+    machines) on every host core, from the same seeded field as the GPU arm,
+    whole RK3 steps after the start-up pass and one untimed step.  At sizes
+    where a step takes tens of seconds it times as many of the requested
+    steps as fit a ~2 minute budget and reports that count as `steps`."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
@@ -533,7 +571,8 @@ def run_reference(args):
     import pyoracle
 
     p = dnsin.workload(args.workload)
-    V0 = initial.perturbed_laminar(p, AMPLITUDE[args.workload], seed=0)
+    amp = AMPLITUDE[args.workload]
+    V0 = initial.perturbed_laminar(p, amp, seed=0)
     threads = os.cpu_count() or 1
     o = pyoracle.Oracle(p, nthreads=threads)
     o.set_field(V0)
@@ -541,7 +580,7 @@ def run_reference(args):
     t0 = time.perf_counter()
     o.step()
     t_one = time.perf_counter() - t0
-    budget = 150.0
+    budget = 120.0
     W = max(0, min(args.warmup - 1, int(budget / 4 / max(t_one, 1e-9))))
     for _ in range(W):
         o.step()
@@ -556,14 +595,14 @@ def run_reference(args):
         "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": ws, "steps": K, "steps_requested": args.steps,
         "warmup": W + 1, "ms_per_step": 1000.0 * t / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic: seeded perturbed-laminar field (numpy default_rng(0))",
-        "config": {"workload": workload_desc(p, "FP64"), "grid_points": p.grid_points(),
-                   "spectral_points": p.spectral_points()},
+        "data": bench_data(0, amp),
+        "config": bench_config(p, ws),
         "ns_per_pt_step": 1e9 * t / K / p.grid_points(),
         "impl": "reference",
         "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{K} RK3 steps after start-up; the reference Fortran/MPI/FFTW build is not "
-                                   f"possible here (no gfortran, MPI or FFTW), so its C restatement runs"},
+                         "sample": f"{K} whole RK3 step(s) after start-up and {W + 1} untimed; the reference "
+                                   f"Fortran/MPI/FFTW build is not possible here (no gfortran, MPI or FFTW), so "
+                                   f"its C restatement runs, OpenMP over planes and modes"},
         "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -644,7 +683,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="retau180", choices=list(AMPLITUDE))
+    ap.add_argument("--workload", default="retau550", choices=list(AMPLITUDE))
     ap.add_argument("--tiles", default="",
                     help="fixed transform tiles instead of autotuning, e.g. fp64:8,4,2,256,256/mixed:8,4,3,256,192 "
                          "(z columns, x rows, x-row variant, z threads, x threads; for reproducible profiler "

@@ -46,14 +46,11 @@ static __device__ __align__(256) double g_noalloc_tables[kTableDoubles];
 static __device__ __align__(256) chgpu::DevScalars g_noalloc_scalars;
 
 struct DeviceAddresses {
-  bool ready = false;
   double* factors = nullptr;
   double* tables = nullptr;
   chgpu::DevScalars* scalars = nullptr;
 };
-constexpr int kMaxDevices = 64;
-DeviceAddresses g_addr[kMaxDevices];
-std::mutex g_mutex;         // guards g_addr and the host staging below
+std::mutex g_mutex;         // guards the host staging below
 StaticTables g_host_tables;  // host staging of the tables (no heap)
 double g_host_pack[kTableDoubles];
 thread_local char* g_err = nullptr;  // the caller's message buffer, if any
@@ -69,21 +66,18 @@ int cuda_error(cudaError_t e, const char* where) {
   return CHGPU_E_CUDA;
 }
 
-// Host code cannot use the arrays' names as device addresses: resolve them
-// once per device, with that device current.
-int resolve_addresses(int dev, DeviceAddresses** out) {
-  if (dev < 0 || dev >= kMaxDevices) return error(CHGPU_E_PARAM, "chgpu_linsolve_noalloc: device ordinal out of range");
-  DeviceAddresses& a = g_addr[dev];
-  if (!a.ready) {
-    cudaError_t e = cudaGetSymbolAddress((void**)&a.factors, g_noalloc_factors);
-    if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(factors)");
-    e = cudaGetSymbolAddress((void**)&a.tables, g_noalloc_tables);
-    if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(tables)");
-    e = cudaGetSymbolAddress((void**)&a.scalars, g_noalloc_scalars);
-    if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(scalars)");
-    a.ready = true;
-  }
-  *out = &a;
+// Host code cannot use the arrays' names as device addresses: they are
+// resolved with the caller's device current, on every call (a lookup, no
+// allocation), so that a context torn down and created again -- where the
+// module, and with it the arrays, may be loaded at other addresses -- is
+// never handed stale pointers.
+int resolve_addresses(DeviceAddresses* a) {
+  cudaError_t e = cudaGetSymbolAddress((void**)&a->factors, g_noalloc_factors);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(factors)");
+  e = cudaGetSymbolAddress((void**)&a->tables, g_noalloc_tables);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(tables)");
+  e = cudaGetSymbolAddress((void**)&a->scalars, g_noalloc_scalars);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(scalars)");
   return 0;
 }
 
@@ -108,12 +102,11 @@ extern "C" int chgpu_linsolve_noalloc(const chgpu_params* p, double lambda, doub
     return CHGPU_E_PARAM;
   }
   std::lock_guard<std::mutex> lock(g_mutex);
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
-  DeviceAddresses* a = nullptr;
-  int rc = resolve_addresses(dev, &a);
+  DeviceAddresses addr;
+  DeviceAddresses* a = &addr;
+  int rc = resolve_addresses(a);
   if (rc) return rc;
+  cudaError_t e = cudaSuccess;
   StaticTables& t = g_host_tables;
   if (!chgpu::compute_tables_static(*p, t)) return error(CHGPU_E_PARAM, "chgpu_linsolve_noalloc: bad ny");
   const int ny = p->ny;

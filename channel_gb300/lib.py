@@ -103,6 +103,7 @@ SIGNATURES = {
     "chgpu_snapshot_wait": (C.c_int, [_P, C.POINTER(_DP)]),
     "chgpu_linsolve_noalloc": (C.c_int, [C.POINTER(Params), C.c_double, C.c_void_p, _DP, C.c_void_p,
                                          C.c_char_p, C.c_size_t]),
+    "chgpu_measure_peaks": (C.c_int, [_DP, _DP, _DP, C.c_char_p, C.c_size_t]),
     # include/chgpu_closure.h
     "chgpu_mlp_create": (C.c_int, [C.c_ulonglong, C.POINTER(C.c_void_p)]),
     "chgpu_mlp_destroy": (C.c_int, [_P]),
@@ -147,6 +148,21 @@ def load_library():
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+def measure_peaks(copy: bool = True) -> dict:
+    """FP64 / FP32 FMA throughput (TFLOP/s) and device copy rate (GB/s) of
+    the current device (chgpu_measure_peaks)."""
+    L = load_library()
+    f64, f32, cp = C.c_double(), C.c_double(), C.c_double()
+    err = C.create_string_buffer(256)
+    rc = L.chgpu_measure_peaks(C.byref(f64), C.byref(f32), C.byref(cp) if copy else None, err, 256)
+    if rc != 0:
+        raise ChannelError(rc, err.value.decode())
+    out = {"fp64_tflops": f64.value, "fp32_tflops": f32.value}
+    if copy:
+        out["copy_gbs"] = cp.value
+    return out
 
 
 def params_struct(p: DnsIn, precision: int = FP64) -> Params:

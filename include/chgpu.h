@@ -237,6 +237,15 @@ const char* chgpu_kernel_kind_name(int kind);
 /* Kernel launches issued by the handle since creation (for accounting). */
 long long chgpu_launch_count(const chgpu_handle* h);
 
+/* Throughput of the current device, for reporting kernels against the roofs
+ * they are bound by: FP64 and FP32 fused multiply-add rates (TFLOP/s, FMA =
+ * 2 flops; 8 independent FMA chains per thread, 8 blocks of 256 threads per
+ * SM, CUDA events) and a device-to-device copy of 1 GiB (GB/s, read + write
+ * bytes).  Any output may be NULL (that measurement is skipped).  Temporarily
+ * allocates 2 GiB when copy_gbs is requested.  No counterpart in the
+ * reference (its `chron` flag times whole steps only). */
+int chgpu_measure_peaks(double* fp64_tflops, double* fp32_tflops, double* copy_gbs, char* err, size_t errlen);
+
 /* The implicit solve of linsolve (linsolve_blocking.inc:3-107) for callers
  * that cannot allocate device memory.  No counterpart in the reference: it
  * exists for hosts that own every byte of device memory themselves (a fixed
@@ -249,21 +258,22 @@ long long chgpu_launch_count(const chgpu_handle* h);
  *           entry components 1 and 2 hold, for iy=1..ny-1, the eta and v
  *           right-hand sides buildrhs leaves there; on return it holds the
  *           solved u, v, w (all rows), exactly as chgpu_linsolve leaves V.
- *   scalars in/out, 7 doubles: [0..2] flow rates fr (out), [3] corrpx and
- *           [4] corrpz (in: previous values, out: new), [5] meanpx (in/out,
- *           updated under CPI), [6] meanpz (in).
+ *   scalars in/out, host memory, 7 doubles: [0..2] flow rates fr (out),
+ *           [3] corrpx and [4] corrpz (in: previous values, out: new),
+ *           [5] meanpx (in/out, updated under CPI), [6] meanpz (in).
  *   stream  cudaStream_t to run on (NULL: legacy default stream); the call
- *           returns after the stream has finished the solve.
+ *           copies tables and scalars from host memory on it and returns
+ *           after the stream has finished the solve.
  *   err     optional buffer for a message when the call fails.
  * The kernel's scratch (the factors of the two pentadiagonal systems), the
  * wall-normal tables and the scalars live in file-scope device arrays of the
  * library: CHGPU_NOALLOC_SCRATCH_BYTES of factor scratch (enough for
  * 4*(ny-1)*(nx+1)*(nz+1) doubles), ny <= CHGPU_NOALLOC_MAX_NY; larger sizes
  * are rejected with CHGPU_E_PARAM and a message.  Every GPU that loads the
- * library holds these arrays until the process exits.  The first call on
- * each device resolves their device addresses, so make that first call
- * before any stream capture.  All calls share the arrays: calls that overlap
- * on the GPU race; each call rewrites every word it later reads. */
+ * library holds these arrays until the process exits.  Each call looks up
+ * their device addresses on the current device.  All calls share the
+ * arrays: calls that overlap on the GPU race; each call rewrites every word
+ * it later reads. */
 #define CHGPU_NOALLOC_SCRATCH_BYTES (64ull << 20)
 #define CHGPU_NOALLOC_MAX_NY 1024
 int chgpu_linsolve_noalloc(const chgpu_params* p, double lambda, double* field, double* scalars, void* stream,

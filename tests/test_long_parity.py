@@ -1,0 +1,171 @@
+"""Parity of the CUDA step with the CPU oracle at the workloads' own sizes and
+run lengths (through the C ABI, FP64 and double-float paths), and of the
+mixed path with FP64 at 383x384x383.
+
+* 127x192x127 (Re_tau~180, adaptive dt): 10 steps against the oracle run
+  here, per-field relative L2 <= 1e-10.
+* 383x384x383 (Re_tau~550, adaptive dt): 1 step against the oracle run here,
+  per-field relative L2 <= 1e-12.
+* 32x64x32: all 200 steps of the workload against the committed oracle
+  fixture tests/golden/small_seed0.npz (Runtimedata lines and the final mean
+  and rms profiles).
+* 127x192x127: all 2000 steps against the committed oracle fixture
+  tests/golden/retau180_seed0.npz: the Runtimedata statistics the
+  correctness statement names -- wall shear (dU/dy, dW/dy at both walls),
+  bulk velocity (the flow rate over the channel height), pressure gradient,
+  and the adaptive time step -- and the final mean and rms profiles.
+* 383x384x383: mixed precision against FP64 over 100 steps from the same
+  field, mean profile, rms profiles and wall shear <= 1e-4 relative.
+
+The fixtures are made by tests/golden/make_golden.py.  These tests are the
+slowest of the suite and sit after the others in collection order.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from helpers import line_close, per_field_rel, profiles, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def oracle_run(name, amp, nsteps):
+    """Field and Runtimedata line of the oracle after nsteps steps."""
+    import pyoracle
+    from channel_gb300 import dnsin, initial
+
+    p = dnsin.workload(name)
+    V0 = initial.perturbed_laminar(p, amp, 0)
+    o = pyoracle.Oracle(p)
+    o.set_field(V0)
+    lines = [o.start()]
+    for _ in range(nsteps):
+        lines.append(o.step())
+    V = o.field()
+    o.close()
+    return p, V0, V, np.array(lines)
+
+
+def gpu_run(p, V0, prec, nsteps, keep_lines=True):
+    from channel_gb300 import Channel
+
+    with Channel(p, prec) as g:
+        g.upload(V0)
+        lines = [g.start()]
+        for _ in range(nsteps):
+            ln = g.step(sync=keep_lines)
+            if keep_lines:
+                lines.append(ln)
+        g.synchronize()
+        if not keep_lines:
+            lines.append(g.stats().line)
+        V = g.download()
+    return V, np.array(lines)
+
+
+@pytest.fixture(scope="module")
+def retau180_oracle_10():
+    return oracle_run("retau180", 0.05, 10)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp64dd"])
+def test_retau180_ten_steps(gpu_lib, retau180_oracle_10, prec):
+    p, V0, Vo, lo = retau180_oracle_10
+    V, lg = gpu_run(p, V0, prec, 10)
+    e = per_field_rel(V, Vo)
+    assert max(e) <= 1e-10, e
+    for s in range(11):
+        ok, err = line_close(lg[s], lo[s], 1e-9)
+        assert ok, (s, err, lg[s], lo[s])
+
+
+def check_lines(lg, lo, groups):
+    """Largest deviation over the run of each Runtimedata group, measured in
+    the group's own norm at each step (vector quantities: wall shear,
+    flow rate, pressure gradient)."""
+    worst = {}
+    for name, cols, tol in groups:
+        scale = np.maximum(np.abs(lo[:, cols]).max(axis=1), 1e-300)
+        err = float((np.abs(lg[:, cols] - lo[:, cols]).max(axis=1) / scale).max())
+        worst[name] = err
+        assert err <= tol, (name, err, tol)
+    return worst
+
+
+def test_small_two_hundred_steps(gpu_lib):
+    from channel_gb300 import dnsin, initial
+
+    g = np.load(GOLD / "small_seed0.npz")
+    p = dnsin.workload("small")
+    V, lg = gpu_run(p, initial.perturbed_laminar(p, 0.01, 0), "fp64", 200)
+    assert lg.shape == g["lines"].shape == (201, 11)
+    check_lines(lg, g["lines"], [("time", [0], 1e-13), ("wall shear", [1, 2, 3, 4], 1e-10),
+                                 ("flow rate", [5, 7], 1e-11), ("dp/dx", [6, 8], 1e-9),
+                                 ("cfl*dt", [9], 1e-9)])
+    U, rms = profiles(V)
+    assert rel_l2(U, g["U"]) <= 1e-11
+    for c in range(3):
+        assert rel_l2(rms[c], g["rms"][c]) <= 1e-9, c
+
+
+def test_retau550_one_step(gpu_lib):
+    """The 383x384x383 workload: one adaptive step of the FP64 path against
+    the oracle (the oracle takes about a minute on 16 cores)."""
+    p, V0, Vo, lo = oracle_run("retau550", 0.05, 1)
+    V, lg = gpu_run(p, V0, "fp64", 1)
+    e = per_field_rel(V, Vo)
+    del V, Vo
+    assert max(e) <= 1e-12, e
+    for s in range(2):
+        ok, err = line_close(lg[s], lo[s], 1e-10)
+        assert ok, (s, err, lg[s], lo[s])
+
+
+# Over 2000 steps the flow leaves the laminar state (the wall shear grows
+# several-fold) and any two FP64 evaluation orders drift apart by the
+# amplification of rounding; the bars are set two orders of magnitude above
+# what the double-float path's drift from FP64 reaches over the same run.
+LONG_GROUPS = [("time", [0], 1e-11), ("wall shear", [1, 2, 3, 4], 1e-8), ("bulk velocity", [5, 7], 1e-10),
+               ("pressure gradient", [6, 8], 1e-7), ("dt", [10], 1e-8)]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp64dd"])
+def test_retau180_two_thousand_steps(gpu_lib, prec):
+    from channel_gb300 import dnsin, initial
+
+    f = GOLD / "retau180_seed0.npz"
+    g = np.load(f)
+    p = dnsin.workload("retau180")
+    V, lg = gpu_run(p, initial.perturbed_laminar(p, 0.05, 0), prec, 2000)
+    lo = g["lines"]
+    assert lg.shape == lo.shape == (2001, 11)
+    check_lines(lg, lo, LONG_GROUPS)
+    U, rms = profiles(V)
+    assert rel_l2(U, g["U"]) <= 1e-8
+    for c in range(3):
+        assert rel_l2(rms[c], g["rms"][c]) <= 1e-7, c
+
+
+def test_retau550_mixed_vs_fp64_hundred_steps(gpu_lib):
+    """Mixed precision (FP32 transforms, products and nonlinear stencils) and
+    FP64 stepped 100 times from the same 383x384x383 field: mean profile, rms
+    profiles of u, v, w and the wall shear within 1e-4 relative, at every
+    step for the wall shear."""
+    from channel_gb300 import dnsin, initial
+
+    p = dnsin.workload("retau550")
+    V0 = initial.perturbed_laminar(p, 0.05, 0)
+    V64, l64 = gpu_run(p, V0, "fp64", 100)
+    U64, r64 = profiles(V64)
+    del V64
+    Vm, lm = gpu_run(p, V0, "mixed", 100)
+    Um, rm = profiles(Vm)
+    del Vm
+    assert rel_l2(Um, U64) <= 1e-4
+    for c in range(3):
+        assert rel_l2(rm[c], r64[c]) <= 1e-4, c
+    ws = np.abs(lm[:, 1:5] - l64[:, 1:5]).max(axis=1) / np.abs(l64[:, 1:5]).max(axis=1)
+    assert float(ws.max()) <= 1e-4, float(ws.max())
