@@ -23,6 +23,7 @@
 #include "../../include/chgpu_closure.h"
 #include "chgpu_internal.h"
 #include "kernels.cuh"
+#include "rfft.cuh"
 #include "mlp.cuh"
 
 using namespace chgpu;
@@ -86,6 +87,11 @@ struct chgpu_handle {
   void* twz = nullptr;
   void* twx = nullptr;
   void* twh = nullptr;
+  // register-blocked transform kernels (convf.cu), used for the lengths with
+  // a compile-time plan: their per-pass twiddle tables
+  void* twzr = nullptr;
+  void* twxr = nullptr;
+  bool zfast = false, xfast = false;
   DevScalars* sc = nullptr;
   DevScalars* sc_host = nullptr;  // pinned
   cudaGraphExec_t graph = nullptr;
@@ -262,6 +268,31 @@ int upload_pack_roots(chgpu_handle* h, void** dst, int n, long double scale) {
   return 0;
 }
 
+// per-pass twiddles of a register-blocked plan (rfft.cuh): pass p >= 1 at
+// rplan_twoff(p), R-1 forward roots w_{Ns R}^{r k} (r = 1..R-1) per k < Ns
+template <typename V2>
+int upload_rplan_twiddles(chgpu_handle* h, void** dst, int n) {
+  using T = decltype(V2::x);
+  int E = 0, TPR = 0;
+  if (!rlen_plan(n, &E, &TPR)) return 0;
+  const int np = rplan_passes(E, TPR);
+  std::vector<V2> w(std::max(1, rplan_twsize(E, TPR)));
+  for (int p = 1; p < np; ++p) {
+    const int R = rplan_radix(E, TPR, p), Ns = rplan_ns(E, TPR, p), off = rplan_twoff(E, TPR, p);
+    for (int k = 0; k < Ns; ++k)
+      for (int r = 1; r < R; ++r) {
+        const long double ang = 2.0L * 3.14159265358979323846264338327950288L * (long double)(r * k) /
+                                (long double)(Ns * R);
+        V2& e = w[off + k * (R - 1) + r - 1];
+        e.x = from_ld<T>(cosl(ang));
+        e.y = from_ld<T>(-sinl(ang));
+      }
+  }
+  CK(h, cudaMalloc(dst, sizeof(V2) * w.size()));
+  CK(h, cudaMemcpy(*dst, w.data(), sizeof(V2) * w.size(), cudaMemcpyHostToDevice));
+  return 0;
+}
+
 cudaEvent_t take_event(chgpu_handle* h) {
   if (!h->ev_pool.empty()) {
     cudaEvent_t e = h->ev_pool.back();
@@ -313,6 +344,10 @@ ConvLaunch conv_launch(chgpu_handle* h, int compute_cfl, int products, int plane
   L.nplanes = nplanes;
   L.compute_cfl = compute_cfl;
   L.products = products;
+  L.twzr = h->twzr;
+  L.twxr = h->twxr;
+  L.zfast = h->zfast;
+  L.xfast = h->xfast;
   return L;
 }
 
@@ -502,7 +537,7 @@ void release(chgpu_handle* h) {
   }
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   void* bufs[] = {h->V, h->F, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->derT, h->derL, h->cst, h->d0lu, h->nud, h->lindd, h->yint, h->dy,
-                  h->twz, h->twx, h->twh, h->sc, h->ex_W, h->ex_P, h->ex_out, h->ex_twz, h->ex_twx,
+                  h->twz, h->twx, h->twh, h->twzr, h->twxr, h->sc, h->ex_W, h->ex_P, h->ex_out, h->ex_twz, h->ex_twx,
                   h->cl_G, h->cl_Z, h->cl_P, h->cl_tau, h->cl_wd, h->cl_twz, h->cl_twx, h->cl_twh};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -570,6 +605,11 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
   // z ones lose occupancy to its registers)
   Radix rz = make_radix(nzd, false), rx = make_radix(nxd, h->prec == CHGPU_MIXED);
   if (rz.nst < 0 || rx.nst < 0) { delete h; return fail(nullptr, CHGPU_E_PARAM, "unsupported FFT length"); }
+  {
+    int e_ = 0, tpr_ = 0;
+    h->zfast = rlen_plan(nzd, &e_, &tpr_);
+    h->xfast = rlen_plan(nxd, &e_, &tpr_) && nxd <= 768;
+  }
   h->halves = d.npairs >= 65536 ? 2 : 1;
   h->split_solve = d.npairs < 65536;
   h->rz.n = rz.n; h->rz.nst = rz.nst; std::memcpy(h->rz.r, rz.r, sizeof rz.r);
@@ -630,18 +670,24 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
       if ((rc = upload_stage_twiddles<float2>(h, &h->twz, h->rz))) break;
       if ((rc = upload_stage_twiddles<float2>(h, &h->twx, h->rx))) break;
       if ((rc = upload_pack_roots<float2>(h, &h->twh, 2 * nxd, 0.5L * (long double)d.factor))) break;
+      if ((rc = upload_rplan_twiddles<float2>(h, &h->twzr, nzd))) break;
+      if ((rc = upload_rplan_twiddles<float2>(h, &h->twxr, nxd))) break;
       if ((rc = upload_derT<float>(h))) break;
       if ((rc = upload_derL<dd>(h))) break;
     } else if (h->prec == CHGPU_FP64DD) {
       if ((rc = upload_stage_twiddles<cdd>(h, &h->twz, h->rz))) break;
       if ((rc = upload_stage_twiddles<cdd>(h, &h->twx, h->rx))) break;
       if ((rc = upload_pack_roots<cdd>(h, &h->twh, 2 * nxd, 0.5L * (long double)d.factor))) break;
+      if ((rc = upload_rplan_twiddles<cdd>(h, &h->twzr, nzd))) break;
+      if ((rc = upload_rplan_twiddles<cdd>(h, &h->twxr, nxd))) break;
       if ((rc = upload_derT<dd>(h))) break;
       if ((rc = upload_derL<double>(h))) break;
     } else {
       if ((rc = upload_stage_twiddles<double2>(h, &h->twz, h->rz))) break;
       if ((rc = upload_stage_twiddles<double2>(h, &h->twx, h->rx))) break;
       if ((rc = upload_pack_roots<double2>(h, &h->twh, 2 * nxd, 0.5L * (long double)d.factor))) break;
+      if ((rc = upload_rplan_twiddles<double2>(h, &h->twzr, nzd))) break;
+      if ((rc = upload_rplan_twiddles<double2>(h, &h->twxr, nxd))) break;
       if ((rc = upload_derT<double>(h))) break;
       if ((rc = upload_derL<double>(h))) break;
     }
@@ -1092,15 +1138,19 @@ int chgpu_autotune(chgpu_handle* h) {
     *t = m0 + m2;
     return 0;
   };
-  h->zthreads = 256;
-  for (int zc = 1; zc <= 8; zc *= 2) {
-    if (conv_zinv_smem(zc, nzd, h->d.nzt, ts) > lim) break;
-    h->zcols = zc;
-    if (int rc = time_z(&ms)) return rc;
-    if (ms < best) {
-      best = ms;
-      best_z = zc;
-    }
+  // the register-blocked kernels have compile-time tiles; the generic
+  // kernels' tiles are tuned where those run (switching between the two
+  // would change the rounding of the step, so the tuner keeps the choice)
+  if (!h->zfast) {
+    h->zthreads = 256;
+    for (int zc = 1; zc <= 8; zc *= 2) {
+      if (conv_zinv_smem(zc, nzd, h->d.nzt, ts) > lim) break;
+      h->zcols = zc;
+      if (int rc = time_z(&ms)) return rc;
+      if (ms < best) {
+        best = ms;
+        best_z = zc;
+      }
   }
   h->zcols = best_z;
   int best_zt = 256;
@@ -1113,34 +1163,37 @@ int chgpu_autotune(chgpu_handle* h) {
     }
   }
   h->zthreads = best_zt;
+  }
   // rows per block and register-cap variant of the x-row kernel, then its block size
-  int best_r = h->xrows, best_b = h->xminb;
-  best = 1e30f;
-  h->xthreads = 256;
-  for (int xb = 1; xb <= 3; ++xb)
-    for (int xr = 1; xr <= 4; xr *= 2) {
-      if (nzd % xr != 0 || conv_x_smem(xr, nxd, ts) > lim) continue;
-      h->xrows = xr;
-      h->xminb = xb;
+  if (!h->xfast) {
+    int best_r = h->xrows, best_b = h->xminb;
+    best = 1e30f;
+    h->xthreads = 256;
+    for (int xb = 1; xb <= 3; ++xb)
+      for (int xr = 1; xr <= 4; xr *= 2) {
+        if (nzd % xr != 0 || conv_x_smem(xr, nxd, ts) > lim) continue;
+        h->xrows = xr;
+        h->xminb = xb;
+        if (int rc = time_conv_stage(h, 1, reps, &ms)) return rc;
+        if (ms < best) {
+          best = ms;
+          best_r = xr;
+          best_b = xb;
+        }
+      }
+    h->xrows = best_r;
+    h->xminb = best_b;
+    int best_xt = 256;
+    for (int xt : {128, 192}) {
+      h->xthreads = xt;
       if (int rc = time_conv_stage(h, 1, reps, &ms)) return rc;
       if (ms < best) {
         best = ms;
-        best_r = xr;
-        best_b = xb;
+        best_xt = xt;
       }
-    }
-  h->xrows = best_r;
-  h->xminb = best_b;
-  int best_xt = 256;
-  for (int xt : {128, 192}) {
-    h->xthreads = xt;
-    if (int rc = time_conv_stage(h, 1, reps, &ms)) return rc;
-    if (ms < best) {
-      best = ms;
-      best_xt = xt;
-    }
   }
   h->xthreads = best_xt;
+  }
   h->tuned = true;
   ++h->version;
   if (h->graph) {  // the captured step holds the old launch shapes
@@ -1158,13 +1211,17 @@ int chgpu_set_tiles(chgpu_handle* h, const int tiles[CHGPU_NTILES]) {
   const size_t ts = tsize(h), lim = (size_t)optin - 1024;
   const int zc = tiles[0], xr = tiles[1], xb = tiles[2], zt = tiles[3], xt = tiles[4];
   auto threads_ok = [](int t) { return t >= 64 && t <= 256 && t % 32 == 0; };
-  if (zc < 1 || zc > 8 || conv_zinv_smem(zc, h->d.nzd, h->d.nzt, ts) > lim || (xr != 1 && xr != 2 && xr != 4) ||
-      h->d.nzd % xr != 0 || conv_x_smem(xr, h->d.nxd, ts) > lim || xb < 1 || xb > 3 || !threads_ok(zt) ||
-      !threads_ok(xt))
+  int e_ = 0, tpr_ = 0;
+  const bool zplan = rlen_plan(h->d.nzd, &e_, &tpr_), xplan = rlen_plan(h->d.nxd, &e_, &tpr_) && h->d.nxd <= 768;
+  if ((zc == 0 && !zplan) || (zc != 0 && (zc < 1 || zc > 8 || conv_zinv_smem(zc, h->d.nzd, h->d.nzt, ts) > lim)) ||
+      (xr != 1 && xr != 2 && xr != 4) || h->d.nzd % xr != 0 || conv_x_smem(xr, h->d.nxd, ts) > lim ||
+      (xb == 0 && !xplan) || xb < 0 || xb > 3 || !threads_ok(zt) || !threads_ok(xt))
     return fail(h, CHGPU_E_PARAM, "chgpu_set_tiles: tiles outside what this handle's sizes allow");
-  h->zcols = zc;
+  h->zfast = zc == 0;
+  if (zc != 0) h->zcols = zc;
   h->xrows = xr;
-  h->xminb = xb;
+  h->xfast = xb == 0;
+  if (xb != 0) h->xminb = xb;
   h->zthreads = zt;
   h->xthreads = xt;
   ++h->version;
@@ -1190,9 +1247,9 @@ int chgpu_set_step_halves(chgpu_handle* h, int halves) {
 
 int chgpu_tiles(const chgpu_handle* h, int tiles[CHGPU_NTILES]) {
   if (!h || !tiles) return CHGPU_E_PARAM;
-  tiles[0] = h->zcols;
+  tiles[0] = h->zfast ? 0 : h->zcols;
   tiles[1] = h->xrows;
-  tiles[2] = h->xminb;
+  tiles[2] = h->xfast ? 0 : h->xminb;
   tiles[3] = h->zthreads;
   tiles[4] = h->xthreads;
   return 0;

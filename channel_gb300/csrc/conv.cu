@@ -334,6 +334,9 @@ void launch_convolutions(const ConvLaunch& L, cudaStream_t s, int stage) {
   using V2 = typename C2<T>::t;
   const Dims& d = L.d;
   const int nxp = d.nx + 1;
+  // lengths with a register-blocked plan (the closure's stresses go through
+  // the x-row kernel below)
+  if ((stage == 1 ? (L.xfast && !L.tau) : L.zfast) && launch_convolutions_r<T>(L, s, stage)) return;
   if (stage == 0) {
     const int ncol = L.ix_hi - L.ix_lo;
     dim3 grid((ncol + L.zcols - 1) / L.zcols, L.nplanes, 3);
@@ -408,7 +411,9 @@ cudaError_t conv_set_smem_limits() {
   if ((e = allow_max_smem(k_xrow<float, 2, true>, optin))) return e;
   if ((e = allow_max_smem(k_xrow<dd, 2, true>, optin))) return e;
   if ((e = allow_max_smem(k_xphys<float>, optin))) return e;
-  return allow_max_smem(k_xrow<dd, 3>, optin);
+  if ((e = convr_set_smem_limits<float>())) return e;
+  if ((e = convr_set_smem_limits<double>())) return e;
+  return convr_set_smem_limits<dd>();
 }
 
 }  // namespace chgpu

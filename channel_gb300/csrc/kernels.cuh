@@ -48,11 +48,26 @@ struct ConvLaunch {
   int compute_cfl;
   int products;  // 0: stop after the x pass (the start-up CFL pass)
   const float2* tau;  // closure stresses added to the products, or null
+  // register-blocked kernels (convf.cu) for the lengths with a compile-time
+  // plan: their twiddle tables, and whether they run the z / x stages
+  const void* twzr;
+  const void* twxr;
+  int zfast, xfast;
 };
 
 // stage 0: z-inverse, 1: x rows, 2: z-forward
 template <typename T> void launch_convolutions(const ConvLaunch& L, cudaStream_t s, int stage);
 cudaError_t conv_set_smem_limits();
+// the register-blocked stage kernels; false when the stage's length has no plan
+template <typename T> bool launch_convolutions_r(const ConvLaunch& L, cudaStream_t s, int stage);
+template <typename T> cudaError_t convr_set_smem_limits();
+// defined in convf_f32.cu, convf_f64.cu, convf_dd.cu
+template <> bool launch_convolutions_r<float>(const ConvLaunch& L, cudaStream_t s, int stage);
+template <> bool launch_convolutions_r<double>(const ConvLaunch& L, cudaStream_t s, int stage);
+template <> bool launch_convolutions_r<dd>(const ConvLaunch& L, cudaStream_t s, int stage);
+template <> cudaError_t convr_set_smem_limits<float>();
+template <> cudaError_t convr_set_smem_limits<double>();
+template <> cudaError_t convr_set_smem_limits<dd>();
 // dynamic shared memory of the z-transform and x-row kernels (padded buffers)
 size_t conv_z_smem(int zcols, int nzd, size_t ts);                     // z-forward
 size_t conv_zinv_smem(int zcols, int nzd, int nzt, size_t ts);         // z-inverse (raw field copy)

@@ -1,0 +1,224 @@
+// Register-blocked Stockham FFT with compile-time lengths, the core of the
+// transform kernels for the lengths the workloads use (32 ... 1536).
+//
+// A length N = E * TPR transform belongs to a group of TPR consecutive
+// threads; thread t of the group holds the E elements x[t + TPR e] in
+// registers.  Pass 1 is one radix-E register DFT per thread (its inputs are
+// exactly the thread's own elements, at stride TPR).  Every later pass, of
+// radix R dividing E, does E/R butterflies per thread: butterfly j = t +
+// TPR i (i < E/R) takes x[j + r N/R] = the thread's element i + r E/R,
+// multiplies by w_{Ns R}^{r k} (k = j mod Ns, Ns the product of the earlier
+// radices), transforms in registers and writes its outputs to
+// (j - k) R + k + r Ns of the group's shared-memory buffer; after a group
+// barrier each thread reads back x'[t + TPR e].  Each pass thus costs one
+// shared-memory store and one load per element, and no index arithmetic
+// beyond compile-time constants.  The output of the last pass is in natural
+// order at j + r Ns (j < Ns), consecutive over the group's threads, so it can
+// go straight to global memory or to an unpadded buffer.
+//
+// Exchange buffers are padded with one slot per E elements: pass 1 writes
+// at stride E across the threads, which without the pad puts a warp on two
+// banks (stride E+1 spreads it over all of them); the loads and the later
+// passes' stores are consecutive runs either way.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "cplx.cuh"
+
+namespace chgpu {
+
+// radix of pass p (p >= 1) for elements per thread E and threads per group
+// TPR: the largest power of two dividing E that still divides what is left
+// of TPR
+__host__ __device__ constexpr int rplan_radix(int E, int TPR, int p) {
+  int rem = TPR;
+  int r = 1;
+  const int rmax = (E % 16 == 0) ? 16 : (E % 8 == 0 ? 8 : (E % 4 == 0 ? 4 : 2));
+  for (int q = 1; q <= p; ++q) {
+    if (rem <= 1) return 1;
+    r = rmax;
+    while (r > rem) r /= 2;
+    rem /= r;
+  }
+  return r;
+}
+__host__ __device__ constexpr int rplan_passes(int E, int TPR) {
+  int n = 1, rem = TPR;
+  const int rmax = (E % 16 == 0) ? 16 : (E % 8 == 0 ? 8 : (E % 4 == 0 ? 4 : 2));
+  while (rem > 1) {
+    int r = rmax;
+    while (r > rem) r /= 2;
+    rem /= r;
+    ++n;
+  }
+  return n;
+}
+// Ns before pass p (p = 0 is the radix-E pass)
+__host__ __device__ constexpr int rplan_ns(int E, int TPR, int p) {
+  int ns = E;
+  for (int q = 1; q < p; ++q) ns *= rplan_radix(E, TPR, q);
+  return p == 0 ? 1 : ns;
+}
+// offset of pass p's twiddles in the plan's table: R-1 values per k < Ns
+__host__ __device__ constexpr int rplan_twoff(int E, int TPR, int p) {
+  int off = 0;
+  for (int q = 1; q < p; ++q) off += rplan_ns(E, TPR, q) * (rplan_radix(E, TPR, q) - 1);
+  return off;
+}
+__host__ __device__ constexpr int rplan_twsize(int E, int TPR) {
+  return rplan_twoff(E, TPR, rplan_passes(E, TPR));
+}
+
+// padded index of an exchange buffer
+template <int E> __device__ __forceinline__ int rpad(int i) { return i + i / E; }
+template <int E, int TPR> __host__ __device__ constexpr int rbuf_size() { return E * TPR + TPR; }
+
+// barrier over one transform group: the warp (or sub-warp groups of one
+// warp, which all run the same passes), or a named barrier of TPR threads
+template <int TPR> __device__ __forceinline__ void group_sync() {
+  if constexpr (TPR <= 32) {
+    __syncwarp();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + (int)(threadIdx.x / TPR)), "r"(TPR) : "memory");
+  }
+}
+
+// pass 1: one radix-E register DFT per thread
+template <int E, int SIGN, typename V> __device__ __forceinline__ void rpass_first(V (&a)[E]) {
+  Dft<E, V>::template run<SIGN>(a);
+}
+
+// Writes the outputs of a pass whose inputs are in a[] (pass p >= 1) or the
+// outputs of pass 1 (p == 0, a[] already transformed) to buf.
+template <int E, int TPR, int P, int SIGN, bool PADDED, typename V>
+__device__ __forceinline__ void rpass_store(V (&a)[E], V* buf, int t, const V* __restrict__ tw) {
+  if constexpr (P == 0) {
+    // pass 1 outputs: butterfly j = t, outputs at t E + r
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+      const int o = t * E + r;
+      buf[PADDED ? rpad<E>(o) : o] = a[r];
+    }
+  } else {
+    constexpr int R = rplan_radix(E, TPR, P);
+    constexpr int Ns = rplan_ns(E, TPR, P);
+    constexpr int B = E / R;
+    const V* twp = tw + rplan_twoff(E, TPR, P);
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      const int j = t + TPR * i;
+      const int k = j % Ns;
+      V b[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) b[r] = a[i + r * B];
+      const V* w = twp + k * (R - 1);
+#pragma unroll
+      for (int r = 1; r < R; ++r) b[r] = cmul_s_inner<SIGN>(b[r], ldg_v(w + r - 1));
+      Dft<R, V>::template run<SIGN>(b);
+      const int base = (j - k) * R + k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int o = base + r * Ns;
+        buf[PADDED ? rpad<E>(o) : o] = b[r];
+      }
+    }
+  }
+}
+
+template <int E, int TPR, typename V> __device__ __forceinline__ void rload(V (&a)[E], const V* buf, int t) {
+#pragma unroll
+  for (int e = 0; e < E; ++e) a[e] = buf[rpad<E>(t + TPR * e)];
+}
+
+// The last pass's butterflies with a caller-supplied sink for each output
+// (natural order index o = j + r Ns): sink(o, value).
+template <int E, int TPR, int SIGN, typename V, typename Sink>
+__device__ __forceinline__ void rpass_last(V (&a)[E], int t, const V* __restrict__ tw, Sink sink) {
+  constexpr int NP = rplan_passes(E, TPR);
+  if constexpr (NP == 1) {
+    // the only pass: a[r] is output r of butterfly t = 0 (TPR == 1)
+#pragma unroll
+    for (int r = 0; r < E; ++r) sink(r, a[r]);
+  } else {
+    constexpr int P = NP - 1;
+    constexpr int R = rplan_radix(E, TPR, P);
+    constexpr int Ns = rplan_ns(E, TPR, P);
+    constexpr int B = E / R;
+    static_assert(Ns * R == E * TPR, "last pass");
+    const V* twp = tw + rplan_twoff(E, TPR, P);
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      const int j = t + TPR * i;  // < Ns, so k = j
+      V b[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) b[r] = a[i + r * B];
+      const V* w = twp + j * (R - 1);
+#pragma unroll
+      for (int r = 1; r < R; ++r) b[r] = cmul_s_inner<SIGN>(b[r], ldg_v(w + r - 1));
+      Dft<R, V>::template run<SIGN>(b);
+#pragma unroll
+      for (int r = 0; r < R; ++r) sink(j + r * Ns, b[r]);
+    }
+  }
+}
+
+// Whole transform: a[] holds the input distribution (x[t + TPR e]); buf is
+// the group's padded exchange buffer (rbuf_size elements); the outputs are
+// handed to sink(index, value) in the last pass.  Every thread of the group
+// calls it; the caller synchronises before reusing buf.
+template <int E, int TPR, int SIGN, typename V, typename Sink>
+__device__ __forceinline__ void rfft(V (&a)[E], V* buf, int t, const V* __restrict__ tw, Sink sink) {
+  constexpr int NP = rplan_passes(E, TPR);
+  rpass_first<E, SIGN>(a);
+  if constexpr (NP == 1) {
+    rpass_last<E, TPR, SIGN>(a, t, tw, sink);
+  } else {
+    rpass_store<E, TPR, 0, SIGN, true>(a, buf, t, tw);
+    group_sync<TPR>();
+    rload<E, TPR>(a, buf, t);
+    group_sync<TPR>();
+    if constexpr (NP >= 3) {
+      rpass_store<E, TPR, 1, SIGN, true>(a, buf, t, tw);
+      group_sync<TPR>();
+      rload<E, TPR>(a, buf, t);
+      group_sync<TPR>();
+    }
+    if constexpr (NP >= 4) {
+      rpass_store<E, TPR, 2, SIGN, true>(a, buf, t, tw);
+      group_sync<TPR>();
+      rload<E, TPR>(a, buf, t);
+      group_sync<TPR>();
+    }
+    static_assert(NP <= 4, "at most four passes");
+    rpass_last<E, TPR, SIGN>(a, t, tw, sink);
+  }
+}
+
+// Compile-time plans of the lengths with register-blocked kernels.
+template <int N> struct RLen;
+template <> struct RLen<32> { static constexpr int E = 16, TPR = 2; };
+template <> struct RLen<48> { static constexpr int E = 24, TPR = 2; };
+template <> struct RLen<64> { static constexpr int E = 16, TPR = 4; };
+template <> struct RLen<96> { static constexpr int E = 24, TPR = 4; };
+template <> struct RLen<192> { static constexpr int E = 24, TPR = 8; };
+template <> struct RLen<384> { static constexpr int E = 24, TPR = 16; };
+template <> struct RLen<768> { static constexpr int E = 24, TPR = 32; };
+template <> struct RLen<1536> { static constexpr int E = 24, TPR = 64; };
+
+// host side: does a length have a register-blocked plan, and its (E, TPR)
+inline bool rlen_plan(int n, int* E, int* TPR) {
+  switch (n) {
+    case 32: *E = 16; *TPR = 2; return true;
+    case 48: *E = 24; *TPR = 2; return true;
+    case 64: *E = 16; *TPR = 4; return true;
+    case 96: *E = 24; *TPR = 4; return true;
+    case 192: *E = 24; *TPR = 8; return true;
+    case 384: *E = 24; *TPR = 16; return true;
+    case 768: *E = 24; *TPR = 32; return true;
+    case 1536: *E = 24; *TPR = 64; return true;
+    default: return false;
+  }
+}
+
+}  // namespace chgpu
