@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", str(ROOT / "include")]
 SOURCES = ["capi.cu", "conv.cu", "convf_f32.cu", "convf_f64.cu", "convf_dd.cu", "solve.cu", "setup.cpp", "noalloc.cu", "stats.cu", "export.cu", "mlp.cu", "peaks.cu",
-           "closure.cu"]
+           "closure.cu", "tke.cu"]
 
 
 def nvcc() -> str:

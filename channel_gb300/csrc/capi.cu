@@ -128,6 +128,15 @@ struct chgpu_handle {
   float2* cl_tau = nullptr;
   float* cl_wd = nullptr;
   void *cl_twz = nullptr, *cl_twx = nullptr, *cl_twh = nullptr;
+  // Reynolds-stress budget spectra (allocated by the first chgpu_tke_reset)
+  double2 *tke_W = nullptr, *tke_N = nullptr, *tke_P = nullptr, *tke_Zt = nullptr, *tke_Xt = nullptr;
+  double *tke_acc = nullptr, *tke_mean = nullptr;
+  void *tke_twz = nullptr, *tke_twx = nullptr, *tke_twh = nullptr;
+  RadixDev tke_rz{}, tke_rx{};
+  int tke_chunk = 0;
+  long long tke_n = 0;
+  bool tke_ready = false, tke_pressure = false;
+  std::vector<double> tke_meanh;  // U, W, dU/dy, dW/dy, d2U/dy2, d2W/dy2, P per plane
   int nsm = 0;
   // per-kernel timing
   bool profiling = false;
@@ -538,7 +547,9 @@ void release(chgpu_handle* h) {
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   void* bufs[] = {h->V, h->F, h->old, h->VV, h->Zb, h->Pb, h->rhs, h->fac, h->der, h->derT, h->derL, h->cst, h->d0lu, h->nud, h->lindd, h->yint, h->dy,
                   h->twz, h->twx, h->twh, h->twzr, h->twxr, h->sc, h->ex_W, h->ex_P, h->ex_out, h->ex_twz, h->ex_twx,
-                  h->cl_G, h->cl_Z, h->cl_P, h->cl_tau, h->cl_wd, h->cl_twz, h->cl_twx, h->cl_twh};
+                  h->cl_G, h->cl_Z, h->cl_P, h->cl_tau, h->cl_wd, h->cl_twz, h->cl_twx, h->cl_twh,
+                  h->tke_W, h->tke_N, h->tke_P, h->tke_Zt, h->tke_Xt, h->tke_acc, h->tke_mean,
+                  h->tke_twz, h->tke_twx, h->tke_twh};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (h->sc_host) cudaFreeHost(h->sc_host);
@@ -606,9 +617,15 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
   Radix rz = make_radix(nzd, false), rx = make_radix(nxd, h->prec == CHGPU_MIXED);
   if (rz.nst < 0 || rx.nst < 0) { delete h; return fail(nullptr, CHGPU_E_PARAM, "unsupported FFT length"); }
   {
+    // register-blocked transforms where they measured faster (GB300, 127x192x127
+    // and 383x384x383): FP32 z and x passes (x-row 92 -> 59 ms, z-forward
+    // 20 -> 10.5 ms per step at 383x384x383); FP64 z passes (even with the
+    // generic kernels; the FP64 x-row kernel stays generic, 977 vs 1017 ms);
+    // double-float keeps the generic kernels (its register-blocked x-row
+    // kernel spills: 820 vs 354 ms)
     int e_ = 0, tpr_ = 0;
-    h->zfast = rlen_plan(nzd, &e_, &tpr_);
-    h->xfast = rlen_plan(nxd, &e_, &tpr_) && nxd <= 768;
+    h->zfast = rlen_plan(nzd, &e_, &tpr_) && h->prec != CHGPU_FP64DD;
+    h->xfast = rlen_plan(nxd, &e_, &tpr_) && nxd <= 768 && h->prec == CHGPU_MIXED;
   }
   h->halves = d.npairs >= 65536 ? 2 : 1;
   h->split_solve = d.npairs < 65536;
@@ -1431,6 +1448,168 @@ int chgpu_profiles(chgpu_handle* h, double* mean, double* var, long long* nsampl
     var[k] = acc[2 * n + k] / N - mean[k] * mean[k];
   }
   if (nsamples) *nsamples = h->stats_n;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Reynolds-stress budget spectra (postpro/tke/uiuj_spectra.f90)
+// ---------------------------------------------------------------------------
+int chgpu_tke_reset(chgpu_handle* h, const double* mean) {
+  if (!h || !mean) return fail(h, CHGPU_E_PARAM, "chgpu_tke_reset: null argument");
+  const Dims& d = h->d;
+  const int np = d.nplanes;
+  const size_t FS = (size_t)np * d.nmodes, nxp = (size_t)d.nx + 1;
+  if (!h->tke_ready) {
+    int dev = 0, optin = 0;
+    CK(h, cudaGetDevice(&dev));
+    CK(h, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    if (tke_x_smem(d.nxd) > (size_t)optin || tke_z_smem(d.nzd) > (size_t)optin)
+      return fail(h, CHGPU_E_PARAM, "chgpu_tke_reset: transform length too large for the budget kernels");
+    // planes per chunk of the padded-grid work: the z-inverted fields of a chunk within ~2 GB
+    const size_t per_plane = 12 * nxp * (size_t)d.nzd * sizeof(double2);
+    h->tke_chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)np, ((size_t)2 << 30) / per_plane));
+    const size_t C = (size_t)h->tke_chunk;
+    CK(h, cudaMalloc((void**)&h->tke_W, sizeof(double2) * 12 * FS));
+    CK(h, cudaMalloc((void**)&h->tke_N, sizeof(double2) * 3 * FS));
+    CK(h, cudaMalloc((void**)&h->tke_P, sizeof(double2) * FS));
+    CK(h, cudaMalloc((void**)&h->tke_Zt, sizeof(double2) * 12 * C * nxp * d.nzd));
+    CK(h, cudaMalloc((void**)&h->tke_Xt, sizeof(double2) * 3 * C * nxp * d.nzd));
+    CK(h, cudaMalloc((void**)&h->tke_acc, sizeof(double) * 36 * (size_t)np * d.nzt));
+    CK(h, cudaMalloc((void**)&h->tke_mean, sizeof(double) * 5 * (size_t)np));
+    Radix rz = make_radix(d.nzd, false), rx = make_radix(d.nxd, false);
+    h->tke_rz.n = rz.n; h->tke_rz.nst = rz.nst; std::memcpy(h->tke_rz.r, rz.r, sizeof rz.r);
+    h->tke_rx.n = rx.n; h->tke_rx.nst = rx.nst; std::memcpy(h->tke_rx.r, rx.r, sizeof rx.r);
+    set_twiddle_offsets(h->tke_rz);
+    set_twiddle_offsets(h->tke_rx);
+    if (int rc = upload_stage_twiddles<double2>(h, &h->tke_twz, h->tke_rz)) return rc;
+    if (int rc = upload_stage_twiddles<double2>(h, &h->tke_twx, h->tke_rx)) return rc;
+    if (int rc = upload_pack_roots<double2>(h, &h->tke_twh, 2 * d.nxd, 0.5L * (long double)d.factor)) return rc;
+    CK(h, tke_set_smem_limits(d.nzd, d.nxd));
+    h->tke_ready = true;
+  }
+  // mean profiles and their y derivatives (uiuj_spectra.f90:152-155)
+  std::vector<double>& m = h->tke_meanh;
+  m.assign(7 * (size_t)np, 0.0);
+  for (int q = 0; q < np; ++q) {
+    m[q] = mean[q];
+    m[(size_t)np + q] = mean[(size_t)np + q];
+    m[6 * (size_t)np + q] = mean[2 * (size_t)np + q];
+  }
+  real_deriv(h->tab, &m[0], &m[2 * (size_t)np], 1);
+  real_deriv(h->tab, &m[(size_t)np], &m[3 * (size_t)np], 1);
+  real_deriv(h->tab, &m[0], &m[4 * (size_t)np], 2);
+  real_deriv(h->tab, &m[(size_t)np], &m[5 * (size_t)np], 2);
+  std::vector<double> dm(5 * (size_t)np);  // U, W, P, dU/dy, dW/dy
+  for (int q = 0; q < np; ++q) {
+    dm[q] = m[q];
+    dm[(size_t)np + q] = m[(size_t)np + q];
+    dm[2 * (size_t)np + q] = m[6 * (size_t)np + q];
+    dm[3 * (size_t)np + q] = m[2 * (size_t)np + q];
+    dm[4 * (size_t)np + q] = m[3 * (size_t)np + q];
+  }
+  CK(h, cudaMemcpyAsync(h->tke_mean, dm.data(), sizeof(double) * dm.size(), cudaMemcpyHostToDevice, h->stream));
+  CK(h, cudaMemsetAsync(h->tke_acc, 0, sizeof(double) * 36 * (size_t)np * d.nzt, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  h->tke_n = 0;
+  h->tke_pressure = false;
+  return 0;
+}
+
+int chgpu_tke_accumulate(chgpu_handle* h, const double* pressure) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "null handle");
+  if (!h->tke_ready) return fail(h, CHGPU_E_STATE, "chgpu_tke_accumulate: chgpu_tke_reset first");
+  if (h->tke_n > 0 && (pressure != nullptr) != h->tke_pressure)
+    return fail(h, CHGPU_E_PARAM, "chgpu_tke_accumulate: give a pressure field with every sample or with none");
+  const Dims& d = h->d;
+  const size_t FS = (size_t)d.nplanes * d.nmodes;
+  if (pressure) {
+    // restart-file layout (iy fastest) to the plane-major layout, through the x work buffer
+    double2* stage = reinterpret_cast<double2*>(h->Pb);
+    CK(h, cudaMemcpyAsync(stage, pressure, sizeof(double2) * FS, cudaMemcpyHostToDevice, h->stream));
+    launch_transpose(stage, h->tke_P, d.nmodes, d.nplanes, 1, h->stream);
+  }
+  TkeLaunch L{};
+  L.d = d;
+  L.bc = h->bc;
+  L.V = h->V;
+  L.W = h->tke_W;
+  L.N3 = h->tke_N;
+  L.P = pressure ? h->tke_P : nullptr;
+  L.Zt = h->tke_Zt;
+  L.Xt = h->tke_Xt;
+  L.acc = h->tke_acc;
+  L.mean = h->tke_mean;
+  L.der = h->der;
+  L.d0lu = h->d0lu;
+  L.twz = (const double2*)h->tke_twz;
+  L.twx = (const double2*)h->tke_twx;
+  L.twh = (const double2*)h->tke_twh;
+  L.rz = h->tke_rz;
+  L.rx = h->tke_rx;
+  L.chunk = h->tke_chunk;
+  launch_tke_snapshot(L, h->stream);
+  CK(h, cudaGetLastError());
+  const int nchunks = (d.nplanes + h->tke_chunk - 1) / h->tke_chunk;
+  h->launches += 3 + (pressure ? 2 : 0) + 3 * nchunks;
+  h->tke_pressure = pressure != nullptr;
+  h->tke_n += 1;
+  return 0;
+}
+
+int chgpu_tke_result(chgpu_handle* h, int timestwo, double* mean7, double* spectra, double* profiles,
+                     long long* nsamples) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "null handle");
+  if (!h->tke_ready || h->tke_n == 0) return fail(h, CHGPU_E_STATE, "chgpu_tke_result: no samples accumulated");
+  const Dims& d = h->d;
+  const int np = d.nplanes, nzt = d.nzt;
+  const size_t S = (size_t)np * nzt;
+  std::vector<double> acc(36 * S);
+  CK(h, cudaMemcpyAsync(acc.data(), h->tke_acc, sizeof(double) * acc.size(), cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  const double N = (double)h->tke_n;
+  // spectra(irs, term, iz, iy) in the reference's order (irs fastest); the
+  // accumulated terms var, prod, psdiss, ttrsp, pstrain, PHIptrsp sit at
+  // term 0, 1, 2, 3, 5, 9 (uiuj_spectra.f90:13-14, :70)
+  static const int kAccTerm[6] = {0, 1, 2, 3, 5, 9};
+  std::vector<double> sp((size_t)60 * S, 0.0);
+  auto SP = [&](int irs, int term, int izp, int plane) -> double& {
+    return sp[(size_t)irs + 6 * ((size_t)term + 10 * ((size_t)izp + (size_t)nzt * plane))];
+  };
+  for (int q = 0; q < 6; ++q)
+    for (int irs = 0; irs < 6; ++irs)
+      for (int plane = 0; plane < np; ++plane)
+        for (int izp = 0; izp < nzt; ++izp)
+          SP(irs, kAccTerm[q], izp, plane) = acc[(size_t)(q * 6 + irs) * S + (size_t)plane * nzt + izp] / N;
+  // flux derivatives (:243-259): PHIvdiff = ni d/dy var, vdiff = ni d2/dy2 var, ptrsp = d/dy PHIptrsp
+  std::vector<double> f0(np), f1(np);
+  for (int izp = 0; izp < nzt; ++izp)
+    for (int irs = 0; irs < 6; ++irs) {
+      for (int q = 0; q < np; ++q) f0[q] = SP(irs, 0, izp, q);
+      real_deriv(h->tab, f0.data(), f1.data(), 1);
+      for (int q = 0; q < np; ++q) SP(irs, 8, izp, q) = f1[q] * d.ni;
+      real_deriv(h->tab, f0.data(), f1.data(), 2);
+      for (int q = 0; q < np; ++q) SP(irs, 4, izp, q) = f1[q] * d.ni;
+      for (int q = 0; q < np; ++q) f0[q] = SP(irs, 9, izp, q);
+      real_deriv(h->tab, f0.data(), f1.data(), 1);
+      for (int q = 0; q < np; ++q) SP(irs, 6, izp, q) = f1[q];
+    }
+  if (timestwo)  // -two (:262)
+    for (int plane = 0; plane < np; ++plane)
+      for (int izp = 0; izp < nzt; ++izp)
+        for (int irs = 0; irs < 6; ++irs) SP(irs, 0, izp, plane) *= 2.0;
+  if (spectra) std::memcpy(spectra, sp.data(), sizeof(double) * sp.size());
+  if (profiles)
+    for (int plane = 0; plane < np; ++plane)
+      for (int term = 0; term < 10; ++term)
+        for (int irs = 0; irs < 6; ++irs) {
+          double s = 0.0;
+          for (int izp = 0; izp < nzt; ++izp) s += SP(irs, term, izp, plane);
+          profiles[(size_t)irs + 6 * ((size_t)term + 10 * (size_t)plane)] = s;
+        }
+  if (mean7)
+    for (int plane = 0; plane < np; ++plane)
+      for (int q = 0; q < 7; ++q) mean7[(size_t)q + 7 * (size_t)plane] = h->tke_meanh[(size_t)q * np + plane];
+  if (nsamples) *nsamples = h->tke_n;
   return 0;
 }
 

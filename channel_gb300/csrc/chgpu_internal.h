@@ -44,6 +44,9 @@ bool compute_tables_static(const chgpu_params& p, StaticTables& t);
 bool fft_fit(int n);                       // ffts.f90:78-86
 void padded_sizes(int nx, int nz, int* nxd, int* nzd);  // dnsdata.f90:110-114
 void compute_tables(const chgpu_params& p, Tables& t);
+// REALderiv / REALderiv2 (dnsdata.f90:419-451): compact first (order 1) or
+// second (order 2) y derivative of a real line f0[iy+1], iy = -1..ny+1
+void real_deriv(const Tables& t, const double* f0, double* f1, int order);
 
 // Radix plan of a length-n transform (n = 2^a or 3*2^a).
 struct Radix {

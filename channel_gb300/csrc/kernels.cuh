@@ -139,6 +139,30 @@ size_t export_x_smem(int xpairs, int nx, int Nx);
 int export_set_smem_limits();  // dynamic shared memory allowed per block, or -1
 void launch_export_chunk(const ExportLaunch& L, int iy0, int nplanes_chunk, cudaStream_t s);
 void launch_force_ghosts(double2* F, const double* der, const Dims& d, cudaStream_t s);
+// Reynolds-stress budget spectra (tke.cu): one snapshot's accumulation
+struct TkeLaunch {
+  Dims d;
+  BcRows bc;
+  const double2* V;  // the field
+  double2* W;        // work: u', v', w' then du'_i/dx_k at field 3 + 3i + k (12 fields, V's layout)
+  double2* N3;       // the convective terms N_0..2 (3 fields, V's layout)
+  double2* P;        // pressure (V's layout, one field), or null
+  double2* Zt;       // z-inverted fields of a chunk of planes: [12][chunk][nx+1][nzd]
+  double2* Xt;       // x-forward N_i of a chunk: [3][chunk][nx+1][nzd]
+  double* acc;       // running sums [6 terms][6 pairs][plane][kz]
+  const double* mean;  // U, W, P, dU/dy, dW/dy per plane
+  const double* der;
+  const double* d0lu;
+  const double2* twz;  // FP64 per-stage roots of the z plan and of the x plan, pack roots
+  const double2* twx;
+  const double2* twh;
+  RadixDev rz, rx;
+  int chunk;  // planes per chunk
+};
+void launch_tke_snapshot(const TkeLaunch& L, cudaStream_t s);
+cudaError_t tke_set_smem_limits(int nzd, int nxd);
+size_t tke_z_smem(int nzd);
+size_t tke_x_smem(int nxd);
 void launch_stats_accumulate(const double2* V, const Dims& d, double* acc, cudaStream_t s);
 
 }  // namespace chgpu

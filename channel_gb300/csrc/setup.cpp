@@ -247,6 +247,45 @@ void vander_array(const double* y, int first, double y0, double M[5][5], const d
 }  // namespace
 
 // Same arithmetic as compute_tables, into fixed arrays.
+void real_deriv(const Tables& t, const double* f0, double* f1, int order) {
+  const int ny = t.ny;
+  auto F0 = [&](int iy) { return f0[iy + 1]; };
+  auto sum5 = [&](const double* c, int iy0) {
+    double s = c[0] * F0(iy0);
+    for (int j = 1; j < 5; ++j) s = s + c[j] * F0(iy0 + j);
+    return s;
+  };
+  const int dk = order == 2 ? 10 : 5;  // d2 or d1 row of der
+  // COMPLEXderiv / COMPLEXderiv2 (dnsdata.f90:339-414) on a real line
+  double* x = f1;  // x[iy+1]
+  x[0 + 1] = sum5(order == 2 ? t.d240 : t.d140, -1);
+  x[-1 + 1] = sum5(order == 2 ? t.d24m1 : t.d14m1, -1);
+  x[ny + 1] = sum5(order == 2 ? t.d24n : t.d14n, ny - 3);
+  x[ny + 1 + 1] = sum5(order == 2 ? t.d24np1 : t.d14np1, ny - 3);
+  for (int iy = 1; iy <= ny - 1; ++iy) x[iy + 1] = sum5(&t.der[(size_t)iy * 20 + dk], iy - 2);
+  const double* d0 = t.der.data();
+  x[1 + 1] = x[1 + 1] - (d0[1 * 20 + 1] * x[0 + 1] + d0[1 * 20 + 0] * x[-1 + 1]);
+  x[2 + 1] = x[2 + 1] - d0[2 * 20 + 0] * x[0 + 1];
+  x[ny - 1 + 1] = x[ny - 1 + 1] - (d0[(size_t)(ny - 1) * 20 + 3] * x[ny + 1] + d0[(size_t)(ny - 1) * 20 + 4] * x[ny + 1 + 1]);
+  x[ny - 2 + 1] = x[ny - 2 + 1] - d0[(size_t)(ny - 2) * 20 + 4] * x[ny + 1];
+  // LeftLU5divStep1 and Step2 with the factored D0mat (rbparmat_blocking.f90:57-100);
+  // row r of the factors is y row iy = r + 1, and x(r) = x[r + 1 + 1]
+  const int nrow = ny + 1;
+  const double* A = t.d0lu.data();
+  for (int r = nrow - 3; r >= 0; --r) {
+    const double* a = A + (size_t)r * 5 + 2;
+    double s = a[1] * x[r + 1 + 2];
+    s = s + a[2] * x[r + 2 + 2];
+    x[r + 2] = (x[r + 2] - s) * a[0];
+  }
+  for (int r = 0; r <= nrow - 1; ++r) {
+    const double* a = A + (size_t)r * 5 + 2;
+    double s = a[-2] * x[r - 2 + 2];
+    s = s + a[-1] * x[r - 1 + 2];
+    x[r + 2] = x[r + 2] - s;
+  }
+}
+
 bool compute_tables_static(const chgpu_params& p, StaticTables& t) {
   const int ny = p.ny;
   if (ny < 8 || ny > StaticTables::kMaxNy) return false;

@@ -104,6 +104,9 @@ SIGNATURES = {
     "chgpu_linsolve_noalloc": (C.c_int, [C.POINTER(Params), C.c_double, C.c_void_p, _DP, C.c_void_p,
                                          C.c_char_p, C.c_size_t]),
     "chgpu_measure_peaks": (C.c_int, [_DP, _DP, _DP, C.c_char_p, C.c_size_t]),
+    "chgpu_tke_reset": (C.c_int, [_P, _DP]),
+    "chgpu_tke_accumulate": (C.c_int, [_P, _DP]),
+    "chgpu_tke_result": (C.c_int, [_P, C.c_int, _DP, _DP, _DP, C.POINTER(C.c_longlong)]),
     # include/chgpu_closure.h
     "chgpu_mlp_create": (C.c_int, [C.c_ulonglong, C.POINTER(C.c_void_p)]),
     "chgpu_mlp_destroy": (C.c_int, [_P]),
@@ -338,6 +341,39 @@ class Channel:
         ns = C.c_longlong()
         self._check(self.lib.chgpu_profiles(self.h, _dp(mean), _dp(var), C.byref(ns)))
         return mean.reshape(3, -1), var.reshape(3, -1), int(ns.value)
+
+    def tke_reset(self, mean_u: np.ndarray, mean_w: np.ndarray, mean_p: np.ndarray | None = None):
+        """Reynolds-stress budget spectra: clears the sums; the mean profiles
+        (ny+3 each) are removed from every sample."""
+        ny3 = self.p.ny + 3
+        m = np.zeros(3 * ny3)
+        m[:ny3] = mean_u
+        m[ny3:2 * ny3] = mean_w
+        if mean_p is not None:
+            m[2 * ny3:] = mean_p
+        self._check(self.lib.chgpu_tke_reset(self.h, _dp(m)))
+
+    def tke_accumulate(self, pressure: np.ndarray | None = None):
+        """One sample of the current field; pressure (nx+1, 2nz+1, ny+3) complex or None."""
+        if pressure is None:
+            self._check(self.lib.chgpu_tke_accumulate(self.h, None))
+            return
+        a = np.ascontiguousarray(pressure, dtype=np.complex128)
+        assert a.shape == (self.p.nx + 1, 2 * self.p.nz + 1, self.p.ny + 3)
+        # restart-file (Fortran) order: iy fastest
+        f = np.ascontiguousarray(a.transpose(2, 1, 0)).reshape(-1)
+        self._check(self.lib.chgpu_tke_accumulate(self.h, _dp(f.view(np.float64))))
+
+    def tke_result(self, timestwo: bool = False):
+        """(mean (7, ny+3), spectra (6, 10, 2nz+1, ny+3), profiles (6, 10, ny+3), samples)."""
+        ny3, nzt = self.p.ny + 3, 2 * self.p.nz + 1
+        mean = np.empty(7 * ny3)
+        sp = np.empty(60 * nzt * ny3)
+        pr = np.empty(60 * ny3)
+        n = C.c_longlong()
+        self._check(self.lib.chgpu_tke_result(self.h, int(timestwo), _dp(mean), _dp(sp), _dp(pr), C.byref(n)))
+        return (mean.reshape((7, ny3), order="F"), sp.reshape((6, 10, nzt, ny3), order="F"),
+                pr.reshape((6, 10, ny3), order="F"), n.value)
 
     def snapshot_async(self):
         self._check(self.lib.chgpu_snapshot_async(self.h))

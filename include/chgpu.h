@@ -209,6 +209,34 @@ int chgpu_stats_reset(chgpu_handle* h);
 int chgpu_stats_accumulate(chgpu_handle* h);
 int chgpu_profiles(chgpu_handle* h, double* mean, double* var, long long* nsamples);
 
+/* Spanwise spectra of the Reynolds-stress budgets, the reference's
+ * post-processing program postpro/tke/uiuj_spectra.f90, accumulated on the
+ * device from the handle's current field (call chgpu_tke_accumulate between
+ * steps, at the statistics cadence).
+ *   chgpu_tke_reset(h, mean): the mean profiles removed from each sample,
+ *     mean = U, W, P (3 arrays of ny+3, iy = -1..ny+1), as the reference
+ *     averages them over the same files first (:135-150); clears the sums.
+ *   chgpu_tke_accumulate(h, pressure): one sample.  pressure: NULL, or the
+ *     pressure field of this sample in V's restart-file layout (one complex
+ *     component); give one with every sample or with none -- without it the
+ *     pressure terms (pstrain, ptrsp, PHIptrsp) stay zero.
+ *   chgpu_tke_result(h, timestwo, mean7, spectra, profiles, nsamples):
+ *     mean7(1:7, iy) = U, W, dU/dy, dW/dy, d2U/dy2, d2W/dy2, P;
+ *     spectra(irs, term, iz, iy) and profiles(irs, term, iy) (the sum over
+ *     iz), Fortran order with irs fastest, irs = uu, vv, ww, uv, vw, uw,
+ *     term = var, prod, psdiss, ttrsp, vdiff, pstrain, ptrsp, PHIttrsp (not
+ *     assigned by the reference: zero), PHIvdiff, PHIptrsp; the sums divided
+ *     by the number of samples, the flux derivatives taken (:243-259) and,
+ *     with timestwo, var doubled (-two, :262) -- the arrays the reference
+ *     writes to uiuj_spectra.bin.  Any output may be NULL.
+ * All sums are FP64 in every precision path.  The first reset allocates 16
+ * field-sized FP64 buffers and the padded-grid work of a chunk of planes
+ * (~2 GB). */
+int chgpu_tke_reset(chgpu_handle* h, const double* mean);
+int chgpu_tke_accumulate(chgpu_handle* h, const double* pressure);
+int chgpu_tke_result(chgpu_handle* h, int timestwo, double* mean7, double* spectra, double* profiles,
+                     long long* nsamples);
+
 /* Field snapshot for output without stalling the time loop (the dt_field /
  * dt_save writes, dnsdata.f90:882-918).  chgpu_snapshot_async copies V to a
  * device staging buffer in stream order and then, on a side stream while

@@ -779,6 +779,32 @@ void orc_deriv(const orc_state* s, const double* f0, double* f1) {
   complex_deriv(s, (const cplx*)f0, (cplx*)f1);
 }
 
+/* COMPLEXderiv2 (dnsdata.f90:378-414) followed by LeftLU5divStep2(D0mat):
+ * the compact second derivative (REALderiv2, dnsdata.f90:438-451, is this on
+ * a real line). */
+static void complex_deriv2(const orc_state* s, const cplx* f0, cplx* f1) {
+  const int ny = s->ny;
+#define F0(iy) f0[YI(iy)]
+#define F1(iy) f1[YI(iy)]
+  F1(0) = csum5(s->d240, &F0(-1));
+  F1(-1) = csum5(s->d24m1, &F0(-1));
+  F1(ny) = csum5(s->d24n, &F0(ny - 3));
+  F1(ny + 1) = csum5(s->d24np1, &F0(ny - 3));
+  for (int iy = 1; iy <= ny - 1; ++iy) F1(iy) = csum5(s->der[iy].d2, &F0(iy - 2));
+  F1(1) = F1(1) - (s->der[1].d0[1] * F1(0) + s->der[1].d0[0] * F1(-1));
+  F1(2) = F1(2) - s->der[2].d0[0] * F1(0);
+  F1(ny - 1) = F1(ny - 1) - (s->der[ny - 1].d0[3] * F1(ny) + s->der[ny - 1].d0[4] * F1(ny + 1));
+  F1(ny - 2) = F1(ny - 2) - s->der[ny - 2].d0[4] * F1(ny);
+  LeftLU5divStep1(f1, s->D0mat, ny + 1);
+  LeftLU5divStep2(s->D0mat, f1, ny + 1);
+#undef F0
+#undef F1
+}
+
+void orc_deriv2(const orc_state* s, const double* f0, double* f1) {
+  complex_deriv2(s, (const cplx*)f0, (cplx*)f1);
+}
+
 static void applybc_0(double* EQ, const double* bc0, const double* bc0m1) { /* dnsdata.f90:458-464 */
   /* EQ rows iy=1.. : EQ[(iy-1)*5 + j+2] */
   double* r1 = EQ;

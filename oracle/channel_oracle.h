@@ -116,6 +116,7 @@ void orc_set_tau(orc_state* s, const double* tau);
 /* COMPLEXderiv followed by LeftLU5divStep2(D0mat) on one y-line
  * (dnsdata.f90:339-373): f0, f1 hold ny+3 complex values (iy=-1..ny+1). */
 void orc_deriv(const orc_state* s, const double* f0, double* f1);
+void orc_deriv2(const orc_state* s, const double* f0, double* f1);
 
 /* Batched complex FFT of length n (n = 2^a or 3*2^a), unnormalised;
  * sign=-1 forward, +1 backward; data interleaved complex, `howmany` rows of

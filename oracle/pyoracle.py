@@ -83,6 +83,7 @@ def lib():
         L.orc_start.argtypes = [P, C.POINTER(Line)]
         L.orc_fft.argtypes = [C.c_int, C.c_int, C.c_int, D]
         L.orc_deriv.argtypes = [P, D, D]
+        L.orc_deriv2.argtypes = [P, D, D]
         L.orc_set_body_force.argtypes = [P, D]
         L.orc_set_tau.argtypes = [P, D]
         L.orc_fftfit.restype = C.c_int
@@ -198,6 +199,13 @@ class Oracle:
         a = np.ascontiguousarray(f, dtype=np.complex128)
         out = np.empty_like(a)
         lib().orc_deriv(self.h, _dp(a.view(np.float64)), _dp(out.view(np.float64)))
+        return out
+
+    def deriv2(self, f: np.ndarray) -> np.ndarray:
+        """Compact second y-derivative of a complex y-line (iy=-1..ny+1)."""
+        a = np.ascontiguousarray(f, dtype=np.complex128)
+        out = np.empty_like(a)
+        lib().orc_deriv2(self.h, _dp(a.view(np.float64)), _dp(out.view(np.float64)))
         return out
 
     def yintegr(self, f: np.ndarray) -> float:
