@@ -92,6 +92,7 @@ struct chgpu_handle {
   void* twzr = nullptr;
   void* twxr = nullptr;
   bool zfast = false, xfast = false;
+  int xrvar = 4;  // register-blocked x-row variant: 4 (registers for 3 blocks per SM) or 5 (for 4)
   DevScalars* sc = nullptr;
   DevScalars* sc_host = nullptr;  // pinned
   cudaGraphExec_t graph = nullptr;
@@ -280,10 +281,10 @@ int upload_pack_roots(chgpu_handle* h, void** dst, int n, long double scale) {
 // per-pass twiddles of a register-blocked plan (rfft.cuh): pass p >= 1 at
 // rplan_twoff(p), R-1 forward roots w_{Ns R}^{r k} (r = 1..R-1) per k < Ns
 template <typename V2>
-int upload_rplan_twiddles(chgpu_handle* h, void** dst, int n) {
+int upload_rplan_twiddles(chgpu_handle* h, void** dst, int n, bool xplan = false) {
   using T = decltype(V2::x);
   int E = 0, TPR = 0;
-  if (!rlen_plan(n, &E, &TPR)) return 0;
+  if (!(xplan ? xlen_plan(n, &E, &TPR) : rlen_plan(n, &E, &TPR))) return 0;
   const int np = rplan_passes(E, TPR);
   std::vector<V2> w(std::max(1, rplan_twsize(E, TPR)));
   for (int p = 1; p < np; ++p) {
@@ -344,7 +345,7 @@ ConvLaunch conv_launch(chgpu_handle* h, int compute_cfl, int products, int plane
   L.sc = h->sc;
   L.zcols = h->zcols;
   L.xrows = h->xrows;
-  L.xminb = h->xminb;
+  L.xminb = h->xfast ? h->xrvar : h->xminb;
   L.zthreads = h->zthreads;
   L.xthreads = h->xthreads;
   L.ix_lo = 0;
@@ -625,7 +626,7 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
     // kernel spills: 820 vs 354 ms)
     int e_ = 0, tpr_ = 0;
     h->zfast = rlen_plan(nzd, &e_, &tpr_) && h->prec != CHGPU_FP64DD;
-    h->xfast = rlen_plan(nxd, &e_, &tpr_) && nxd <= 768 && h->prec == CHGPU_MIXED;
+    h->xfast = xlen_plan(nxd, &e_, &tpr_) && h->prec == CHGPU_MIXED;
   }
   h->halves = d.npairs >= 65536 ? 2 : 1;
   h->split_solve = d.npairs < 65536;
@@ -688,7 +689,7 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
       if ((rc = upload_stage_twiddles<float2>(h, &h->twx, h->rx))) break;
       if ((rc = upload_pack_roots<float2>(h, &h->twh, 2 * nxd, 0.5L * (long double)d.factor))) break;
       if ((rc = upload_rplan_twiddles<float2>(h, &h->twzr, nzd))) break;
-      if ((rc = upload_rplan_twiddles<float2>(h, &h->twxr, nxd))) break;
+      if ((rc = upload_rplan_twiddles<float2>(h, &h->twxr, nxd, true))) break;
       if ((rc = upload_derT<float>(h))) break;
       if ((rc = upload_derL<dd>(h))) break;
     } else if (h->prec == CHGPU_FP64DD) {
@@ -696,7 +697,7 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
       if ((rc = upload_stage_twiddles<cdd>(h, &h->twx, h->rx))) break;
       if ((rc = upload_pack_roots<cdd>(h, &h->twh, 2 * nxd, 0.5L * (long double)d.factor))) break;
       if ((rc = upload_rplan_twiddles<cdd>(h, &h->twzr, nzd))) break;
-      if ((rc = upload_rplan_twiddles<cdd>(h, &h->twxr, nxd))) break;
+      if ((rc = upload_rplan_twiddles<cdd>(h, &h->twxr, nxd, true))) break;
       if ((rc = upload_derT<dd>(h))) break;
       if ((rc = upload_derL<double>(h))) break;
     } else {
@@ -704,7 +705,7 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
       if ((rc = upload_stage_twiddles<double2>(h, &h->twx, h->rx))) break;
       if ((rc = upload_pack_roots<double2>(h, &h->twh, 2 * nxd, 0.5L * (long double)d.factor))) break;
       if ((rc = upload_rplan_twiddles<double2>(h, &h->twzr, nzd))) break;
-      if ((rc = upload_rplan_twiddles<double2>(h, &h->twxr, nxd))) break;
+      if ((rc = upload_rplan_twiddles<double2>(h, &h->twxr, nxd, true))) break;
       if ((rc = upload_derT<double>(h))) break;
       if ((rc = upload_derL<double>(h))) break;
     }
@@ -1181,6 +1182,20 @@ int chgpu_autotune(chgpu_handle* h) {
   }
   h->zthreads = best_zt;
   }
+  // the register-blocked x-row kernel's register cap (3 or 4 resident blocks)
+  if (h->xfast) {
+    float best_v = 1e30f;
+    int bv = h->xrvar;
+    for (int v = 4; v <= 5; ++v) {
+      h->xrvar = v;
+      if (int rc = time_conv_stage(h, 1, reps, &ms)) return rc;
+      if (ms < best_v) {
+        best_v = ms;
+        bv = v;
+      }
+    }
+    h->xrvar = bv;
+  }
   // rows per block and register-cap variant of the x-row kernel, then its block size
   if (!h->xfast) {
     int best_r = h->xrows, best_b = h->xminb;
@@ -1229,16 +1244,17 @@ int chgpu_set_tiles(chgpu_handle* h, const int tiles[CHGPU_NTILES]) {
   const int zc = tiles[0], xr = tiles[1], xb = tiles[2], zt = tiles[3], xt = tiles[4];
   auto threads_ok = [](int t) { return t >= 64 && t <= 256 && t % 32 == 0; };
   int e_ = 0, tpr_ = 0;
-  const bool zplan = rlen_plan(h->d.nzd, &e_, &tpr_), xplan = rlen_plan(h->d.nxd, &e_, &tpr_) && h->d.nxd <= 768;
+  const bool zplan = rlen_plan(h->d.nzd, &e_, &tpr_), xplan = xlen_plan(h->d.nxd, &e_, &tpr_);
   if ((zc == 0 && !zplan) || (zc != 0 && (zc < 1 || zc > 8 || conv_zinv_smem(zc, h->d.nzd, h->d.nzt, ts) > lim)) ||
       (xr != 1 && xr != 2 && xr != 4) || h->d.nzd % xr != 0 || conv_x_smem(xr, h->d.nxd, ts) > lim ||
-      (xb == 0 && !xplan) || xb < 0 || xb > 3 || !threads_ok(zt) || !threads_ok(xt))
+      (xb >= 4 && !xplan) || xb < 1 || xb > 5 || !threads_ok(zt) || !threads_ok(xt))
     return fail(h, CHGPU_E_PARAM, "chgpu_set_tiles: tiles outside what this handle's sizes allow");
   h->zfast = zc == 0;
   if (zc != 0) h->zcols = zc;
   h->xrows = xr;
-  h->xfast = xb == 0;
-  if (xb != 0) h->xminb = xb;
+  h->xfast = xb >= 4;
+  if (xb >= 4) h->xrvar = xb;
+  else h->xminb = xb;
   h->zthreads = zt;
   h->xthreads = xt;
   ++h->version;
@@ -1266,7 +1282,7 @@ int chgpu_tiles(const chgpu_handle* h, int tiles[CHGPU_NTILES]) {
   if (!h || !tiles) return CHGPU_E_PARAM;
   tiles[0] = h->zfast ? 0 : h->zcols;
   tiles[1] = h->xrows;
-  tiles[2] = h->xfast ? 0 : h->xminb;
+  tiles[2] = h->xfast ? h->xrvar : h->xminb;
   tiles[3] = h->zthreads;
   tiles[4] = h->xthreads;
   return 0;

@@ -58,13 +58,22 @@ __device__ __forceinline__ void rblock_max_atomic(double v, double* target) {
 
 // blocks of the z kernels: 256 threads, at most 32 columns
 template <int TPR> constexpr int z_cols() { return (256 / TPR) < 32 ? (256 / TPR) : 32; }
-// rows per x block: as many as keep the block's shared memory near 100 KB
-// (two resident blocks per SM), at least one warp, at most 32
+// rows per x block: as many as keep the block's shared memory within 74 KB
+// (three resident blocks per SM), at least one warp, at most 256 threads
 template <int M, int TPR, int S> constexpr int x_rows() {
   int nr = 32;
-  while (nr > 1 && nr * (4 * M + TPR + 1) * S > 102 * 1024) nr /= 2;
+  while (nr > 1 && (nr * (3 * M + TPR + 1) * S > 74 * 1024 || nr * TPR > 256)) nr /= 2;
   while (nr * TPR < 32) nr *= 2;
   return nr;
+}
+// resident blocks per SM the x-row kernel's registers are capped for: as
+// many as its shared memory lets share an SM (1 KB reserved per block), at
+// most CAP (tiles x-row variant 4: 3, variant 5: 4; the autotuner times both)
+template <int M, int TPR, int S, int CAP> constexpr int x_minb() {
+  const int bytes = x_rows<M, TPR, S>() * (3 * M + TPR + 1) * S + 1024;
+  const int by_smem = 233472 / bytes;
+  const int b = by_smem < CAP ? by_smem : CAP;
+  return b < 1 ? 1 : b;
 }
 
 }  // namespace
@@ -129,27 +138,36 @@ __global__ void __launch_bounds__(NC * TPR) k_zfwd_r(const typename C2<T>::t* __
   });
 }
 
-template <typename T, int E, int TPR, int NR>
-__global__ void __launch_bounds__(NR * TPR) k_xrow_r(const typename C2<T>::t* __restrict__ Zb,
-                                                     typename C2<T>::t* __restrict__ Pb,
-                                                     const typename C2<T>::t* __restrict__ tw,
-                                                     const typename C2<T>::t* __restrict__ twh,
-                                                     const T* __restrict__ cst, Dims d, int plane0, int compute_cfl,
-                                                     DevScalars* sc) {
+// Row layout in shared memory: u and v in physical space (M each), then the
+// padded exchange buffer X (M + TPR), which first holds the row's w
+// spectrum.  w itself stays in registers after its transform: the last pass
+// leaves each thread exactly the elements the products' forward transforms
+// start from, so only u and v need shared memory.
+template <int M, int TPR> constexpr int x_row_stride() { return 3 * M + TPR + 1; }
+
+template <typename T, int E, int TPR, int NR, int MINB>
+__global__ void __launch_bounds__(NR * TPR, MINB) k_xrow_r(const typename C2<T>::t* __restrict__ Zb,
+                                                           typename C2<T>::t* __restrict__ Pb,
+                                                           const typename C2<T>::t* __restrict__ tw,
+                                                           const typename C2<T>::t* __restrict__ twh,
+                                                           const T* __restrict__ cst, Dims d, int plane0,
+                                                           int compute_cfl, DevScalars* sc) {
   using V2 = typename C2<T>::t;
   constexpr int M = E * TPR;
-  constexpr int RS = 4 * M + TPR + 1;  // per row: u, v, w (M each), the padded exchange buffer, one bank shift
+  constexpr int RS = x_row_stride<M, TPR>();
   constexpr int NT = NR * TPR;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V2* S = reinterpret_cast<V2*>(smem_raw);
   const int row = threadIdx.x / TPR, t = threadIdx.x % TPR;
-  V2* ph = S + row * RS;
-  V2* xb = ph + 3 * M;
+  V2* U = S + row * RS;
+  V2* Vv = U + M;
+  V2* X = U + 2 * M;
   const int nx = d.nx, nxp = nx + 1, nzd = d.nzd;
   const int plane = plane0 + blockIdx.y;
   const int jz0 = blockIdx.x * NR;
   const int nrow = min(NR, nzd - jz0);
-  // the block's rows of the three spectra (zTOx): NR consecutive jz per kx
+  // the block's rows of the three spectra (zTOx): NR consecutive jz per kx,
+  // u into U, v into V, w into X
   for (int c = 0; c < 3; ++c) {
     const V2* src = Zb + ((size_t)c * d.nplanes + plane) * nxp * nzd + jz0;
     for (int i = threadIdx.x; i < nxp * NR; i += NT) {
@@ -160,24 +178,31 @@ __global__ void __launch_bounds__(NR * TPR) k_xrow_r(const typename C2<T>::t* __
     }
   }
   __syncthreads();
-  // u, v, w: c2r by the half-length packing
+  // c2r by the half-length packing
   //   Z[k] = (X[k] + conj X[M-k]) + i (X[k] - conj X[M-k]) e^{+i pi k / M}
   // (only Re of the kx = 0 entry; the x zero band kx > nx, dnsdata.f90:535)
-#pragma unroll 1
-  for (int c = 0; c < 3; ++c) {
-    V2* X = ph + c * M;
-    V2 a[E];
+  auto pack = [&](const V2* F, V2 (&a)[E]) {
 #pragma unroll
     for (int e = 0; e < E; ++e) {
       const int n = t + TPR * e;
-      V2 xk = n <= nx ? X[n] : czero<V2>();
+      V2 xk = n <= nx ? F[n] : czero<V2>();
       V2 xm = czero<V2>();
       if (n == 0) xk.y = T();
-      else if (M - n <= nx) xm = conjg(X[M - n]);
+      else if (M - n <= nx) xm = conjg(F[M - n]);
       const V2 ev = xk + xm, od = cmul_s<+1>(xk - xm, ldg_v(twh + n));
       a[e] = ev + mul_is<+1>(od);
     }
-    rfft<E, TPR, +1>(a, xb, t, tw, [&](int o, V2 v) { X[o] = v; });
+  };
+  V2 w[E];  // w in physical space, w[e] at x pair t + TPR e
+  pack(X, w);
+  group_sync<TPR>();  // every read of the w spectrum before X becomes the exchange buffer
+  rfft_regs<E, TPR, +1>(w, X, t, tw);
+#pragma unroll 1
+  for (int c = 0; c < 2; ++c) {
+    V2* F = c == 0 ? U : Vv;
+    V2 a[E];
+    pack(F, a);
+    rfft<E, TPR, +1>(a, X, t, tw, [&](int o, V2 v) { F[o] = v; });
   }
   group_sync<TPR>();
   // CFL (dnsdata.f90:552-556) over the physical values of this row
@@ -187,12 +212,12 @@ __global__ void __launch_bounds__(NR * TPR) k_xrow_r(const typename C2<T>::t* __
     if (plane >= 2 && plane <= d.ny && row < nrow) {
       using Nm = Num<T>;
       const T rdx = cst[1], rdz = cst[2], rdy = cst[3 + plane];
-#pragma unroll 4
+#pragma unroll
       for (int e = 0; e < E; ++e) {
         const int n = t + TPR * e;
-        const V2 u = ph[n], v = ph[M + n], w = ph[2 * M + n];
-        const T c0 = Nm::abs(u.x) * rdx + Nm::abs(v.x) * rdy + Nm::abs(w.x) * rdz;
-        const T c1 = Nm::abs(u.y) * rdx + Nm::abs(v.y) * rdy + Nm::abs(w.y) * rdz;
+        const V2 u = U[n], v = Vv[n], ww = w[e];
+        const T c0 = Nm::abs(u.x) * rdx + Nm::abs(v.x) * rdy + Nm::abs(ww.x) * rdz;
+        const T c1 = Nm::abs(u.y) * rdx + Nm::abs(v.y) * rdy + Nm::abs(ww.y) * rdz;
         cfl = Nm::max(cfl, Nm::max(c0, c1));
         bad = bad || !Nm::finite(c0) || !Nm::finite(c1);
       }
@@ -201,23 +226,32 @@ __global__ void __launch_bounds__(NR * TPR) k_xrow_r(const typename C2<T>::t* __
     if (bad) cd = (double)INFINITY;  // a non-finite velocity shows up as an infinite CFL
     rblock_max_atomic(cd, &sc->cfl);
   }
-  // products uu, vv, ww, uv, vw, uw (dnsdata.f90:581-584); `factor` enters in
+  // products (dnsdata.f90:581-584), those with w first (w then dies):
+  // ww, vw, uw, uu, vv, uv -> Pb slots 2, 4, 5, 0, 1, 3; `factor` enters in
   // the unpacking, g = factor/2 and twh[2M + k] = (factor/2) e^{-i pi k/M}
   const T g = cst[0];
 #pragma unroll 1
-  for (int p = 0; p < 6; ++p) {
-    const int fa = p < 3 ? p : (p == 5 ? 0 : p - 3);
-    const int fb = p < 3 ? p : (p == 3 ? 1 : 2);
-    const V2* A = ph + fa * M;
-    const V2* B = ph + fb * M;
+  for (int q = 0; q < 6; ++q) {
+    const int p = q == 0 ? 2 : q == 1 ? 4 : q == 2 ? 5 : q == 3 ? 0 : q == 4 ? 1 : 3;
     V2 a[E];
+    if (q < 3) {
+      const V2* B = q == 1 ? Vv : U;
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-      const int n = t + TPR * e;
-      const V2 x = A[n], y = B[n];
-      a[e] = mk<V2>(x.x * y.x, x.y * y.y);
+      for (int e = 0; e < E; ++e) {
+        const V2 y = w[e], x = q == 0 ? y : B[t + TPR * e];
+        a[e] = mk<V2>(x.x * y.x, x.y * y.y);
+      }
+    } else {
+      const V2* A = q == 4 ? Vv : U;
+      const V2* B = q == 3 ? U : Vv;
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int n = t + TPR * e;
+        const V2 x = A[n], y = B[n];
+        a[e] = mk<V2>(x.x * y.x, x.y * y.y);
+      }
     }
-    rfft<E, TPR, -1>(a, xb, t, tw, [&](int o, V2 v) { xb[o] = v; });
+    rfft<E, TPR, -1>(a, X, t, tw, [&](int o, V2 v) { X[o] = v; });
     group_sync<TPR>();
     // r2c unpacking, kx = 0..nx (HFT, dnsdata.f90:586):
     //   X = g (Z_k + conj Z_{M-k}) + (g w_k) (-i) (Z_k - conj Z_{M-k})
@@ -225,14 +259,14 @@ __global__ void __launch_bounds__(NR * TPR) k_xrow_r(const typename C2<T>::t* __
     for (int e = 0; e < E; ++e) {
       const int k = t + TPR * e;
       if (k <= nx) {
-        const V2 zk = xb[k];
-        const V2 zm = conjg(xb[k == 0 ? 0 : M - k]);
+        const V2 zk = X[k];
+        const V2 zm = conjg(X[k == 0 ? 0 : M - k]);
         const V2 sm = zk + zm, df = zk - zm;
-        const V2 w = ldg_v(twh + 2 * M + k);
+        const V2 wk = ldg_v(twh + 2 * M + k);
         if constexpr (std::is_same<T, dd>::value) {
-          a[e] = scale(sm, g) + cmul(w, mk<V2>(df.y, T() - df.x));
+          a[e] = scale(sm, g) + cmul(wk, mk<V2>(df.y, T() - df.x));
         } else {
-          a[e] = mk<V2>(fma(g, sm.x, fma(w.x, df.y, w.y * df.x)), fma(g, sm.y, fma(w.y, df.y, -(w.x * df.x))));
+          a[e] = mk<V2>(fma(g, sm.x, fma(wk.x, df.y, wk.y * df.x)), fma(g, sm.y, fma(wk.y, df.y, -(wk.x * df.x))));
         }
       }
     }
@@ -240,14 +274,14 @@ __global__ void __launch_bounds__(NR * TPR) k_xrow_r(const typename C2<T>::t* __
 #pragma unroll
     for (int e = 0; e < E; ++e) {
       const int k = t + TPR * e;
-      if (k <= nx) xb[k] = a[e];
+      if (k <= nx) X[k] = a[e];
     }
     __syncthreads();
     // xTOz: the block's rows of product p, NR consecutive jz per kx
     V2* dst = Pb + ((size_t)p * d.nplanes + plane) * nxp * nzd + jz0;
     for (int i = threadIdx.x; i < nxp * NR; i += NT) {
       const int r = i % NR, k = i / NR;
-      if (r < nrow) dst[(size_t)k * nzd + r] = S[r * RS + 3 * M + k];
+      if (r < nrow) dst[(size_t)k * nzd + r] = S[r * RS + 2 * M + k];
     }
     __syncthreads();
   }
@@ -272,14 +306,15 @@ void launch_z_len(const ConvLaunch& L, cudaStream_t s, int stage) {
   }
 }
 
-template <typename T, int M>
+template <typename T, int M, int CAP>
 void launch_x_len(const ConvLaunch& L, cudaStream_t s) {
   using V2 = typename C2<T>::t;
-  constexpr int E = RLen<M>::E, TPR = RLen<M>::TPR, NR = x_rows<M, TPR, (int)sizeof(V2)>();
-  const size_t sm = (size_t)NR * (4 * M + TPR + 1) * sizeof(V2);
+  constexpr int E = XLen<M>::E, TPR = XLen<M>::TPR, NR = x_rows<M, TPR, (int)sizeof(V2)>();
+  constexpr int MINB = x_minb<M, TPR, (int)sizeof(V2), CAP>();
+  const size_t sm = (size_t)NR * x_row_stride<M, TPR>() * sizeof(V2);
   const Dims& d = L.d;
   dim3 grid((d.nzd + NR - 1) / NR, L.nplanes);
-  k_xrow_r<T, E, TPR, NR><<<grid, NR * TPR, sm, s>>>((const V2*)L.Zb, (V2*)L.Pb, (const V2*)L.twxr, (const V2*)L.twh,
+  k_xrow_r<T, E, TPR, NR, MINB><<<grid, NR * TPR, sm, s>>>((const V2*)L.Zb, (V2*)L.Pb, (const V2*)L.twxr, (const V2*)L.twh,
                                                       (const T*)L.cst, d, L.plane0, L.compute_cfl, L.sc);
 }
 
@@ -290,8 +325,12 @@ template <int N> constexpr bool x_plan() { return N <= 768; }
 template <typename T, int N>
 bool launch_len(const ConvLaunch& L, cudaStream_t s, int stage) {
   if (stage == 1) {
-    if constexpr (x_plan<N>()) launch_x_len<T, N>(L, s);
-    else return false;
+    if constexpr (x_plan<N>()) {
+      if (L.xminb == 5) launch_x_len<T, N, 4>(L, s);
+      else launch_x_len<T, N, 3>(L, s);
+    } else {
+      return false;
+    }
   } else {
     launch_z_len<T, N>(L, s, stage);
   }
@@ -300,18 +339,25 @@ bool launch_len(const ConvLaunch& L, cudaStream_t s, int stage) {
 
 template <typename K>
 cudaError_t allow_smem(K* kernel, size_t bytes) {
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  // the largest shared-memory carveout: residency is limited by shared memory
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  return e;
 }
 
 template <typename T, int N>
 cudaError_t set_limits_len() {
   using V2 = typename C2<T>::t;
   constexpr int E = RLen<N>::E, TPR = RLen<N>::TPR, NC = z_cols<TPR>();
-  constexpr int NR = x_rows<N, TPR, (int)sizeof(V2)>();
   cudaError_t e = allow_smem(k_zinv_r<T, E, TPR, NC>, (size_t)NC * rbuf_size<E, TPR>() * sizeof(V2));
   if (e == cudaSuccess) e = allow_smem(k_zfwd_r<T, E, TPR, NC>, (size_t)NC * rbuf_size<E, TPR>() * sizeof(V2));
-  if constexpr (x_plan<N>())
-    if (e == cudaSuccess) e = allow_smem(k_xrow_r<T, E, TPR, NR>, (size_t)NR * (4 * N + TPR + 1) * sizeof(V2));
+  if constexpr (x_plan<N>()) {
+    constexpr int XE = XLen<N>::E, XT = XLen<N>::TPR, XNR = x_rows<N, XT, (int)sizeof(V2)>();
+    constexpr size_t xsm = (size_t)XNR * x_row_stride<N, XT>() * sizeof(V2);
+    constexpr int MB3 = x_minb<N, XT, (int)sizeof(V2), 3>(), MB4 = x_minb<N, XT, (int)sizeof(V2), 4>();
+    if (e == cudaSuccess) e = allow_smem(k_xrow_r<T, XE, XT, XNR, MB3>, xsm);
+    if (e == cudaSuccess) e = allow_smem(k_xrow_r<T, XE, XT, XNR, MB4>, xsm);
+  }
   return e;
 }
 

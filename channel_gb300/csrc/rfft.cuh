@@ -24,6 +24,8 @@
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "cplx.cuh"
 
 namespace chgpu {
@@ -89,6 +91,31 @@ template <int E, int SIGN, typename V> __device__ __forceinline__ void rpass_fir
   Dft<E, V>::template run<SIGN>(a);
 }
 
+// The R-1 twiddles w^1..w^(R-1) of one butterfly from its run of the
+// table.  FP32: only w^1, w^2, w^4 are loaded and the others formed as
+// products (w^3 = w w^2, w^5 = w w^4, w^6 = w^2 w^4, w^7 = w^3 w^4: at most
+// two more roundings, ~1e-7), which halves the loads that dominate the
+// kernels' latency; FP64 and double-float load every value (their
+// multiplications are what bounds them).
+template <int R, typename V> __device__ __forceinline__ void load_twiddles(const V* w, V (&tw)[R]) {
+  if constexpr (std::is_same<V, float2>::value && R == 8) {
+    tw[1] = ldg_v(w);
+    tw[2] = ldg_v(w + 1);
+    tw[4] = ldg_v(w + 3);
+    tw[3] = cmul(tw[1], tw[2]);
+    tw[5] = cmul(tw[1], tw[4]);
+    tw[6] = cmul(tw[2], tw[4]);
+    tw[7] = cmul(tw[3], tw[4]);
+  } else if constexpr (std::is_same<V, float2>::value && R == 4) {
+    tw[1] = ldg_v(w);
+    tw[2] = ldg_v(w + 1);
+    tw[3] = cmul(tw[1], tw[2]);
+  } else {
+#pragma unroll
+    for (int r = 1; r < R; ++r) tw[r] = ldg_v(w + r - 1);
+  }
+}
+
 // Writes the outputs of a pass whose inputs are in a[] (pass p >= 1) or the
 // outputs of pass 1 (p == 0, a[] already transformed) to buf.
 template <int E, int TPR, int P, int SIGN, bool PADDED, typename V>
@@ -112,9 +139,10 @@ __device__ __forceinline__ void rpass_store(V (&a)[E], V* buf, int t, const V* _
       V b[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) b[r] = a[i + r * B];
-      const V* w = twp + k * (R - 1);
+      V tw_[R];
+      load_twiddles<R>(twp + k * (R - 1), tw_);
 #pragma unroll
-      for (int r = 1; r < R; ++r) b[r] = cmul_s_inner<SIGN>(b[r], ldg_v(w + r - 1));
+      for (int r = 1; r < R; ++r) b[r] = cmul_s_inner<SIGN>(b[r], tw_[r]);
       Dft<R, V>::template run<SIGN>(b);
       const int base = (j - k) * R + k;
 #pragma unroll
@@ -131,15 +159,19 @@ template <int E, int TPR, typename V> __device__ __forceinline__ void rload(V (&
   for (int e = 0; e < E; ++e) a[e] = buf[rpad<E>(t + TPR * e)];
 }
 
-// The last pass's butterflies with a caller-supplied sink for each output
-// (natural order index o = j + r Ns): sink(o, value).
-template <int E, int TPR, int SIGN, typename V, typename Sink>
-__device__ __forceinline__ void rpass_last(V (&a)[E], int t, const V* __restrict__ tw, Sink sink) {
+// The last pass's butterflies.  Their outputs j + r Ns (j = t + TPR i < Ns =
+// N/R) are the elements x[t + TPR e], e = i + r E/R, of the same thread: the
+// output distribution equals the input distribution.  TO_REGS keeps them
+// in a[] (a[e] = x[t + TPR e]); otherwise each goes to sink(index, value).
+template <int E, int TPR, int SIGN, bool TO_REGS, typename V, typename Sink>
+__device__ __forceinline__ void rpass_last_any(V (&a)[E], int t, const V* __restrict__ tw, Sink sink) {
   constexpr int NP = rplan_passes(E, TPR);
   if constexpr (NP == 1) {
     // the only pass: a[r] is output r of butterfly t = 0 (TPR == 1)
+    if constexpr (!TO_REGS) {
 #pragma unroll
-    for (int r = 0; r < E; ++r) sink(r, a[r]);
+      for (int r = 0; r < E; ++r) sink(r, a[r]);
+    }
   } else {
     constexpr int P = NP - 1;
     constexpr int R = rplan_radix(E, TPR, P);
@@ -153,46 +185,62 @@ __device__ __forceinline__ void rpass_last(V (&a)[E], int t, const V* __restrict
       V b[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) b[r] = a[i + r * B];
-      const V* w = twp + j * (R - 1);
+      V tw_[R];
+      load_twiddles<R>(twp + j * (R - 1), tw_);
 #pragma unroll
-      for (int r = 1; r < R; ++r) b[r] = cmul_s_inner<SIGN>(b[r], ldg_v(w + r - 1));
+      for (int r = 1; r < R; ++r) b[r] = cmul_s_inner<SIGN>(b[r], tw_[r]);
       Dft<R, V>::template run<SIGN>(b);
 #pragma unroll
-      for (int r = 0; r < R; ++r) sink(j + r * Ns, b[r]);
+      for (int r = 0; r < R; ++r) {
+        if constexpr (TO_REGS) a[i + r * B] = b[r];
+        else sink(j + r * Ns, b[r]);
+      }
     }
   }
 }
 
-// Whole transform: a[] holds the input distribution (x[t + TPR e]); buf is
-// the group's padded exchange buffer (rbuf_size elements); the outputs are
-// handed to sink(index, value) in the last pass.  Every thread of the group
-// calls it; the caller synchronises before reusing buf.
-template <int E, int TPR, int SIGN, typename V, typename Sink>
-__device__ __forceinline__ void rfft(V (&a)[E], V* buf, int t, const V* __restrict__ tw, Sink sink) {
+// Every pass but the last: a[] holds the input distribution on entry and the
+// last pass's inputs on return; buf is the group's padded exchange buffer
+// (rbuf_size elements).  Every thread of the group calls it.
+template <int E, int TPR, int SIGN, typename V>
+__device__ __forceinline__ void rfft_head(V (&a)[E], V* buf, int t, const V* __restrict__ tw) {
   constexpr int NP = rplan_passes(E, TPR);
   rpass_first<E, SIGN>(a);
-  if constexpr (NP == 1) {
-    rpass_last<E, TPR, SIGN>(a, t, tw, sink);
-  } else {
+  if constexpr (NP >= 2) {
     rpass_store<E, TPR, 0, SIGN, true>(a, buf, t, tw);
     group_sync<TPR>();
     rload<E, TPR>(a, buf, t);
     group_sync<TPR>();
-    if constexpr (NP >= 3) {
-      rpass_store<E, TPR, 1, SIGN, true>(a, buf, t, tw);
-      group_sync<TPR>();
-      rload<E, TPR>(a, buf, t);
-      group_sync<TPR>();
-    }
-    if constexpr (NP >= 4) {
-      rpass_store<E, TPR, 2, SIGN, true>(a, buf, t, tw);
-      group_sync<TPR>();
-      rload<E, TPR>(a, buf, t);
-      group_sync<TPR>();
-    }
-    static_assert(NP <= 4, "at most four passes");
-    rpass_last<E, TPR, SIGN>(a, t, tw, sink);
   }
+  if constexpr (NP >= 3) {
+    rpass_store<E, TPR, 1, SIGN, true>(a, buf, t, tw);
+    group_sync<TPR>();
+    rload<E, TPR>(a, buf, t);
+    group_sync<TPR>();
+  }
+  if constexpr (NP >= 4) {
+    rpass_store<E, TPR, 2, SIGN, true>(a, buf, t, tw);
+    group_sync<TPR>();
+    rload<E, TPR>(a, buf, t);
+    group_sync<TPR>();
+  }
+  static_assert(NP <= 4, "at most four passes");
+}
+
+// Whole transform, a[] holding the input distribution (x[t + TPR e]) on
+// entry, the outputs handed to sink(index, value).  The caller synchronises
+// the group before reusing buf.
+template <int E, int TPR, int SIGN, typename V, typename Sink>
+__device__ __forceinline__ void rfft(V (&a)[E], V* buf, int t, const V* __restrict__ tw, Sink sink) {
+  rfft_head<E, TPR, SIGN>(a, buf, t, tw);
+  rpass_last_any<E, TPR, SIGN, false>(a, t, tw, sink);
+}
+
+// Whole transform with the outputs left in a[] (a[e] = x[t + TPR e]).
+template <int E, int TPR, int SIGN, typename V>
+__device__ __forceinline__ void rfft_regs(V (&a)[E], V* buf, int t, const V* __restrict__ tw) {
+  rfft_head<E, TPR, SIGN>(a, buf, t, tw);
+  rpass_last_any<E, TPR, SIGN, true>(a, t, tw, [](int, V) {});
 }
 
 // Compile-time plans of the lengths with register-blocked kernels.
@@ -205,6 +253,31 @@ template <> struct RLen<192> { static constexpr int E = 24, TPR = 8; };
 template <> struct RLen<384> { static constexpr int E = 24, TPR = 16; };
 template <> struct RLen<768> { static constexpr int E = 24, TPR = 32; };
 template <> struct RLen<1536> { static constexpr int E = 24, TPR = 64; };
+
+// Plans of the x-row kernel, which keeps a transform's worth of w in
+// registers next to the one it computes: 12 elements per thread (8 for the
+// power-of-two lengths), so that several blocks share an SM.
+template <int N> struct XLen;
+template <> struct XLen<32> { static constexpr int E = 8, TPR = 4; };
+template <> struct XLen<48> { static constexpr int E = 12, TPR = 4; };
+template <> struct XLen<64> { static constexpr int E = 8, TPR = 8; };
+template <> struct XLen<96> { static constexpr int E = 12, TPR = 8; };
+template <> struct XLen<192> { static constexpr int E = 12, TPR = 16; };
+template <> struct XLen<384> { static constexpr int E = 12, TPR = 32; };
+template <> struct XLen<768> { static constexpr int E = 12, TPR = 64; };
+
+inline bool xlen_plan(int n, int* E, int* TPR) {
+  switch (n) {
+    case 32: *E = 8; *TPR = 4; return true;
+    case 48: *E = 12; *TPR = 4; return true;
+    case 64: *E = 8; *TPR = 8; return true;
+    case 96: *E = 12; *TPR = 8; return true;
+    case 192: *E = 12; *TPR = 16; return true;
+    case 384: *E = 12; *TPR = 32; return true;
+    case 768: *E = 12; *TPR = 64; return true;
+    default: return false;
+  }
+}
 
 // host side: does a length have a register-blocked plan, and its (E, TPR)
 inline bool rlen_plan(int n, int* E, int* TPR) {

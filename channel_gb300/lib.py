@@ -360,9 +360,8 @@ class Channel:
             return
         a = np.ascontiguousarray(pressure, dtype=np.complex128)
         assert a.shape == (self.p.nx + 1, 2 * self.p.nz + 1, self.p.ny + 3)
-        # restart-file (Fortran) order: iy fastest
-        f = np.ascontiguousarray(a.transpose(2, 1, 0)).reshape(-1)
-        self._check(self.lib.chgpu_tke_accumulate(self.h, _dp(f.view(np.float64))))
+        # C order of (nx+1, 2nz+1, ny+3) is the restart-file order (iy fastest)
+        self._check(self.lib.chgpu_tke_accumulate(self.h, _dp(a.view(np.float64))))
 
     def tke_result(self, timestwo: bool = False):
         """(mean (7, ny+3), spectra (6, 10, 2nz+1, ny+3), profiles (6, 10, ny+3), samples)."""

@@ -151,8 +151,18 @@ const char* chgpu_ensemble_last_error(const chgpu_ensemble* e);
  * shared-memory budget.  No counterpart in the reference. */
 #define CHGPU_NTILES 5
 int chgpu_autotune(chgpu_handle* h);
-/* tiles = {z columns per block, x rows per block, x-row register variant,
- *          z threads per block, x threads per block}. */
+/* tiles = {z columns per block, x rows per block, x-row variant, z threads
+ *          per block, x threads per block}.  z columns 0: the
+ * register-blocked z kernels (compile-time plans for nzd = 32, 48, 64, 96,
+ * 192, 384, 768, 1536); x-row variant 1-3: the generic kernel with its
+ * registers capped for that many 256-thread blocks per SM, 4 and 5: the
+ * register-blocked x-row kernel (nxd = 32 ... 768) with registers for 3 or
+ * 4 resident blocks.  A handle starts with the register-blocked kernels
+ * where they measured faster (FP32: z and x; FP64: z); the autotuner keeps
+ * that choice and tunes within it, so its tiles do not change the results.
+ * Switching between generic and register-blocked kernels with
+ * chgpu_set_tiles changes the rounding of the transforms (their
+ * factorisations differ), not their accuracy. */
 int chgpu_tiles(const chgpu_handle* h, int tiles[CHGPU_NTILES]);
 /* Applies tiles found by chgpu_autotune on another handle of the same sizes
  * and precision; CHGPU_E_PARAM when they do not fit this handle. */
