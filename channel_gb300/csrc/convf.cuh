@@ -58,19 +58,25 @@ __device__ __forceinline__ void rblock_max_atomic(double v, double* target) {
 
 // blocks of the z kernels: 256 threads, at most 32 columns
 template <int TPR> constexpr int z_cols() { return (256 / TPR) < 32 ? (256 / TPR) : 32; }
+// shared memory per x row: u, v (and w without WREG) in physical space,
+// the padded exchange buffer, one bank shift
+template <int M, int TPR, bool WREG> constexpr int x_row_stride() { return (WREG ? 3 : 4) * M + TPR + 1; }
 // rows per x block: as many as keep the block's shared memory within 74 KB
-// (three resident blocks per SM), at least one warp, at most 256 threads
-template <int M, int TPR, int S> constexpr int x_rows() {
+// with w in registers (three resident blocks per SM) or 102 KB without (two),
+// at least one warp, at most 256 threads
+template <int M, int TPR, bool WREG, int S> constexpr int x_rows() {
   int nr = 32;
-  while (nr > 1 && (nr * (3 * M + TPR + 1) * S > 74 * 1024 || nr * TPR > 256)) nr /= 2;
+  const int budget = (WREG ? 74 : 102) * 1024;
+  while (nr > 1 && (nr * x_row_stride<M, TPR, WREG>() * S > budget || nr * TPR > 256)) nr /= 2;
   while (nr * TPR < 32) nr *= 2;
   return nr;
 }
 // resident blocks per SM the x-row kernel's registers are capped for: as
 // many as its shared memory lets share an SM (1 KB reserved per block), at
 // most CAP (tiles x-row variant 4: 3, variant 5: 4; the autotuner times both)
-template <int M, int TPR, int S, int CAP> constexpr int x_minb() {
-  const int bytes = x_rows<M, TPR, S>() * (3 * M + TPR + 1) * S + 1024;
+template <int M, int TPR, bool WREG, int S, int CAP> constexpr int x_minb() {
+  if (!WREG) return 1;  // no register cap: two blocks' shared memory set the residency
+  const int bytes = x_rows<M, TPR, WREG, S>() * x_row_stride<M, TPR, WREG>() * S + 1024;
   const int by_smem = 233472 / bytes;
   const int b = by_smem < CAP ? by_smem : CAP;
   return b < 1 ? 1 : b;
@@ -140,12 +146,11 @@ __global__ void __launch_bounds__(NC * TPR) k_zfwd_r(const typename C2<T>::t* __
 
 // Row layout in shared memory: u and v in physical space (M each), then the
 // padded exchange buffer X (M + TPR), which first holds the row's w
-// spectrum.  w itself stays in registers after its transform: the last pass
+// spectrum; without WREG a fourth slot W (M) after X holds w in physical
+// space.  With WREG w stays in registers after its transform: the last pass
 // leaves each thread exactly the elements the products' forward transforms
 // start from, so only u and v need shared memory.
-template <int M, int TPR> constexpr int x_row_stride() { return 3 * M + TPR + 1; }
-
-template <typename T, int E, int TPR, int NR, int MINB>
+template <typename T, int E, int TPR, int NR, int MINB, bool WREG>
 __global__ void __launch_bounds__(NR * TPR, MINB) k_xrow_r(const typename C2<T>::t* __restrict__ Zb,
                                                            typename C2<T>::t* __restrict__ Pb,
                                                            const typename C2<T>::t* __restrict__ tw,
@@ -154,7 +159,7 @@ __global__ void __launch_bounds__(NR * TPR, MINB) k_xrow_r(const typename C2<T>:
                                                            int compute_cfl, DevScalars* sc) {
   using V2 = typename C2<T>::t;
   constexpr int M = E * TPR;
-  constexpr int RS = x_row_stride<M, TPR>();
+  constexpr int RS = x_row_stride<M, TPR, WREG>();
   constexpr int NT = NR * TPR;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V2* S = reinterpret_cast<V2*>(smem_raw);
@@ -193,10 +198,23 @@ __global__ void __launch_bounds__(NR * TPR, MINB) k_xrow_r(const typename C2<T>:
       a[e] = ev + mul_is<+1>(od);
     }
   };
-  V2 w[E];  // w in physical space, w[e] at x pair t + TPR e
-  pack(X, w);
-  group_sync<TPR>();  // every read of the w spectrum before X becomes the exchange buffer
-  rfft_regs<E, TPR, +1>(w, X, t, tw);
+  V2* Wp = X + M + TPR;  // w in physical space without WREG
+  V2 w[WREG ? E : 1];    // with WREG: w in physical space, w[e] at x pair t + TPR e
+  if constexpr (WREG) {
+    pack(X, w);
+    group_sync<TPR>();  // every read of the w spectrum before X becomes the exchange buffer
+    rfft_regs<E, TPR, +1>(w, X, t, tw);
+  } else {
+    V2 a[E];
+    pack(X, a);
+    group_sync<TPR>();
+    rfft<E, TPR, +1>(a, X, t, tw, [&](int o, V2 v) { Wp[o] = v; });
+  }
+  // w at pair t + TPR e
+  auto wv = [&](int e) -> V2 {
+    if constexpr (WREG) return w[e];
+    else return Wp[t + TPR * e];
+  };
 #pragma unroll 1
   for (int c = 0; c < 2; ++c) {
     V2* F = c == 0 ? U : Vv;
@@ -215,7 +233,7 @@ __global__ void __launch_bounds__(NR * TPR, MINB) k_xrow_r(const typename C2<T>:
 #pragma unroll
       for (int e = 0; e < E; ++e) {
         const int n = t + TPR * e;
-        const V2 u = U[n], v = Vv[n], ww = w[e];
+        const V2 u = U[n], v = Vv[n], ww = wv(e);
         const T c0 = Nm::abs(u.x) * rdx + Nm::abs(v.x) * rdy + Nm::abs(ww.x) * rdz;
         const T c1 = Nm::abs(u.y) * rdx + Nm::abs(v.y) * rdy + Nm::abs(ww.y) * rdz;
         cfl = Nm::max(cfl, Nm::max(c0, c1));
@@ -238,7 +256,7 @@ __global__ void __launch_bounds__(NR * TPR, MINB) k_xrow_r(const typename C2<T>:
       const V2* B = q == 1 ? Vv : U;
 #pragma unroll
       for (int e = 0; e < E; ++e) {
-        const V2 y = w[e], x = q == 0 ? y : B[t + TPR * e];
+        const V2 y = wv(e), x = q == 0 ? y : B[t + TPR * e];
         a[e] = mk<V2>(x.x * y.x, x.y * y.y);
       }
     } else {
@@ -309,12 +327,14 @@ void launch_z_len(const ConvLaunch& L, cudaStream_t s, int stage) {
 template <typename T, int M, int CAP>
 void launch_x_len(const ConvLaunch& L, cudaStream_t s) {
   using V2 = typename C2<T>::t;
-  constexpr int E = XLen<M>::E, TPR = XLen<M>::TPR, NR = x_rows<M, TPR, (int)sizeof(V2)>();
-  constexpr int MINB = x_minb<M, TPR, (int)sizeof(V2), CAP>();
-  const size_t sm = (size_t)NR * x_row_stride<M, TPR>() * sizeof(V2);
+  constexpr int E = XLen<M>::E, TPR = XLen<M>::TPR;
+  constexpr bool WREG = XLen<M>::WREG;
+  constexpr int NR = x_rows<M, TPR, WREG, (int)sizeof(V2)>();
+  constexpr int MINB = x_minb<M, TPR, WREG, (int)sizeof(V2), CAP>();
+  const size_t sm = (size_t)NR * x_row_stride<M, TPR, WREG>() * sizeof(V2);
   const Dims& d = L.d;
   dim3 grid((d.nzd + NR - 1) / NR, L.nplanes);
-  k_xrow_r<T, E, TPR, NR, MINB><<<grid, NR * TPR, sm, s>>>((const V2*)L.Zb, (V2*)L.Pb, (const V2*)L.twxr, (const V2*)L.twh,
+  k_xrow_r<T, E, TPR, NR, MINB, WREG><<<grid, NR * TPR, sm, s>>>((const V2*)L.Zb, (V2*)L.Pb, (const V2*)L.twxr, (const V2*)L.twh,
                                                       (const T*)L.cst, d, L.plane0, L.compute_cfl, L.sc);
 }
 
@@ -337,11 +357,15 @@ bool launch_len(const ConvLaunch& L, cudaStream_t s, int stage) {
   return true;
 }
 
+// carveout: the x-row kernel with w in registers asks for the largest
+// shared-memory carveout (three or four 74 KB blocks); the others keep the default,
+// whose larger L1 serves their twiddle loads (the largest carveout made
+// z-forward 30% slower)
 template <typename K>
-cudaError_t allow_smem(K* kernel, size_t bytes) {
+cudaError_t allow_smem(K* kernel, size_t bytes, bool max_carveout = false) {
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  // the largest shared-memory carveout: residency is limited by shared memory
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e == cudaSuccess && max_carveout)
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   return e;
 }
 
@@ -352,11 +376,13 @@ cudaError_t set_limits_len() {
   cudaError_t e = allow_smem(k_zinv_r<T, E, TPR, NC>, (size_t)NC * rbuf_size<E, TPR>() * sizeof(V2));
   if (e == cudaSuccess) e = allow_smem(k_zfwd_r<T, E, TPR, NC>, (size_t)NC * rbuf_size<E, TPR>() * sizeof(V2));
   if constexpr (x_plan<N>()) {
-    constexpr int XE = XLen<N>::E, XT = XLen<N>::TPR, XNR = x_rows<N, XT, (int)sizeof(V2)>();
-    constexpr size_t xsm = (size_t)XNR * x_row_stride<N, XT>() * sizeof(V2);
-    constexpr int MB3 = x_minb<N, XT, (int)sizeof(V2), 3>(), MB4 = x_minb<N, XT, (int)sizeof(V2), 4>();
-    if (e == cudaSuccess) e = allow_smem(k_xrow_r<T, XE, XT, XNR, MB3>, xsm);
-    if (e == cudaSuccess) e = allow_smem(k_xrow_r<T, XE, XT, XNR, MB4>, xsm);
+    constexpr int XE = XLen<N>::E, XT = XLen<N>::TPR;
+    constexpr bool WR = XLen<N>::WREG;
+    constexpr int XNR = x_rows<N, XT, WR, (int)sizeof(V2)>();
+    constexpr size_t xsm = (size_t)XNR * x_row_stride<N, XT, WR>() * sizeof(V2);
+    constexpr int MB3 = x_minb<N, XT, WR, (int)sizeof(V2), 3>(), MB4 = x_minb<N, XT, WR, (int)sizeof(V2), 4>();
+    if (e == cudaSuccess) e = allow_smem(k_xrow_r<T, XE, XT, XNR, MB3, WR>, xsm, WR);
+    if (e == cudaSuccess) e = allow_smem(k_xrow_r<T, XE, XT, XNR, MB4, WR>, xsm, WR);
   }
   return e;
 }

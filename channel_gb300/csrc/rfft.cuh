@@ -254,17 +254,20 @@ template <> struct RLen<384> { static constexpr int E = 24, TPR = 16; };
 template <> struct RLen<768> { static constexpr int E = 24, TPR = 32; };
 template <> struct RLen<1536> { static constexpr int E = 24, TPR = 64; };
 
-// Plans of the x-row kernel, which keeps a transform's worth of w in
-// registers next to the one it computes: 12 elements per thread (8 for the
-// power-of-two lengths), so that several blocks share an SM.
+// Plans of the x-row kernel.  WREG: w's physical values stay in registers
+// next to the transform being computed (12 elements per thread, 8 for the
+// power-of-two lengths, so that three or four blocks share an SM); without
+// it w too sits in shared memory and a thread holds 24 elements (measured
+// faster at 768 points, where two 64-thread groups per row would need named
+// barriers at every exchange).
 template <int N> struct XLen;
-template <> struct XLen<32> { static constexpr int E = 8, TPR = 4; };
-template <> struct XLen<48> { static constexpr int E = 12, TPR = 4; };
-template <> struct XLen<64> { static constexpr int E = 8, TPR = 8; };
-template <> struct XLen<96> { static constexpr int E = 12, TPR = 8; };
-template <> struct XLen<192> { static constexpr int E = 12, TPR = 16; };
-template <> struct XLen<384> { static constexpr int E = 12, TPR = 32; };
-template <> struct XLen<768> { static constexpr int E = 12, TPR = 64; };
+template <> struct XLen<32> { static constexpr int E = 8, TPR = 4; static constexpr bool WREG = true; };
+template <> struct XLen<48> { static constexpr int E = 12, TPR = 4; static constexpr bool WREG = true; };
+template <> struct XLen<64> { static constexpr int E = 8, TPR = 8; static constexpr bool WREG = true; };
+template <> struct XLen<96> { static constexpr int E = 12, TPR = 8; static constexpr bool WREG = true; };
+template <> struct XLen<192> { static constexpr int E = 12, TPR = 16; static constexpr bool WREG = true; };
+template <> struct XLen<384> { static constexpr int E = 12, TPR = 32; static constexpr bool WREG = true; };
+template <> struct XLen<768> { static constexpr int E = 24, TPR = 32; static constexpr bool WREG = false; };
 
 inline bool xlen_plan(int n, int* E, int* TPR) {
   switch (n) {
@@ -274,7 +277,7 @@ inline bool xlen_plan(int n, int* E, int* TPR) {
     case 96: *E = 12; *TPR = 8; return true;
     case 192: *E = 12; *TPR = 16; return true;
     case 384: *E = 12; *TPR = 32; return true;
-    case 768: *E = 12; *TPR = 64; return true;
+    case 768: *E = 24; *TPR = 32; return true;
     default: return false;
   }
 }
