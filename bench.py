@@ -34,7 +34,8 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "RK3 steps/s & ns/pt/step, FP64 vs mixed on 1 GB300 at ≤1e-4 stats error"
-AMPLITUDE = {"small": 0.01, "retau180": 0.05, "retau550": 0.05, "coarse": 0.05}
+AMPLITUDE = {"small": 0.01, "retau180": 0.05, "retau550": 0.05, "coarse": 0.05, "probe768": 0.05,
+             "probe1536": 0.05}
 
 
 def dist_env():
@@ -521,7 +522,8 @@ def run_ours(args):
         "data": bench_data(rank, amp),
         "config": bench_config(p, ws),
         "tiles": {k: {"z_cols": t[0], "x_rows": t[1], "x_variant": t[2], "z_threads": t[3],
-                      "x_threads": t[4]} for k, t in TILES.items()},
+                      "x_threads": t[4], "solve_form": t[5] if len(t) > 5 else None,
+                      "step_halves": t[6] if len(t) > 6 else None} for k, t in TILES.items()},
         "tiles_from": "--tiles" if args.tiles else "chgpu_autotune on the first handle of each precision",
         "ns_per_pt_step": ms64 * 1e6 / gpts,
         "ns_per_spectral_pt_step": ms64 * 1e6 / p.spectral_points(),
@@ -685,7 +687,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="retau550", choices=list(AMPLITUDE))
     ap.add_argument("--tiles", default="",
-                    help="fixed transform tiles instead of autotuning, e.g. fp64:8,4,2,256,256/mixed:8,4,3,256,192 "
+                    help="fixed tiles instead of autotuning, e.g. fp64:0,4,2,256,256,2,1/mixed:0,2,4,256,256,1,2 "
                          "(z columns, x rows, x-row variant, z threads, x threads; for reproducible profiler "
                          "captures)")
     ap.add_argument("--mode", default="full", choices=["full", "timed", "long", "closure"],

@@ -673,7 +673,7 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
                         "x work buffer"))) break;
     if ((rc = dev_alloc((void**)&h->rhs, sizeof(double2) * 2 * (p->ny - 1) * nmodes, "rhs"))) break;
     if ((rc = dev_alloc((void**)&h->fac,
-                        sizeof(double) * (h->split_solve ? kFacPerRow : kFacPerRowFused) * (p->ny - 1) *
+                        sizeof(double) * kFacPerRow * (p->ny - 1) *
                             (size_t)d.npairs,
                         "factors")))
       break;
@@ -1134,6 +1134,77 @@ int time_conv_stage(chgpu_handle* h, int stage, int reps, float* ms) {
 
 }  // namespace
 
+namespace {
+
+// The banded solves as one fused kernel (two threads per (kx, +-kz) pair,
+// one per system) or as the factorisation kernel and a substitution kernel
+// with four threads per pair (one per system and mode), and the step on one
+// stream or in two kx halves on two streams: the four combinations timed as
+// whole steps on this handle's sizes, the fastest kept.  All four perform the
+// same operations in the same order (the results are bit-identical).  The
+// field, the RK history and the module scalars are saved first and put back.
+int tune_solve_and_halves(chgpu_handle* h) {
+  const Dims& d = h->d;
+  const size_t vbytes = sizeof(double2) * 3 * (size_t)d.nplanes * d.nmodes;
+  const size_t obytes = tsize(h) * 2 * (size_t)(d.ny - 1) * d.nmodes;
+  void *sv = nullptr, *so = nullptr, *ss = nullptr;
+  if (cudaMalloc(&sv, vbytes) != cudaSuccess || cudaMalloc(&so, obytes) != cudaSuccess ||
+      cudaMalloc(&ss, sizeof(DevScalars)) != cudaSuccess) {
+    // no room for the saved state: keep the current choice
+    cudaGetLastError();
+    if (sv) cudaFree(sv);
+    if (so) cudaFree(so);
+    return 0;
+  }
+  CK(h, cudaMemcpyAsync(sv, h->V, vbytes, cudaMemcpyDeviceToDevice, h->stream));
+  CK(h, cudaMemcpyAsync(so, h->old, obytes, cudaMemcpyDeviceToDevice, h->stream));
+  CK(h, cudaMemcpyAsync(ss, h->sc, sizeof(DevScalars), cudaMemcpyDeviceToDevice, h->stream));
+  const bool prof = h->profiling;
+  h->profiling = false;
+  float best = 1e30f;
+  bool best_split = h->split_solve;
+  int best_halves = h->halves;
+  cudaEvent_t a = take_event(h), b = take_event(h);
+  int rc = 0;
+  for (int form = 0; form < 4 && rc == 0; ++form) {
+    h->split_solve = (form & 1) != 0;
+    h->halves = (form & 2) ? 2 : 1;
+    enqueue_step(h);  // warm-up
+    cudaEventRecord(a, h->stream);
+    enqueue_step(h);
+    cudaEventRecord(b, h->stream);
+    cudaError_t e = cudaEventSynchronize(b);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    if (e != cudaSuccess) {
+      rc = cuda_fail(h, e, "chgpu_autotune: timing the solve forms");
+      break;
+    }
+    if (ms < best) {
+      best = ms;
+      best_split = h->split_solve;
+      best_halves = h->halves;
+    }
+  }
+  h->ev_pool.push_back(a);
+  h->ev_pool.push_back(b);
+  h->split_solve = best_split;
+  h->halves = best_halves;
+  h->profiling = prof;
+  cudaMemcpyAsync(h->V, sv, vbytes, cudaMemcpyDeviceToDevice, h->stream);
+  cudaMemcpyAsync(h->old, so, obytes, cudaMemcpyDeviceToDevice, h->stream);
+  cudaMemcpyAsync(h->sc, ss, sizeof(DevScalars), cudaMemcpyDeviceToDevice, h->stream);
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  cudaFree(sv);
+  cudaFree(so);
+  cudaFree(ss);
+  if (rc == 0 && e != cudaSuccess) rc = cuda_fail(h, e, "chgpu_autotune: restoring the state");
+  return rc;
+}
+
+}  // namespace
+
 int chgpu_autotune(chgpu_handle* h) {
   if (!h) return fail(h, CHGPU_E_PARAM, "null handle");
   int dev = 0, optin = 0;
@@ -1226,6 +1297,7 @@ int chgpu_autotune(chgpu_handle* h) {
   }
   h->xthreads = best_xt;
   }
+  if (int rc = tune_solve_and_halves(h)) return rc;
   h->tuned = true;
   ++h->version;
   if (h->graph) {  // the captured step holds the old launch shapes
@@ -1241,13 +1313,14 @@ int chgpu_set_tiles(chgpu_handle* h, const int tiles[CHGPU_NTILES]) {
   CK(h, cudaGetDevice(&dev));
   CK(h, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   const size_t ts = tsize(h), lim = (size_t)optin - 1024;
-  const int zc = tiles[0], xr = tiles[1], xb = tiles[2], zt = tiles[3], xt = tiles[4];
+  const int zc = tiles[0], xr = tiles[1], xb = tiles[2], zt = tiles[3], xt = tiles[4], sf = tiles[5], hv = tiles[6];
   auto threads_ok = [](int t) { return t >= 64 && t <= 256 && t % 32 == 0; };
   int e_ = 0, tpr_ = 0;
   const bool zplan = rlen_plan(h->d.nzd, &e_, &tpr_), xplan = xlen_plan(h->d.nxd, &e_, &tpr_);
   if ((zc == 0 && !zplan) || (zc != 0 && (zc < 1 || zc > 8 || conv_zinv_smem(zc, h->d.nzd, h->d.nzt, ts) > lim)) ||
       (xr != 1 && xr != 2 && xr != 4) || h->d.nzd % xr != 0 || conv_x_smem(xr, h->d.nxd, ts) > lim ||
-      (xb >= 4 && !xplan) || xb < 1 || xb > 5 || !threads_ok(zt) || !threads_ok(xt))
+      (xb >= 4 && !xplan) || xb < 1 || xb > 5 || !threads_ok(zt) || !threads_ok(xt) || (sf != 1 && sf != 2) ||
+      (hv != 1 && hv != 2))
     return fail(h, CHGPU_E_PARAM, "chgpu_set_tiles: tiles outside what this handle's sizes allow");
   h->zfast = zc == 0;
   if (zc != 0) h->zcols = zc;
@@ -1257,6 +1330,8 @@ int chgpu_set_tiles(chgpu_handle* h, const int tiles[CHGPU_NTILES]) {
   else h->xminb = xb;
   h->zthreads = zt;
   h->xthreads = xt;
+  h->split_solve = sf == 2;
+  h->halves = hv;
   ++h->version;
   if (h->graph) {
     cudaGraphExecDestroy(h->graph);
@@ -1285,6 +1360,8 @@ int chgpu_tiles(const chgpu_handle* h, int tiles[CHGPU_NTILES]) {
   tiles[2] = h->xfast ? h->xrvar : h->xminb;
   tiles[3] = h->zthreads;
   tiles[4] = h->xthreads;
+  tiles[5] = h->split_solve ? 2 : 1;
+  tiles[6] = h->halves;
   return 0;
 }
 

@@ -178,7 +178,8 @@ def write(path, p: DnsIn) -> None:
 # The channel workloads these tools are exercised on (sizes and physics).
 def workload(name: str) -> DnsIn:
     """Named workloads: 'small' 32x64x32 fixed dt, 'retau180' 127x192x127,
-    'retau550' 383x384x383, 'coarse' 47x96x47 on the Re_tau 550 domain."""
+    'retau550' 383x384x383, 'coarse' 47x96x47 on the Re_tau 550 domain; 'probe768' and
+    'probe1536' are small profiling grids with that workload's x / z transform lengths."""
     if name == "small":
         return DnsIn(nx=32, ny=64, nz=32, alfa0=1.0, beta0=2.0, re=4000.0, a=1.6, ymin=0.0, ymax=2.0,
                      meanflowx=4.0 / 3.0, deltat=0.004, cflmax=0.0, nstep=200)
@@ -188,6 +189,14 @@ def workload(name: str) -> DnsIn:
     if name == "retau550":
         return DnsIn(nx=383, ny=384, nz=383, alfa0=0.5, beta0=1.0, re=14000.0, a=1.8, ymin=0.0, ymax=2.0,
                      meanflowx=4.0 / 3.0, deltat=0.0, cflmax=1.0, nstep=100)
+    # profiling probes: the 383x384x383 domain with 64 planes, x rows of that
+    # workload's length (768 complex points) or z columns of it (1536)
+    if name == "probe768":
+        return DnsIn(nx=511, ny=64, nz=64, alfa0=0.5, beta0=1.0, re=14000.0, a=1.8, ymin=0.0, ymax=2.0,
+                     meanflowx=4.0 / 3.0, deltat=0.0, cflmax=1.0, nstep=10)
+    if name == "probe1536":
+        return DnsIn(nx=63, ny=64, nz=383, alfa0=0.5, beta0=1.0, re=14000.0, a=1.8, ymin=0.0, ymax=2.0,
+                     meanflowx=4.0 / 3.0, deltat=0.0, cflmax=1.0, nstep=10)
     if name == "coarse":
         return DnsIn(nx=47, ny=96, nz=47, alfa0=0.5, beta0=1.0, re=14000.0, a=1.8, ymin=0.0, ymax=2.0,
                      meanflowx=4.0 / 3.0, deltat=0.0, cflmax=1.0, nstep=100)

@@ -290,13 +290,18 @@ class Channel:
         return self.tiles()
 
     def tiles(self) -> tuple:
-        """(z columns, x rows, x-row variant, z threads, x threads)."""
-        t = (C.c_int * 5)()
+        """(z columns, x rows, x-row variant, z threads, x threads, solve form,
+        step halves)."""
+        t = (C.c_int * 7)()
         self._check(self.lib.chgpu_tiles(self.h, t))
         return tuple(t)
 
     def set_tiles(self, tiles) -> None:
-        self._check(self.lib.chgpu_set_tiles(self.h, (C.c_int * 5)(*tiles)))
+        """Tiles of tiles(); five values keep this handle's solve form and halves."""
+        tiles = tuple(tiles)
+        if len(tiles) == 5:
+            tiles = tiles + self.tiles()[5:]
+        self._check(self.lib.chgpu_set_tiles(self.h, (C.c_int * 7)(*tiles)))
 
     def set_step_halves(self, halves: int) -> None:
         """1: the step on one stream; 2: rhs / solve split in two kx halves on two streams."""

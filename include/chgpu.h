@@ -140,19 +140,24 @@ void* chgpu_ensemble_stream(chgpu_ensemble* e);
 /* Message of the ensemble's last failing call (or of a failed create). */
 const char* chgpu_ensemble_last_error(const chgpu_ensemble* e);
 
-/* Autotuner of the transform tiles: times the z-transform kernels for 1, 2,
- * 4 and 8 columns per block and then 128, 192 or 256 threads per block, and
- * the x-row kernel for 1, 2 and 4 rows per block in each of its
- * register-cap variants (compiled for 1, 2 and 3 resident blocks per SM) and
- * then its block size, on this handle's sizes, and keeps the fastest.  Takes
- * a few dozen kernel launches; the field, the RK history and the module
- * scalars are untouched, and the results of a step do not depend on the
- * tiles.  Optional: without it the handle uses tiles sized from the
- * shared-memory budget.  No counterpart in the reference. */
-#define CHGPU_NTILES 5
+/* Autotuner of the step's launch shapes on this handle's sizes: the z
+ * transforms (1, 2, 4 or 8 columns per block, then 128, 192 or 256 threads
+ * per block) and the x-row kernel (1, 2 or 4 rows per block in each of its
+ * register-cap variants, then its block size) where the generic transform
+ * kernels run, the register cap of the register-blocked x-row kernel where
+ * it runs; then the banded solves as one fused kernel (two threads per
+ * (kx, +-kz) pair) or as factorisation + substitution kernels (four threads
+ * per pair), and the step on one stream or in two kx halves, timed as whole
+ * steps.  Keeps the fastest; the field, the RK history and the module
+ * scalars are saved and put back, and the results of a step do not depend on
+ * the tiles.  Optional: without it the handle uses tiles sized from the
+ * shared-memory budget, the split solve below 65 536 pairs and two halves
+ * from there on.  No counterpart in the reference. */
+#define CHGPU_NTILES 7
 int chgpu_autotune(chgpu_handle* h);
 /* tiles = {z columns per block, x rows per block, x-row variant, z threads
- *          per block, x threads per block}.  z columns 0: the
+ *          per block, x threads per block, solve form (1: fused, 2: split),
+ *          step halves (1 or 2)}.  z columns 0: the
  * register-blocked z kernels (compile-time plans for nzd = 32, 48, 64, 96,
  * 192, 384, 768, 1536); x-row variant 1-3: the generic kernel with its
  * registers capped for that many 256-thread blocks per SM, 4 and 5: the

@@ -181,7 +181,9 @@ def test_autotuned_tiles_give_identical_steps(gpu_lib, prec):
     from channel_gb300 import ChannelError
 
     with pytest.raises(ChannelError):
-        u.set_tiles((9, 3, 1, 256, 256))
+        u.set_tiles((9, 3, 1, 256, 256, 1, 1))
+    with pytest.raises(ChannelError):
+        u.set_tiles(tiles[:5] + (3, 1))
     for h in (g, t, u):
         h.close()
 
@@ -208,6 +210,31 @@ def test_stepped_field_is_divergence_free(gpu_lib, prec, tol):
             scale = max(np.abs(vp).max(), np.abs(p.alfa0 * ix * u).max(), 1e-30)
             worst = max(worst, float(np.abs(res).max() / scale))
     assert worst <= tol, worst
+    g.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_solve_forms_are_identical(gpu_lib, prec):
+    """The fused solve (two threads per pair) and the factorisation +
+    substitution kernels (four threads per pair), on one stream and in two
+    halves, give the same field and Runtimedata bit for bit: the autotuner's
+    choice among them changes nothing but the time."""
+    p, V0, _, g = make("small", 0.02, 6, prec)
+    from channel_gb300 import Channel
+
+    base = g.tiles()
+    out = []
+    for form, halves in ((1, 1), (2, 1), (1, 2), (2, 2)):
+        with Channel(p, prec) as h:
+            h.set_tiles(base[:5] + (form, halves))
+            h.upload(V0)
+            h.start()
+            for _ in range(3):
+                ln = h.step()
+            out.append((h.download(), ln))
+    for V, ln in out[1:]:
+        assert np.array_equal(V, out[0][0])
+        assert np.array_equal(ln, out[0][1])
     g.close()
 
 
