@@ -1340,6 +1340,15 @@ int chgpu_set_tiles(chgpu_handle* h, const int tiles[CHGPU_NTILES]) {
   return 0;
 }
 
+int chgpu_set_wait_limit(chgpu_handle* h, int polls) {
+  if (!h) return fail(h, CHGPU_E_PARAM, "null handle");
+  const int v = polls < 0 ? 0 : polls + 1;
+  h->sc_host->first_wait = v;  // the host copy is uploaded whole by chgpu_start
+  CK(h, cudaMemcpyAsync(&h->sc->first_wait, &v, sizeof v, cudaMemcpyHostToDevice, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
 int chgpu_set_step_halves(chgpu_handle* h, int halves) {
   if (!h || (halves != 1 && halves != 2)) return fail(h, CHGPU_E_PARAM, "chgpu_set_step_halves: 1 or 2");
   if (h->halves != halves) {

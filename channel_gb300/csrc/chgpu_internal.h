@@ -73,7 +73,8 @@ struct DevScalars {
   long long istep;
   int error;  // bit 0: non-finite CFL or statistics; bit 1: a bulk-copy wait ran out;
               // bit 2: a tensor-core completion wait of the closure ran out
-  int pad;
+  int first_wait;  // 0: the full poll limit; k > 0: a generic z kernel's first bulk-copy wait
+                   // makes k-1 polls (chgpu_set_wait_limit, for tests of the time-out path)
 };
 
 }  // namespace chgpu

@@ -256,9 +256,9 @@ __global__ void __launch_bounds__(256) k_zinv(const double2* __restrict__ V, typ
   if (threadIdx.x == 0) mbar_init(&bar, 1);
   __syncthreads();
   if (threadIdx.x == 0) bulk_copy_g2s(const_cast<double2*>(raw), V + (colbase + ix0) * nzt, bytes, &bar);
-  if (!mbar_wait(&bar, 0, kBulkWaitPolls)) {
+  if (!mbar_wait(&bar, 0, sc->first_wait > 0 ? sc->first_wait - 1 : kBulkWaitPolls)) {
     if (threadIdx.x == 0) atomicOr(&sc->error, 2);
-    mbar_wait(&bar, 0, kBulkWaitPolls);  // the copy in flight, once more
+    mbar_wait(&bar, 0, kBulkWaitPolls);  // the copy in flight, with the full limit
     return;
   }
   const FastDiv by_nzd(nzd);
@@ -304,9 +304,9 @@ __global__ void __launch_bounds__(256) k_zfwd(const typename C2<T>::t* __restric
   if (threadIdx.x == 0) mbar_init(&bar, 1);
   __syncthreads();
   if (threadIdx.x == 0) bulk_copy_g2s(bufB, in, bytes, &bar);
-  if (!mbar_wait(&bar, 0, kBulkWaitPolls)) {
+  if (!mbar_wait(&bar, 0, sc->first_wait > 0 ? sc->first_wait - 1 : kBulkWaitPolls)) {
     if (threadIdx.x == 0) atomicOr(&sc->error, 2);
-    mbar_wait(&bar, 0, kBulkWaitPolls);  // the copy in flight, once more
+    mbar_wait(&bar, 0, kBulkWaitPolls);  // the copy in flight, with the full limit
     return;
   }
   for (int idx = threadIdx.x; idx < nb * nzd; idx += blockDim.x) bufA[pad32(idx)] = bufB[idx];

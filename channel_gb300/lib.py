@@ -94,6 +94,7 @@ SIGNATURES = {
     "chgpu_tiles": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "chgpu_set_tiles": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "chgpu_set_step_halves": (C.c_int, [_P, C.c_int]),
+    "chgpu_set_wait_limit": (C.c_int, [_P, C.c_int]),
     "chgpu_export_dims": (C.c_int, [_P, C.c_float, C.POINTER(C.c_int)]),
     "chgpu_export_physical": (C.c_int, [_P, C.POINTER(ExportOpts), _DP]),
     "chgpu_stats_reset": (C.c_int, [_P]),
@@ -302,6 +303,10 @@ class Channel:
         if len(tiles) == 5:
             tiles = tiles + self.tiles()[5:]
         self._check(self.lib.chgpu_set_tiles(self.h, (C.c_int * 7)(*tiles)))
+
+    def set_wait_limit(self, polls: int) -> None:
+        """Poll count of the first device-side wait (generic z kernels); < 0: default."""
+        self._check(self.lib.chgpu_set_wait_limit(self.h, polls))
 
     def set_step_halves(self, halves: int) -> None:
         """1: the step on one stream; 2: rhs / solve split in two kx halves on two streams."""

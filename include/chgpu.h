@@ -277,6 +277,17 @@ int chgpu_set_profiling(chgpu_handle* h, int on);
 int chgpu_kernel_times(chgpu_handle* h, double ms[CHGPU_NKINDS], long long launches[CHGPU_NKINDS]);
 const char* chgpu_kernel_kind_name(int kind);
 
+/* The device-side waits of the generic z-transform kernels (their bulk
+ * copies into shared memory) give up after a bounded number of polls, set the
+ * handle's error word and return; the next synchronising call reports
+ * CHGPU_E_CUDA ("... did not complete in time").  chgpu_set_wait_limit sets
+ * the first wait's poll count (polls >= 0; < 0 restores the default of 2^22,
+ * seconds in all), so that the time-out path can be exercised: with 0 the
+ * wait gives up at once, then waits (with the full limit) for the copy in
+ * flight and returns.  The register-blocked kernels have no such waits.  No
+ * counterpart in the reference. */
+int chgpu_set_wait_limit(chgpu_handle* h, int polls);
+
 /* Kernel launches issued by the handle since creation (for accounting). */
 long long chgpu_launch_count(const chgpu_handle* h);
 
