@@ -146,8 +146,7 @@ __global__ void __launch_bounds__(NC * TPR) k_zfwd_r(const typename C2<T>::t* __
 
 // Row layout in shared memory: u and v in physical space (M each), then the
 // padded exchange buffer X (M + TPR), which first holds the row's w
-// spectrum; without WREG a fourth slot W (M) after X holds w in physical
-// space.  With WREG w stays in registers after its transform: the last pass
+// spectrum; without WREG w's physical values take a third slot before X.  With WREG w stays in registers after its transform: the last pass
 // leaves each thread exactly the elements the products' forward transforms
 // start from, so only u and v need shared memory.
 template <typename T, int E, int TPR, int NR, int MINB, bool WREG>
@@ -166,17 +165,17 @@ __global__ void __launch_bounds__(NR * TPR, MINB) k_xrow_r(const typename C2<T>:
   const int row = threadIdx.x / TPR, t = threadIdx.x % TPR;
   V2* U = S + row * RS;
   V2* Vv = U + M;
-  V2* X = U + 2 * M;
+  V2* X = U + (WREG ? 2 : 3) * M;  // the exchange buffer; without WREG w's slot sits before it
   const int nx = d.nx, nxp = nx + 1, nzd = d.nzd;
   const int plane = plane0 + blockIdx.y;
   const int jz0 = blockIdx.x * NR;
   const int nrow = min(NR, nzd - jz0);
   // the block's rows of the three spectra (zTOx): NR consecutive jz per kx,
   // u into U, v into V, w into X (with WREG) or into its own slot W
-  V2* Wp = X + M + TPR;  // w in physical space without WREG
+  V2* Wp = U + 2 * M;  // w in physical space without WREG
   for (int c = 0; c < 3; ++c) {
     const V2* src = Zb + ((size_t)c * d.nplanes + plane) * nxp * nzd + jz0;
-    const int off = c < 2 || WREG ? c * M : 3 * M + TPR;
+    const int off = c * M;
     for (int i = threadIdx.x; i < nxp * NR; i += NT) {
       const int r = i % NR, k = i / NR;
       V2 v = czero<V2>();
@@ -246,12 +245,15 @@ __global__ void __launch_bounds__(NR * TPR, MINB) k_xrow_r(const typename C2<T>:
   const T g = cst[0];
 #pragma unroll 1
   for (int q = 0; q < 6; ++q) {
-    const int p = q == 0 ? 2 : q == 1 ? 4 : q == 2 ? 5 : q == 3 ? 0 : q == 4 ? 1 : 3;
+    // with WREG the products with w first (w then dies): ww, vw, uw, uu, vv, uv
+    const int p = !WREG ? q : (q == 0 ? 2 : q == 1 ? 4 : q == 2 ? 5 : q == 3 ? 0 : q == 4 ? 1 : 3);
     V2 a[E];
     if constexpr (!WREG) {
-      // factors of product q from the three slots
-      const V2* A = q == 0 ? Wp : (q == 1 ? Vv : (q == 2 ? U : (q == 3 ? U : (q == 4 ? Vv : U))));
-      const V2* B = q < 3 ? Wp : (q == 3 ? U : Vv);
+      // factors of product p (uu, vv, ww, uv, vw, uw) from the u, v, w slots
+      const int fa = p < 3 ? p : (p == 5 ? 0 : p - 3);
+      const int fb = p < 3 ? p : (p == 3 ? 1 : 2);
+      const V2* A = U + fa * M;
+      const V2* B = U + fb * M;
 #pragma unroll
       for (int e = 0; e < E; ++e) {
         const int n = t + TPR * e;
@@ -305,7 +307,7 @@ __global__ void __launch_bounds__(NR * TPR, MINB) k_xrow_r(const typename C2<T>:
     V2* dst = Pb + ((size_t)p * d.nplanes + plane) * nxp * nzd + jz0;
     for (int i = threadIdx.x; i < nxp * NR; i += NT) {
       const int r = i % NR, k = i / NR;
-      if (r < nrow) dst[(size_t)k * nzd + r] = S[r * RS + 2 * M + k];
+      if (r < nrow) dst[(size_t)k * nzd + r] = S[r * RS + (WREG ? 2 : 3) * M + k];
     }
     __syncthreads();
   }
