@@ -611,12 +611,15 @@ def run_reference(args):
 
 
 def run_closure(args):
-    """The learned closure on the Re_tau 180 grid: FP64 DNS 127x192x127 from a
-    seeded broadband field, coarse solver 47x192x47 (the x and z modes of the
-    47x96x47 closure grid on the DNS's y grid), training on the tensor cores,
-    explained variance on held-out snapshots and the coarse solver's error
-    against the filtered DNS with and without the network; then the training
-    kernel's throughput and the cost of the closure in the coarse step."""
+    """The learned closure on the 47x96x47 coarse grid: the 127x192x127
+    (Re_tau~180) DNS from the seeded perturbed-laminar field, spun up to
+    developed turbulence (200 time units, mixed precision), then FP64DD (FP64
+    parity bars) snapshots 0.5 time units apart; per snapshot the subgrid
+    stresses of the Fourier cutoff at 47x47 modes and the y restriction to 96
+    planes (every other DNS plane); training on the tensor cores; explained
+    variance on held-out snapshots and the FP64 coarse solver's error against
+    the filtered DNS with and without the network; then the training kernel's
+    throughput and the cost of the closure in the coarse step."""
     import dataclasses
 
     import torch
@@ -624,8 +627,12 @@ def run_closure(args):
     from channel_gb300 import closure as cl
 
     pf = dnsin.workload("retau180")
-    net, rep = cl.pipeline(pf, 47, 47, amp=0.002, kmax=48, spinup=150, every=15, nsnap=12, nval=3,
-                           points=400_000, steps=20_000, horizons=(10, 40))
+    nsnap = args.steps if args.steps >= 10 else 200
+    net, rep = cl.pipeline(pf, 47, 47, amp=0.05, kmax=4, nyc=96, spinup_time=200.0, every_time=0.5, nsnap=nsnap,
+                           nval=max(2, nsnap // 10), points=200_000, steps=100_000, horizons=(10, 40, 100),
+                           precision="fp64dd", coarse_precision="fp64", spinup_precision="mixed")
+    if net is not None and args.save_net:
+        net.save(args.save_net)
     # training throughput: Adam steps of 152 x 128 points on resident data
     m = cl.Mlp(1)
     rng = np.random.default_rng(0)
@@ -649,8 +656,8 @@ def run_closure(args):
     fl_train = 2.0 * (11264 + 35840) * batch / dt_train
     m.close()
     # the closure's share of the coarse step
-    pc = dataclasses.replace(pf, nx=47, nz=47)
-    V0 = cl.restrict(initial.perturbed_laminar(pf, 0.002, 0, kmax=48), 47, 47)
+    pc = dataclasses.replace(pf, nx=47, nz=47, ny=96)
+    V0 = cl.filtered(initial.perturbed_laminar(pf, 0.05, 0), pf, pc)
     step_ms = {}
     probe = cl.Mlp(2) if net is None else net
     for name, on in (("plain", False), ("closure", True)):
@@ -673,7 +680,7 @@ def run_closure(args):
                                "arithmetic": "tcgen05.mma kind::f16, BF16 operands, FP32 accumulators in TMEM"},
            "inference_points_per_s": n / dt_pred,
            "coarse_step_ms": step_ms,
-           "data": "synthetic: seeded broadband field (initial.perturbed_laminar, modes up to kmax), FP64 DNS"}
+           "data": "synthetic: seeded perturbed-laminar field spun up to developed turbulence, FP64DD DNS"}
     print(json.dumps(out), flush=True)
     if net is not None:
         net.close()
@@ -686,6 +693,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="retau550", choices=list(AMPLITUDE))
+    ap.add_argument("--save-net", default="", help="closure mode: write the kept network (parameters and "
+                                                     "normalisation, .npz) to this path")
     ap.add_argument("--tiles", default="",
                     help="fixed tiles instead of autotuning, e.g. fp64:0,4,2,256,256,2,1/mixed:0,2,4,256,256,1,2 "
                          "(z columns, x rows, x-row variant, z threads, x threads; for reproducible profiler "

@@ -152,6 +152,45 @@ def restrict(S: np.ndarray, nx: int, nz: int) -> np.ndarray:
     return np.ascontiguousarray(S[..., :nx + 1, nzf - nz:nzf + nz + 1, :])
 
 
+def restrict_y(S: np.ndarray, pf, pc) -> np.ndarray:
+    """Spectra shaped (..., ny_f+3) on the fine y grid to the coarse one of
+    ny_c = ny_f / 2 planes and the same stretching: coarse plane iy is fine
+    plane 2 iy (the tanh grids coincide there, dnsdata.f90:153), so the
+    interior and wall planes are injected; the two ghost planes iy = -1 and
+    ny_c + 1, which the coarse solver rebuilds from its wall conditions in
+    its first solve, are extrapolated from the four nearest coarse planes
+    (cubic Lagrange in y).  Equal y grids: S unchanged."""
+    if pf.ny == pc.ny:
+        return S
+    if pf.ny != 2 * pc.ny or pf.a != pc.a or pf.ymin != pc.ymin or pf.ymax != pc.ymax:
+        raise ValueError("the coarse y grid must be every other point of the fine one")
+    nyc = pc.ny
+    out = np.empty(S.shape[:-1] + (nyc + 3,), dtype=S.dtype)
+    out[..., 1:nyc + 2] = S[..., 1:2 * nyc + 2:2]  # iy_c = 0..nyc <- iy_f = 0, 2, .., 2 nyc
+    yc = pc.y()
+
+    def extrap(target, idx):
+        x = yc[idx]
+        acc = 0.0
+        for a, ia in enumerate(idx):
+            w = 1.0
+            for b in range(len(idx)):
+                if b != a:
+                    w *= (yc[target] - x[b]) / (x[a] - x[b])
+            acc = acc + w * out[..., ia]
+        return acc
+
+    out[..., 0] = extrap(0, [1, 2, 3, 4])
+    out[..., nyc + 2] = extrap(nyc + 2, [nyc - 2, nyc - 1, nyc, nyc + 1])
+    return out
+
+
+def filtered(V: np.ndarray, pf, pc) -> np.ndarray:
+    """The filtered DNS field on the coarse grid: Fourier cutoff at the coarse
+    modes, then the y restriction."""
+    return restrict_y(restrict(V, pc.nx, pc.nz), pf, pc)
+
+
 def sgs_sample(fine, coarse, V: np.ndarray | None = None):
     """(features, targets) at every closure point of the coarse handle for the
     fine field V (default: the fine handle's current field).  Targets are the
@@ -162,14 +201,12 @@ def sgs_sample(fine, coarse, V: np.ndarray | None = None):
         V = fine.download()
     else:
         fine.upload(V)
-    if fine.p.ny != coarse.p.ny or fine.p.a != coarse.p.a or fine.p.alfa0 != coarse.p.alfa0 \
-            or fine.p.beta0 != coarse.p.beta0:
-        raise ValueError("fine and coarse runs need the same domain and y grid")
+    if fine.p.alfa0 != coarse.p.alfa0 or fine.p.beta0 != coarse.p.beta0:
+        raise ValueError("fine and coarse runs need the same domain")
     Pf = fine.products()
-    nx, nz = coarse.p.nx, coarse.p.nz
-    coarse.upload(restrict(V, nx, nz))
+    coarse.upload(filtered(V, fine.p, coarse.p))
     Pc = coarse.products()
-    targ = coarse.closure_physical(restrict(Pf, nx, nz) - Pc)
+    targ = coarse.closure_physical(filtered(Pf, fine.p, coarse.p) - Pc)
     feat = coarse.closure_features()
     return feat, targ
 
@@ -226,8 +263,8 @@ def a_posteriori(pf, pc, V0: np.ndarray, nsteps: int, dt: float, nets: dict, pre
         f.start()
         for _ in range(nsteps):
             f.step(sync=False)
-        ref = restrict(f.download(), pc.nx, pc.nz)
-    V0c = restrict(V0, pc.nx, pc.nz)
+        ref = filtered(f.download(), pf, pc)
+    V0c = filtered(V0, pf, pc)
     change = np.linalg.norm(ref - V0c)
     out = {}
     for name, net in nets.items():
@@ -245,12 +282,20 @@ def a_posteriori(pf, pc, V0: np.ndarray, nsteps: int, dt: float, nets: dict, pre
 
 def pipeline(pf, nxc: int, nzc: int, amp: float, kmax: int, seed: int = 0, spinup: int = 150, every: int = 15,
              nsnap: int = 12, nval: int = 3, points: int = 400_000, steps: int = 20_000, horizons=(10, 40),
-             precision: str = "fp64", lr: float = 3e-3, lr_final: float = 2e-4) -> tuple[Mlp | None, dict]:
+             precision: str = "fp64", lr: float = 3e-3, lr_final: float = 2e-4, nyc: int | None = None,
+             spinup_time: float | None = None, every_time: float | None = None,
+             coarse_precision: str | None = None,
+             spinup_precision: str | None = None) -> tuple[Mlp | None, dict]:
     """The closure end to end on one GPU.
 
     1. The fine DNS (precision, adaptive dt) from a seeded broadband field
-       (initial.perturbed_laminar with modes up to kmax), spinup steps, then
-       nsnap snapshots every `every` steps.
+       (initial.perturbed_laminar with modes up to kmax), spinup steps (or
+       spinup_time time units), then nsnap snapshots every `every` steps (or
+       every_time time units).  The wall shear is recorded along the way, so
+       the report shows whether the flow had settled.  spinup_precision
+       runs the spin-up in another precision (the field is handed over).
+       The coarse grid is (nxc, nyc, nzc) on the same domain; nyc = ny/2
+       restricts in y as well (restrict_y).
     2. Per snapshot, features and subgrid-stress targets at the closure
        points of the coarse grid (nxc, nzc; the fine y grid), a random subset
        of `points` of them.
@@ -270,28 +315,72 @@ def pipeline(pf, nxc: int, nzc: int, amp: float, kmax: int, seed: int = 0, spinu
     from .lib import Channel
 
     t0 = time.time()
-    pc = dataclasses.replace(pf, nx=nxc, nz=nzc)
+    cprec = coarse_precision or precision
+    pc = dataclasses.replace(pf, nx=nxc, nz=nzc, ny=nyc or pf.ny)
     V0 = initial.perturbed_laminar(pf, amp, seed, kmax=kmax)
-    snaps, dts = [], []
-    with Channel(pf, precision) as f:
-        f.upload(V0)
-        f.start()
-        for k in range(spinup + every * nsnap):
-            st = f.step()
-            if k >= spinup and (k - spinup) % every == every - 1:
-                snaps.append(f.download())
-                dts.append(float(st[10]))
-    t1 = time.time()
+    snaps, dts, history = {}, [], []
     rng = np.random.default_rng(seed)
     feats, targs = [], []
-    with Channel(pf, precision) as fs, Channel(pc, precision) as c:
+    ntr = nsnap - nval
+    t_sample = 0.0
+    # each snapshot is sampled as it is taken (fs: the fine products, c: the
+    # coarse run); only the first held-out field is kept, for the a posteriori test
+    k = 0
+    if spinup_precision is not None and spinup_precision != precision:
+        with Channel(pf, spinup_precision) as s:
+            s.upload(V0)
+            st = s.start()
+            t_start = float(st[0])
+            while (float(st[0]) - t_start < spinup_time) if spinup_time is not None else (k < spinup):
+                st = s.step()
+                k += 1
+                if k % 100 == 0:
+                    history.append([float(st[0]), float(st[1]), float(st[2])])
+            V0 = s.download()
+            t_resume = float(st[0])
+        spun = True
+    else:
+        spun = False
+    with Channel(pf, precision) as f, Channel(pf, precision) as fs, Channel(pc, cprec) as c:
         npts = c.closure_points()
-        for V in snaps:
+        f.upload(V0)
+        st = f.start(time=t_resume) if spun else f.start()
+        t_start = float(st[0])
+        if not spun:
+            if spinup_time is not None:
+                while float(st[0]) - t_start < spinup_time:
+                    st = f.step()
+                    k += 1
+                    if k % 100 == 0:
+                        history.append([float(st[0]), float(st[1]), float(st[2])])
+            else:
+                for _ in range(spinup):
+                    st = f.step()
+                    k += 1
+        spin_steps = k
+        t_next = float(st[0])
+        while len(feats) < nsnap:
+            st = f.step()
+            k += 1
+            if k % 100 == 0:
+                history.append([float(st[0]), float(st[1]), float(st[2])])
+            due = (float(st[0]) >= t_next + every_time) if every_time is not None else ((k - spin_steps) % every == 0)
+            if not due:
+                continue
+            t_next = float(st[0])
+            ts = time.time()
+            V = f.download()
+            if len(feats) == ntr:
+                snaps[ntr] = V
+            dts.append(float(st[10]))
             feat, targ = sgs_sample(fs, c, V)
             idx = np.sort(rng.choice(feat.shape[1], min(points, feat.shape[1]), replace=False))
             feats.append(feat[:, idx])
             targs.append(targ[:, idx])
-    t2 = time.time()
+            t_sample += time.time() - ts
+        dns_steps = k
+    t1 = time.time()
+    t2 = t1
     ntr = nsnap - nval
     Ftr, Ttr = np.concatenate(feats[:ntr], 1), np.concatenate(targs[:ntr], 1)
     Fva, Tva = np.concatenate(feats[ntr:], 1), np.concatenate(targs[ntr:], 1)
@@ -301,13 +390,16 @@ def pipeline(pf, nxc: int, nzc: int, amp: float, kmax: int, seed: int = 0, spinu
     r2_train = explained(net.predict(Ftr[:, :points]), Ttr[:, :points])
     apost = {}
     for hz in horizons:
-        apost[hz] = a_posteriori(pf, pc, snaps[ntr], hz, 0.8 * dts[ntr], {"plain": None, "closure": net}, precision)
+        apost[hz] = a_posteriori(pf, pc, snaps[ntr], hz, 0.8 * dts[ntr], {"plain": None, "closure": net}, cprec)
     t4 = time.time()
     keep = all(a["closure"] < a["plain"] for a in apost.values())
     report = {
         "fine": [pf.nx, pf.ny, pf.nz], "coarse": [pc.nx, pc.ny, pc.nz], "precision": precision,
         "initial_field": {"amplitude": amp, "kmax": kmax, "seed": seed},
-        "snapshots": {"spinup": spinup, "every": every, "count": nsnap, "held_out": nval,
+        "dns": {"steps": dns_steps, "spinup_steps": spin_steps, "time_units": history[-1][0] if history else None,
+                "wall_shear_history": history[::max(1, len(history) // 60)]},
+        "snapshots": {"spinup": spinup_time if spinup_time is not None else spinup,
+                      "every": every_time if every_time is not None else every, "count": nsnap, "held_out": nval,
                       "closure_points_per_snapshot": npts, "sampled_per_snapshot": int(feats[0].shape[1])},
         "train": {"points": int(Ftr.shape[1]), "steps": steps, "batch": 152 * 128,
                   "loss_first": float(losses[:max(1, steps // 100)].mean()),
@@ -318,7 +410,7 @@ def pipeline(pf, nxc: int, nzc: int, amp: float, kmax: int, seed: int = 0, spinu
         "a_posteriori": {str(hz): {**a, "gain": a["plain"] / a["closure"] if a["closure"] > 0 else None}
                          for hz, a in apost.items()},
         "kept": keep,
-        "seconds": {"dns": t1 - t0, "samples": t2 - t1, "training": t3 - t2, "a_posteriori": t4 - t3},
+        "seconds": {"dns": t1 - t0 - t_sample, "samples": t_sample, "training": t3 - t2, "a_posteriori": t4 - t3},
     }
     if not keep:
         net.close()

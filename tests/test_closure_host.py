@@ -69,3 +69,27 @@ def test_header_constants_match_the_binding():
     import mlp_oracle as mo
 
     assert mo.NPARAMS == cl.NPARAMS and mo.OFF_B4 + 6 == cl.NPARAMS
+
+
+def test_y_restriction_injects_and_extrapolates():
+    """Coarse plane iy is fine plane 2 iy (the tanh grids coincide), and the
+    ghost planes come from cubic extrapolation: exact for cubic profiles."""
+    import dataclasses
+
+    from channel_gb300 import closure as cl
+    from channel_gb300 import dnsin
+
+    pf = dnsin.workload("retau180")
+    pc = dataclasses.replace(pf, nx=47, nz=47, ny=96)
+    yf, yc = pf.y(), pc.y()
+    assert np.allclose(yc[1:-1], yf[1:-1:2][: pc.ny + 1], rtol=0, atol=1e-15)
+    rng = np.random.default_rng(0)
+    coef = rng.normal(size=(2, 3, 4)) + 1j * rng.normal(size=(2, 3, 4))
+    poly = np.polynomial.polynomial.polyval
+    S = np.array([[poly(yf, coef[i, j]) for j in range(3)] for i in range(2)])
+    R = cl.restrict_y(S, pf, pc)
+    want = np.array([[poly(yc, coef[i, j]) for j in range(3)] for i in range(2)])
+    assert R.shape == (2, 3, pc.ny + 3)
+    np.testing.assert_allclose(R, want, rtol=1e-10, atol=1e-10)
+    with pytest.raises(ValueError):
+        cl.restrict_y(S, pf, dataclasses.replace(pc, ny=64))

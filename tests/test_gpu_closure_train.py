@@ -59,3 +59,20 @@ def test_harmful_network_falls_back_to_the_plain_solver(trained):
     a = cl.a_posteriori(pf, pc, V0, 10, 0.004, {"plain": None, "closure": bad})
     assert a["closure"] > a["plain"]
     bad.close()
+
+
+def test_pipeline_with_y_restriction(gpu_lib):
+    """The pipeline with a coarse y grid of half the planes (every other DNS
+    plane; the closure grid of 47x96x47 against a 192-plane DNS has this
+    ratio): snapshots by time, spin-up in another precision, a finite report."""
+    from channel_gb300 import closure as cl
+
+    net, rep = cl.pipeline(fine_params(), 23, 23, amp=0.004, kmax=24, nyc=48, spinup_time=0.3, every_time=0.04,
+                           nsnap=4, nval=1, points=50_000, steps=600, horizons=(5,), precision="fp64dd",
+                           coarse_precision="fp64", spinup_precision="mixed")
+    assert rep["coarse"] == [23, 48, 23]
+    assert rep["dns"]["spinup_steps"] > 0 and rep["snapshots"]["count"] == 4
+    a = rep["a_posteriori"]["5"]
+    assert np.isfinite(a["plain"]) and np.isfinite(a["closure"])
+    if net is not None:
+        net.close()
