@@ -324,8 +324,14 @@ def ensemble_run(K=10, W=3, n=64):
     ens.close()
     pts = sum((p.nx + 1) * (2 * p.nz + 1) * (p.ny + 3) for p in ps)
     ok = all(np.isfinite(l).all() for l in lines)
+    peak = measured_peaks().get("hbm_gbs") or 6800.0
+    gbs = 912.0 * pts / (ms * 1e-3) / 1e9  # the mixed step's compulsory bytes per spectral point and step
     return {"members": n, "precision": "mixed", "ms_per_ensemble_step": ms, "member_steps_per_s": n * 1e3 / ms,
             "spectral_points": pts, "ns_per_spectral_pt_step": ms * 1e6 / pts, "steps": K, "warmup": W,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "bytes": "912 B per spectral point and step (the mixed step's compulsory traffic: "
+                                  "field in, products out, products and field and history in, history and "
+                                  "field out)"},
             "finite": ok, "workload": "dnsin.ensemble_workloads(64, seed 0): nx,nz in {16,24,32}, ny in {48,64,96}, "
                                       "Re 2000-4000, alfa0 1-2, beta0 2-4, dt 0.004; one graph launch per step"}
 
