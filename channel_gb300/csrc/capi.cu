@@ -63,8 +63,12 @@ struct chgpu_handle {
   // hides its latency and the split is 4-19% slower (extra factor traffic,
   // half the warps idle during v')
   bool split_solve = false;
-  cudaStream_t stream2 = nullptr;
-  cudaEvent_t ev_vv = nullptr, ev_solved = nullptr;
+  // split form with each substep's factorisation on a third stream, started
+  // with the substep (it needs only dt and the RK coefficient): the FP64-pipe
+  // bound k_factor runs beside the FP32 / memory-bound transforms and k_rhs
+  bool factor_ahead = false;
+  cudaStream_t stream2 = nullptr, stream3 = nullptr;
+  cudaEvent_t ev_vv = nullptr, ev_solved = nullptr, ev_fac_fork = nullptr, ev_factored = nullptr;
   // device buffers
   double2* V = nullptr;
   void* old = nullptr;
@@ -440,8 +444,24 @@ void run_rhs(chgpu_handle* h, const double* ode, cudaStream_t s = nullptr, int m
 
 // rhs_in_field: read the right-hand sides from V (the reference's in-place
 // convention) instead of the separate buffer k_rhs writes.
+// k_factor of one substep on the third stream, after everything enqueued on
+// the main stream so far (the previous substep's k_solve, which reads fac,
+// and for a step's first substep the outstats that set dt) and, with two
+// halves, after half B's solve; k_solve waits for ev_factored.
+void enqueue_factor(chgpu_handle* h, double ode1, bool after_half_b) {
+  SolveLaunch L = solve_launch(h, nullptr);
+  L.ode[0] = ode1;
+  L.lambda_from_dt = 1;
+  cudaEventRecord(h->ev_fac_fork, h->stream);
+  cudaStreamWaitEvent(h->stream3, h->ev_fac_fork, 0);
+  if (after_half_b) cudaStreamWaitEvent(h->stream3, h->ev_solved, 0);
+  launch_factor(L, h->stream3);
+  cudaEventRecord(h->ev_factored, h->stream3);
+  h->launches += 1;
+}
+
 void run_linsolve(chgpu_handle* h, double ode1, double lambda, int from_dt, bool rhs_in_field,
-                  cudaStream_t s = nullptr, int q_lo = 0, int q_hi = -1) {
+                  cudaStream_t s = nullptr, int q_lo = 0, int q_hi = -1, bool factored = false) {
   SolveLaunch L = solve_launch(h, nullptr);
   L.ode[0] = ode1;
   L.lambda = lambda;
@@ -461,8 +481,10 @@ void run_linsolve(chgpu_handle* h, double ode1, double lambda, int from_dt, bool
   }
   if (!s) s = h->stream;
   L.split_solve = h->split_solve ? 1 : 0;
+  L.factored = factored && h->split_solve ? 1 : 0;
+  if (L.factored) cudaStreamWaitEvent(s, h->ev_factored, 0);
   timed(h, 4, [&] { launch_linsolve(L, s); });
-  h->launches += h->split_solve ? 2 : 1;
+  h->launches += h->split_solve && !L.factored ? 2 : 1;
 }
 
 void run_outstats(chgpu_handle* h) {
@@ -481,17 +503,23 @@ void run_outstats(chgpu_handle* h) {
 // latency-bound solve of one half overlaps the other half's work.  The x pass, which needs every kx, joins
 // both; so does the end of the step.  Nothing half B's kernels read is
 // written by half A's (the mean-mode scalars are read only for the mean mode).
+//
+// With factor_ahead (split solve, no per-kernel timing) each substep's
+// k_factor is enqueued first on the third stream and overlaps the substep's
+// transforms and k_rhs; the solves wait for it.
 void enqueue_step(chgpu_handle* h) {
   const bool split = h->halves == 2 && !h->profiling && h->d.nx >= 1 && !h->cl_on && !h->cl_fixed;
+  const bool ahead = h->split_solve && h->factor_ahead && !h->profiling;
   const int KA = (h->d.nx + 1 + 1) / 2, nxp = h->d.nx + 1;
   const int mA = KA * h->d.nzt, qA = KA * (h->d.nz + 1);
   for (int k = 0; k < 3; ++k) {
+    if (ahead) enqueue_factor(h, RK[k][0], split && k > 0);
     timed(h, 5, [&] { launch_advance_time(h->sc, 2.0 / RK[k][0], k == 0, h->stream); });
     h->launches += 1;
     if (!split) {
       run_convolutions(h, k == 2, 1, 0, h->d.nplanes);
       run_rhs(h, RK[k]);
-      run_linsolve(h, RK[k][0], 0.0, 1, false);
+      run_linsolve(h, RK[k][0], 0.0, 1, false, nullptr, 0, -1, ahead);
       continue;
     }
     if (k == 0) {
@@ -508,9 +536,9 @@ void enqueue_step(chgpu_handle* h) {
     cudaEventRecord(h->ev_vv, h->stream);
     cudaStreamWaitEvent(h->stream2, h->ev_vv, 0);
     run_rhs(h, RK[k], h->stream2, mA, h->d.nmodes);
-    run_linsolve(h, RK[k][0], 0.0, 1, false, h->stream2, qA, h->d.npairs);
+    run_linsolve(h, RK[k][0], 0.0, 1, false, h->stream2, qA, h->d.npairs, ahead);
     cudaEventRecord(h->ev_solved, h->stream2);
-    run_linsolve(h, RK[k][0], 0.0, 1, false, h->stream, 0, qA);
+    run_linsolve(h, RK[k][0], 0.0, 1, false, h->stream, 0, qA, ahead);
   }
   if (split) cudaStreamWaitEvent(h->stream, h->ev_solved, 0);
   run_outstats(h);
@@ -562,7 +590,10 @@ void release(chgpu_handle* h) {
   if (h->snap_stream) cudaStreamDestroy(h->snap_stream);
   if (h->ev_vv) cudaEventDestroy(h->ev_vv);
   if (h->ev_solved) cudaEventDestroy(h->ev_solved);
+  if (h->ev_fac_fork) cudaEventDestroy(h->ev_fac_fork);
+  if (h->ev_factored) cudaEventDestroy(h->ev_factored);
   if (h->stream2) cudaStreamDestroy(h->stream2);
+  if (h->stream3) cudaStreamDestroy(h->stream3);
   if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -662,6 +693,9 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_vv, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_solved, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream3, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fac_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_factored, cudaEventDisableTiming);
     if (e != cudaSuccess) { rc = cuda_fail(h, e, "cudaStreamCreate"); break; }
     e = conv_set_smem_limits();
     if (e != cudaSuccess) { rc = cuda_fail(h, e, "cudaFuncSetAttribute"); break; }
@@ -770,6 +804,7 @@ int chgpu_destroy(chgpu_handle* h) {
   // pinned buffer, a half of the split step) ends before anything is freed
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->stream2) cudaStreamSynchronize(h->stream2);
+  if (h->stream3) cudaStreamSynchronize(h->stream3);
   if (h->snap_stream) cudaStreamSynchronize(h->snap_stream);
   release(h);
   delete h;
@@ -1137,12 +1172,14 @@ int time_conv_stage(chgpu_handle* h, int stage, int reps, float* ms) {
 namespace {
 
 // The banded solves as one fused kernel (two threads per (kx, +-kz) pair,
-// one per system) or as the factorisation kernel and a substitution kernel
-// with four threads per pair (one per system and mode), and the step on one
-// stream or in two kx halves on two streams: the four combinations timed as
-// whole steps on this handle's sizes, the fastest kept.  All four perform the
-// same operations in the same order (the results are bit-identical).  The
-// field, the RK history and the module scalars are saved first and put back.
+// one per system), as the factorisation kernel and a substitution kernel
+// with four threads per pair (one per system and mode), or as those two with
+// the factorisation on a third stream beside the substep's transforms; and
+// the step on one stream or in two kx halves on two streams: the six
+// combinations timed as whole steps on this handle's sizes, the fastest
+// kept.  All six perform the same operations in the same order (the results
+// are bit-identical).  The field, the RK history and the module scalars are
+// saved first and put back.
 int tune_solve_and_halves(chgpu_handle* h) {
   const Dims& d = h->d;
   const size_t vbytes = sizeof(double2) * 3 * (size_t)d.nplanes * d.nmodes;
@@ -1162,13 +1199,14 @@ int tune_solve_and_halves(chgpu_handle* h) {
   const bool prof = h->profiling;
   h->profiling = false;
   float best = 1e30f;
-  bool best_split = h->split_solve;
+  bool best_split = h->split_solve, best_ahead = h->factor_ahead;
   int best_halves = h->halves;
   cudaEvent_t a = take_event(h), b = take_event(h);
   int rc = 0;
-  for (int form = 0; form < 4 && rc == 0; ++form) {
-    h->split_solve = (form & 1) != 0;
-    h->halves = (form & 2) ? 2 : 1;
+  for (int form = 0; form < 6 && rc == 0; ++form) {
+    h->split_solve = form % 3 != 0;
+    h->factor_ahead = form % 3 == 2;
+    h->halves = form >= 3 ? 2 : 1;
     enqueue_step(h);  // warm-up
     cudaEventRecord(a, h->stream);
     enqueue_step(h);
@@ -1184,12 +1222,14 @@ int tune_solve_and_halves(chgpu_handle* h) {
     if (ms < best) {
       best = ms;
       best_split = h->split_solve;
+      best_ahead = h->factor_ahead;
       best_halves = h->halves;
     }
   }
   h->ev_pool.push_back(a);
   h->ev_pool.push_back(b);
   h->split_solve = best_split;
+  h->factor_ahead = best_ahead;
   h->halves = best_halves;
   h->profiling = prof;
   cudaMemcpyAsync(h->V, sv, vbytes, cudaMemcpyDeviceToDevice, h->stream);
@@ -1319,7 +1359,7 @@ int chgpu_set_tiles(chgpu_handle* h, const int tiles[CHGPU_NTILES]) {
   const bool zplan = rlen_plan(h->d.nzd, &e_, &tpr_), xplan = xlen_plan(h->d.nxd, &e_, &tpr_);
   if ((zc == 0 && !zplan) || (zc != 0 && (zc < 1 || zc > 8 || conv_zinv_smem(zc, h->d.nzd, h->d.nzt, ts) > lim)) ||
       (xr != 1 && xr != 2 && xr != 4) || h->d.nzd % xr != 0 || conv_x_smem(xr, h->d.nxd, ts) > lim ||
-      (xb >= 4 && !xplan) || xb < 1 || xb > 5 || !threads_ok(zt) || !threads_ok(xt) || (sf != 1 && sf != 2) ||
+      (xb >= 4 && !xplan) || xb < 1 || xb > 5 || !threads_ok(zt) || !threads_ok(xt) || sf < 1 || sf > 3 ||
       (hv != 1 && hv != 2))
     return fail(h, CHGPU_E_PARAM, "chgpu_set_tiles: tiles outside what this handle's sizes allow");
   h->zfast = zc == 0;
@@ -1330,7 +1370,8 @@ int chgpu_set_tiles(chgpu_handle* h, const int tiles[CHGPU_NTILES]) {
   else h->xminb = xb;
   h->zthreads = zt;
   h->xthreads = xt;
-  h->split_solve = sf == 2;
+  h->split_solve = sf >= 2;
+  h->factor_ahead = sf == 3;
   h->halves = hv;
   ++h->version;
   if (h->graph) {
@@ -1369,7 +1410,7 @@ int chgpu_tiles(const chgpu_handle* h, int tiles[CHGPU_NTILES]) {
   tiles[2] = h->xfast ? h->xrvar : h->xminb;
   tiles[3] = h->zthreads;
   tiles[4] = h->xthreads;
-  tiles[5] = h->split_solve ? 2 : 1;
+  tiles[5] = h->split_solve ? (h->factor_ahead ? 3 : 2) : 1;
   tiles[6] = h->halves;
   return 0;
 }

@@ -111,10 +111,12 @@ struct SolveLaunch {
   int m_lo, m_hi;     // modes of k_rhs (all: 0, nmodes); a range of whole kx columns
   int q_lo, q_hi;     // (kx, +-kz) pairs of k_linsolve (all: 0, npairs)
   int split_solve;    // 0: the fused k_linsolve; 1: k_factor then k_solve (fac holds kFacPerRow per row)
+  int factored;       // split form: fac already holds this substep's factors (k_factor ran ahead), k_solve only
 };
 
 template <typename T> void launch_rhs(const SolveLaunch& L, cudaStream_t s);
 void launch_linsolve(const SolveLaunch& L, cudaStream_t s);
+void launch_factor(const SolveLaunch& L, cudaStream_t s);  // k_factor alone, pairs q_lo..q_hi
 void launch_advance_time(DevScalars* sc, double coef, int new_step, cudaStream_t s);
 void launch_outstats(const SolveLaunch& L, cudaStream_t s);
 void launch_flowrate(const SolveLaunch& L, cudaStream_t s);

@@ -25,6 +25,8 @@
 //              of the fused kernel where it has too few to hide latency.
 #include <cuda_runtime.h>
 
+#include <cstdio>
+
 #include <type_traits>
 
 #include "chgpu_internal.h"
@@ -342,6 +344,35 @@ __device__ __forceinline__ void bc_bot2(double A[5], const double* bc0) {
   for (int j = 1; j < 4; ++j) A[j] = A[j] - e * bc0[j + 1] / bc0[1];
 }
 
+// Reciprocal of a pivot by Newton-Raphson iteration (the reciprocal
+// iteration of Markstein, "Computation of elementary functions on the IBM
+// RISC System/6000 processor", IBM J. Res. Develop. 34(1), 1990): the start
+// is the FP32 approximate reciprocal (relative error <= 2^-23) of x's
+// leading 24 significand bits (truncation error < 2^-23), scaled by x's
+// binary exponent through the exponent field; two steps y <- y + y (1 - x y)
+// square the error twice (2^-22 -> 2^-44 -> 2^-88), so the result is 1/x
+// rounded once, within half an ulp plus 2^-88 relative.  Four FP64 fused
+// multiply-adds, on a GPU whose FP64 pipe bounds these solves.  x with a
+// biased exponent outside [1, 2044] (zero, subnormal, |x| >= 2^1022, Inf,
+// NaN) takes the IEEE division.
+__device__ __forceinline__ double rcp_nr(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e < 1 || e > 2044) return 1.0 / x;
+  const unsigned hi = (unsigned)(b >> 32);
+  const float mf = __uint_as_float(0x3f800000u | ((hi & 0xfffffu) << 3) | (unsigned)((b >> 29) & 0x7u));  // [1, 2)
+  float rf;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(mf));  // (0.5, 1]
+  const unsigned u = __float_as_uint(rf);
+  const unsigned long long ey = (unsigned long long)((int)((u >> 23) & 0xffu) - 127 + 2046 - e);  // in [1, 2046]
+  double y = __longlong_as_double(
+      (long long)(((unsigned long long)(hi & 0x80000000u) << 32) | (ey << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+  double r = fma(-x, y, 1.0);
+  y = fma(y, r, y);
+  r = fma(-x, y, 1.0);
+  return fma(y, r, y);
+}
+
 // LU5decompStep for one row given the (scaled) lower entries of the two rows
 // below: L1 = row+1 (j=-2,-1), L2 = row+2.
 __device__ __forceinline__ void lu_row(double A[5], const double L1[2], const double L2[2]) {
@@ -351,22 +382,26 @@ __device__ __forceinline__ void lu_row(double A[5], const double L1[2], const do
   piv = A[3];
   A[2] = A[2] - piv * L1[1];
   A[1] = A[1] - piv * L1[0];
-  piv = 1.0 / A[2];
+  piv = rcp_nr(A[2]);
   A[2] = piv;
   A[0] = A[0] * piv;
   A[1] = A[1] * piv;
 }
 
-__device__ __forceinline__ double2 step1(double2 x, const double A[5], double2 x1, double2 x2) {
-  double2 s = rmul(A[3], x1);
-  s = s + rmul(A[4], x2);
-  return rmul(A[2], x - s);
+// LeftLU5divStep1 row, x = (b - u1 x(+1) - u2 x(+2)) / d with A[2] = 1/d:
+// the two differences as fused multiply-adds (three FP64 operations per
+// component where the sum-then-subtract order of the reference takes four)
+__device__ __forceinline__ double2 step1u(double2 b, double rd, double u1, double u2, double2 x1, double2 x2) {
+  return make_double2(rd * fma(-u2, x2.x, fma(-u1, x1.x, b.x)), rd * fma(-u2, x2.y, fma(-u1, x1.y, b.y)));
+}
+__device__ __forceinline__ double2 step1(double2 b, const double A[5], double2 x1, double2 x2) {
+  return step1u(b, A[2], A[3], A[4], x1, x2);
 }
 
+// LeftLU5divStep2 row, b - l2 b(-2) - l1 b(-1), as two fused multiply-adds
+// per component
 __device__ __forceinline__ double2 step2(double2 b, double lm2, double lm1, double2 bm2, double2 bm1) {
-  double2 s = rmul(lm2, bm2);
-  s = s + rmul(lm1, bm1);
-  return b - s;
+  return make_double2(fma(-lm1, bm1.x, fma(-lm2, bm2.x, b.x)), fma(-lm1, bm1.y, fma(-lm2, bm2.y, b.y)));
 }
 
 __device__ __forceinline__ double2 dot3(const double2* v, const double* c) {  // sum(v(1:3)*c(0:2))
@@ -916,9 +951,7 @@ __global__ void __launch_bounds__(128, 4) k_solve(double2* __restrict__ V, const
         if (iy == ny - 2) b = b - make_double2(sc->wallrhs[4], sc->wallrhs[5]);
         if (iy == ny - 1) b = b - make_double2(sc->wallrhs[6], sc->wallrhs[7]);
       }
-      double2 sacc = rmul(u1, x1);
-      sacc = sacc + rmul(u2, x2);
-      const double2 x = rmul(dv, b - sacc);
+      const double2 x = step1u(b, dv, u1, u2, x1, x2);
       x2 = x1;
       x1 = x;
       V[vidx(d, vc, iy, m)] = x;
@@ -1005,6 +1038,13 @@ __global__ void __launch_bounds__(128, 4) k_solve(double2* __restrict__ V, const
   else deriv_uw<double>(V, der, d0lu, lindd, bc, d, mm[t], ka, (t == 0 ? 1.0 : -1.0) * kb, k2);
 }
 
+void launch_factor(const SolveLaunch& L, cudaStream_t s) {
+  if (L.q_hi <= L.q_lo) return;
+  const unsigned grid = (unsigned)((L.q_hi - L.q_lo + 31) / 32);
+  k_factor<<<grid, 64, 0, s>>>(L.fac, L.der, L.bc, L.d, L.lambda, L.ode[0], L.lambda_from_dt, L.sc, L.nud, L.q_lo,
+                               L.q_hi);
+}
+
 void launch_linsolve(const SolveLaunch& L, cudaStream_t s) {
   if (L.q_hi <= L.q_lo) return;
   const unsigned grid = (unsigned)((L.q_hi - L.q_lo + 31) / 32);
@@ -1014,8 +1054,7 @@ void launch_linsolve(const SolveLaunch& L, cudaStream_t s) {
                                    L.q_hi);
     return;
   }
-  k_factor<<<grid, 64, 0, s>>>(L.fac, L.der, L.bc, L.d, L.lambda, L.ode[0], L.lambda_from_dt, L.sc, L.nud, L.q_lo,
-                               L.q_hi);
+  if (!L.factored) launch_factor(L, s);
   k_solve<<<grid, 128, 0, s>>>(L.V, L.rhs_src, L.rhs_cstride, L.rhs_plane_off, L.fac, L.der, L.d0lu, L.yint, L.bc,
                                L.d, L.sc, (const dd*)L.lindd, L.q_lo, L.q_hi);
 }
@@ -1148,3 +1187,35 @@ void launch_transpose(const double2* in, double2* out, int rows, int cols, int b
 }
 
 }  // namespace chgpu
+
+// ---------------------------------------------------------------------------
+// the pivot reciprocal over caller values, for its accuracy test
+// ---------------------------------------------------------------------------
+namespace chgpu {
+__global__ void k_rcp_values(const double* __restrict__ x, double* __restrict__ y, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = rcp_nr(x[i]);
+}
+}  // namespace chgpu
+
+extern "C" int chgpu_pivot_reciprocal(const double* x, double* y, size_t n, char* err, size_t errlen) {
+  if (!x || !y) {
+    if (err && errlen) snprintf(err, errlen, "null buffer");
+    return CHGPU_E_PARAM;
+  }
+  if (n == 0) return CHGPU_OK;
+  double* dx = nullptr;
+  cudaError_t e = cudaMalloc(&dx, 2 * n * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemcpy(dx, x, n * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    chgpu::k_rcp_values<<<(unsigned)((n + 255) / 256), 256>>>(dx, dx + n, n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(y, dx + n, n * sizeof(double), cudaMemcpyDeviceToHost);
+  if (dx) cudaFree(dx);
+  if (e != cudaSuccess) {
+    if (err && errlen) snprintf(err, errlen, "pivot reciprocal: %s", cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? CHGPU_E_NOMEM : CHGPU_E_CUDA;
+  }
+  return CHGPU_OK;
+}

@@ -105,6 +105,7 @@ SIGNATURES = {
     "chgpu_linsolve_noalloc": (C.c_int, [C.POINTER(Params), C.c_double, C.c_void_p, _DP, C.c_void_p,
                                          C.c_char_p, C.c_size_t]),
     "chgpu_measure_peaks": (C.c_int, [_DP, _DP, _DP, C.c_char_p, C.c_size_t]),
+    "chgpu_pivot_reciprocal": (C.c_int, [_DP, _DP, C.c_size_t, C.c_char_p, C.c_size_t]),
     "chgpu_tke_reset": (C.c_int, [_P, _DP]),
     "chgpu_tke_accumulate": (C.c_int, [_P, _DP]),
     "chgpu_tke_result": (C.c_int, [_P, C.c_int, _DP, _DP, _DP, C.POINTER(C.c_longlong)]),
@@ -167,6 +168,19 @@ def measure_peaks(copy: bool = True) -> dict:
     if copy:
         out["copy_gbs"] = cp.value
     return out
+
+
+def pivot_reciprocal(x) -> np.ndarray:
+    """1/x as the banded solves form their pivot reciprocals
+    (chgpu_pivot_reciprocal), for an array of float64 values."""
+    L = load_library()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.empty_like(x)
+    err = C.create_string_buffer(256)
+    rc = L.chgpu_pivot_reciprocal(x.ctypes.data_as(_DP), y.ctypes.data_as(_DP), x.size, err, 256)
+    if rc != 0:
+        raise ChannelError(rc, err.value.decode())
+    return y
 
 
 def params_struct(p: DnsIn, precision: int = FP64) -> Params:

@@ -146,9 +146,10 @@ const char* chgpu_ensemble_last_error(const chgpu_ensemble* e);
  * register-cap variants, then its block size) where the generic transform
  * kernels run, the register cap of the register-blocked x-row kernel where
  * it runs; then the banded solves as one fused kernel (two threads per
- * (kx, +-kz) pair) or as factorisation + substitution kernels (four threads
- * per pair), and the step on one stream or in two kx halves, timed as whole
- * steps.  Keeps the fastest; the field, the RK history and the module
+ * (kx, +-kz) pair), as factorisation + substitution kernels (four threads
+ * per pair), or as those two with each substep's factorisation on a side
+ * stream, overlapping the substep's transforms (it needs only dt); and the
+ * step on one stream or in two kx halves, timed as whole steps.  Keeps the fastest; the field, the RK history and the module
  * scalars are saved and put back, and the results of a step do not depend on
  * the tiles.  Optional: without it the handle uses tiles sized from the
  * shared-memory budget, the split solve below 65 536 pairs and two halves
@@ -156,8 +157,9 @@ const char* chgpu_ensemble_last_error(const chgpu_ensemble* e);
 #define CHGPU_NTILES 7
 int chgpu_autotune(chgpu_handle* h);
 /* tiles = {z columns per block, x rows per block, x-row variant, z threads
- *          per block, x threads per block, solve form (1: fused, 2: split),
- *          step halves (1 or 2)}.  z columns 0: the
+ *          per block, x threads per block, solve form (1: fused, 2: split,
+ *          3: split with the factorisation ahead on a side stream), step
+ *          halves (1 or 2)}.  z columns 0: the
  * register-blocked z kernels (compile-time plans for nzd = 32, 48, 64, 96,
  * 192, 384, 768, 1536); x-row variant 1-3: the generic kernel with its
  * registers capped for that many 256-thread blocks per SM, 4 and 5: the
@@ -299,6 +301,13 @@ long long chgpu_launch_count(const chgpu_handle* h);
  * allocates 2 GiB when copy_gbs is requested.  No counterpart in the
  * reference (its `chron` flag times whole steps only). */
 int chgpu_measure_peaks(double* fp64_tflops, double* fp32_tflops, double* copy_gbs, char* err, size_t errlen);
+
+/* y[i] = 1/x[i] as the banded solves form their pivot reciprocals (a
+ * Newton-Raphson reciprocal: within half an ulp plus 2^-88 relative of the
+ * exact value), for n host values; allocates 16 n bytes of device memory for
+ * the call.  No counterpart in the reference (LU5decompStep divides,
+ * rbparmat_blocking.f90:41). */
+int chgpu_pivot_reciprocal(const double* x, double* y, size_t n, char* err, size_t errlen);
 
 /* The implicit solve of linsolve (linsolve_blocking.inc:3-107) for callers
  * that cannot allocate device memory.  No counterpart in the reference: it
