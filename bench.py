@@ -214,6 +214,7 @@ def timed_run(p, V0, prec, K, W, ws, clocks_gpu=None):
     from channel_gb300 import Channel
 
     g = tuned(Channel(p, prec), prec)
+    tiles = g.tiles()
     g.upload(V0)
     g.start()
     for _ in range(W):
@@ -244,7 +245,7 @@ def timed_run(p, V0, prec, K, W, ws, clocks_gpu=None):
     V = g.download()
     g.close()
     return {"ms": max_over_ranks(ms, ws), "launches": launches, "V": V, "line": np.array(st.line),
-            "clocks": sampler.summary() if sampler else None}
+            "clocks": sampler.summary() if sampler else None, "tiles": tiles}
 
 
 def kernel_attribution(p, V0, prec, nsteps):
@@ -456,6 +457,7 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": ws * 1000.0 / ms64, "unit": "steps/s", "ms_per_step": ms64,
                               "fp64dd_ms_per_step": rdd["ms"] / K, "mixed_ms_per_step": rmx["ms"] / K,
+                              "tiles": {"fp64": r64["tiles"], "fp64dd": rdd["tiles"], "mixed": rmx["tiles"]},
                               "mode": "timed"}), flush=True)
         return
     U64, rr64 = profiles(r64["V"])

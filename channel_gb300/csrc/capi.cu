@@ -62,11 +62,13 @@ struct chgpu_handle {
   // warps per SM and the split is 14-17% faster; at 147 456 the fused kernel
   // hides its latency and the split is 4-19% slower (extra factor traffic,
   // half the warps idle during v')
-  bool split_solve = false;
-  // split form with each substep's factorisation on a third stream, started
-  // with the substep (it needs only dt and the RK coefficient): the FP64-pipe
-  // bound k_factor runs beside the FP32 / memory-bound transforms and k_rhs
-  bool factor_ahead = false;
+  // 1: fused (k_linsolve); 2: split (k_factor, k_solve); 3: split with each
+  // substep's factorisation on a third stream, started with the substep (it
+  // needs only dt and the RK coefficient), so that the FP64-pipe bound
+  // k_factor runs beside the FP32 / memory-bound transforms and k_rhs; 4: the
+  // factorisation ahead as in 3, the substitutions by the fused kernel's two
+  // threads per pair reading the factors
+  int solve_form = 1;
   cudaStream_t stream2 = nullptr, stream3 = nullptr;
   cudaEvent_t ev_vv = nullptr, ev_solved = nullptr, ev_fac_fork = nullptr, ev_factored = nullptr;
   // device buffers
@@ -480,11 +482,11 @@ void run_linsolve(chgpu_handle* h, double ode1, double lambda, int from_dt, bool
     L.rhs_plane_off = -1;
   }
   if (!s) s = h->stream;
-  L.split_solve = h->split_solve ? 1 : 0;
-  L.factored = factored && h->split_solve ? 1 : 0;
+  L.split_solve = h->solve_form == 1 ? 0 : (h->solve_form == 4 ? 2 : 1);
+  L.factored = factored && h->solve_form >= 2 ? 1 : 0;
   if (L.factored) cudaStreamWaitEvent(s, h->ev_factored, 0);
   timed(h, 4, [&] { launch_linsolve(L, s); });
-  h->launches += h->split_solve && !L.factored ? 2 : 1;
+  h->launches += h->solve_form >= 2 && !L.factored ? 2 : 1;
 }
 
 void run_outstats(chgpu_handle* h) {
@@ -504,12 +506,12 @@ void run_outstats(chgpu_handle* h) {
 // both; so does the end of the step.  Nothing half B's kernels read is
 // written by half A's (the mean-mode scalars are read only for the mean mode).
 //
-// With factor_ahead (split solve, no per-kernel timing) each substep's
+// With the factorisation ahead (solve forms 3 and 4, no per-kernel timing) each substep's
 // k_factor is enqueued first on the third stream and overlaps the substep's
 // transforms and k_rhs; the solves wait for it.
 void enqueue_step(chgpu_handle* h) {
   const bool split = h->halves == 2 && !h->profiling && h->d.nx >= 1 && !h->cl_on && !h->cl_fixed;
-  const bool ahead = h->split_solve && h->factor_ahead && !h->profiling;
+  const bool ahead = h->solve_form >= 3 && !h->profiling;
   const int KA = (h->d.nx + 1 + 1) / 2, nxp = h->d.nx + 1;
   const int mA = KA * h->d.nzt, qA = KA * (h->d.nz + 1);
   for (int k = 0; k < 3; ++k) {
@@ -660,7 +662,7 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
     h->xfast = xlen_plan(nxd, &e_, &tpr_) && h->prec == CHGPU_MIXED;
   }
   h->halves = d.npairs >= 65536 ? 2 : 1;
-  h->split_solve = d.npairs < 65536;
+  h->solve_form = d.npairs < 65536 ? 3 : 1;
   h->rz.n = rz.n; h->rz.nst = rz.nst; std::memcpy(h->rz.r, rz.r, sizeof rz.r);
   h->rx.n = rx.n; h->rx.nst = rx.nst; std::memcpy(h->rx.r, rx.r, sizeof rx.r);
   set_twiddle_offsets(h->rz);
@@ -1173,13 +1175,14 @@ namespace {
 
 // The banded solves as one fused kernel (two threads per (kx, +-kz) pair,
 // one per system), as the factorisation kernel and a substitution kernel
-// with four threads per pair (one per system and mode), or as those two with
-// the factorisation on a third stream beside the substep's transforms; and
-// the step on one stream or in two kx halves on two streams: the six
-// combinations timed as whole steps on this handle's sizes, the fastest
-// kept.  All six perform the same operations in the same order (the results
-// are bit-identical).  The field, the RK history and the module scalars are
-// saved first and put back.
+// with four threads per pair (one per system and mode), as those two with
+// the factorisation on a third stream beside the substep's transforms, or
+// with the factorisation ahead and the fused kernel's two threads per pair
+// substituting; and the step on one stream or in two kx halves on two
+// streams: the eight combinations timed as whole steps on this handle's
+// sizes, the fastest kept.  All eight perform the same operations in the same
+// order (the results are bit-identical).  The field, the RK history and the
+// module scalars are saved first and put back.
 int tune_solve_and_halves(chgpu_handle* h) {
   const Dims& d = h->d;
   const size_t vbytes = sizeof(double2) * 3 * (size_t)d.nplanes * d.nmodes;
@@ -1199,14 +1202,12 @@ int tune_solve_and_halves(chgpu_handle* h) {
   const bool prof = h->profiling;
   h->profiling = false;
   float best = 1e30f;
-  bool best_split = h->split_solve, best_ahead = h->factor_ahead;
-  int best_halves = h->halves;
+  int best_form = h->solve_form, best_halves = h->halves;
   cudaEvent_t a = take_event(h), b = take_event(h);
   int rc = 0;
-  for (int form = 0; form < 6 && rc == 0; ++form) {
-    h->split_solve = form % 3 != 0;
-    h->factor_ahead = form % 3 == 2;
-    h->halves = form >= 3 ? 2 : 1;
+  for (int c = 0; c < 8 && rc == 0; ++c) {
+    h->solve_form = 1 + c % 4;
+    h->halves = c >= 4 ? 2 : 1;
     enqueue_step(h);  // warm-up
     cudaEventRecord(a, h->stream);
     enqueue_step(h);
@@ -1221,15 +1222,13 @@ int tune_solve_and_halves(chgpu_handle* h) {
     }
     if (ms < best) {
       best = ms;
-      best_split = h->split_solve;
-      best_ahead = h->factor_ahead;
+      best_form = h->solve_form;
       best_halves = h->halves;
     }
   }
   h->ev_pool.push_back(a);
   h->ev_pool.push_back(b);
-  h->split_solve = best_split;
-  h->factor_ahead = best_ahead;
+  h->solve_form = best_form;
   h->halves = best_halves;
   h->profiling = prof;
   cudaMemcpyAsync(h->V, sv, vbytes, cudaMemcpyDeviceToDevice, h->stream);
@@ -1359,7 +1358,7 @@ int chgpu_set_tiles(chgpu_handle* h, const int tiles[CHGPU_NTILES]) {
   const bool zplan = rlen_plan(h->d.nzd, &e_, &tpr_), xplan = xlen_plan(h->d.nxd, &e_, &tpr_);
   if ((zc == 0 && !zplan) || (zc != 0 && (zc < 1 || zc > 8 || conv_zinv_smem(zc, h->d.nzd, h->d.nzt, ts) > lim)) ||
       (xr != 1 && xr != 2 && xr != 4) || h->d.nzd % xr != 0 || conv_x_smem(xr, h->d.nxd, ts) > lim ||
-      (xb >= 4 && !xplan) || xb < 1 || xb > 5 || !threads_ok(zt) || !threads_ok(xt) || sf < 1 || sf > 3 ||
+      (xb >= 4 && !xplan) || xb < 1 || xb > 5 || !threads_ok(zt) || !threads_ok(xt) || sf < 1 || sf > 4 ||
       (hv != 1 && hv != 2))
     return fail(h, CHGPU_E_PARAM, "chgpu_set_tiles: tiles outside what this handle's sizes allow");
   h->zfast = zc == 0;
@@ -1370,8 +1369,7 @@ int chgpu_set_tiles(chgpu_handle* h, const int tiles[CHGPU_NTILES]) {
   else h->xminb = xb;
   h->zthreads = zt;
   h->xthreads = xt;
-  h->split_solve = sf >= 2;
-  h->factor_ahead = sf == 3;
+  h->solve_form = sf;
   h->halves = hv;
   ++h->version;
   if (h->graph) {
@@ -1410,7 +1408,7 @@ int chgpu_tiles(const chgpu_handle* h, int tiles[CHGPU_NTILES]) {
   tiles[2] = h->xfast ? h->xrvar : h->xminb;
   tiles[3] = h->zthreads;
   tiles[4] = h->xthreads;
-  tiles[5] = h->split_solve ? (h->factor_ahead ? 3 : 2) : 1;
+  tiles[5] = h->solve_form;
   tiles[6] = h->halves;
   return 0;
 }

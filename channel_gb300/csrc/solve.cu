@@ -29,6 +29,7 @@
 
 #include <type_traits>
 
+#include "async.cuh"
 #include "chgpu_internal.h"
 #include "cplx.cuh"
 #include "kernels.cuh"
@@ -146,6 +147,37 @@ __global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2*
   const L a = L((float)ix) * derL[tailL], b = L((float)iz) * derL[tailL + 1];
   const L k2 = a * a + b * b;
   const L lode2 = Num<L>::from_double(ode2), lode3 = Num<L>::from_double(ode3);
+  // STAGED (FP32 path): the next D rows' products (plane iy+3), field rows
+  // iy+2 and RK history at iy are copied into a per-thread ring in shared
+  // memory while the current row is computed (cp.async), instead of loaded
+  // at the top of each row into registers the window already fills
+  constexpr bool STAGED = std::is_same<T, float>::value;
+  constexpr int D = 2;
+  constexpr int SLOT = 128 * (6 * (int)sizeof(V2) + 3 * 16 + 2 * (int)sizeof(O2));
+  __shared__ __align__(16) unsigned char stage_raw[STAGED ? (D + 1) * SLOT : 16];
+  const int tid = threadIdx.x;
+  auto s_vv = [&](int s, int k) { return reinterpret_cast<V2*>(stage_raw + s * SLOT) + k * 128 + tid; };
+  auto s_v = [&](int s, int c) {
+    return reinterpret_cast<double2*>(stage_raw + s * SLOT + 128 * 6 * (int)sizeof(V2)) + c * 128 + tid;
+  };
+  auto s_old = [&](int s, int c) {
+    return reinterpret_cast<O2*>(stage_raw + s * SLOT + 128 * (6 * (int)sizeof(V2) + 3 * 16)) + c * 128 + tid;
+  };
+  // issue the copies of row rr of this block's run (none past its rows), then close the group
+  auto stage = [&](int rr) {
+    if constexpr (STAGED) {
+      if (rr < nrows) {
+        const int iy = iy0 + rr, s = rr % (D + 1);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) cp_async8(s_vv(s, k), &VV[((size_t)k * d.nplanes + (iy + 3)) * d.nmodes + m]);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) cp_async16(s_v(s, c), &V[vidx(d, c, iy + 2, m)]);
+        cp_async8(s_old(s, 0), &old[((size_t)0 * (d.ny - 1) + (iy - 1)) * d.nmodes + m]);
+        cp_async8(s_old(s, 1), &old[((size_t)1 * (d.ny - 1) + (iy - 1)) * d.nmodes + m]);
+      }
+      cp_async_commit();
+    }
+  };
   // windows over rows iy-2..iy+2: the six product spectra (plane = row + 1) and the field
   V2 vv[6][5];
   LV v1[5], v2[5], v3[5];
@@ -157,6 +189,8 @@ __global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2*
     v2[j + 1] = cvt2<LV>(V[vidx(d, 1, iy0 - 2 + j, m)]);
     v3[j + 1] = cvt2<LV>(V[vidx(d, 2, iy0 - 2 + j, m)]);
   }
+#pragma unroll
+  for (int q = 0; q < D; ++q) stage(q);
 #pragma unroll 1
   for (int rr = 0; rr < RB; ++rr) {
   if (rr >= nrows) break;
@@ -171,11 +205,27 @@ __global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2*
     v2[j] = v2[j + 1];
     v3[j] = v3[j + 1];
   }
+  O2 o_eta, o_d2v;  // RK history at this row
+  if constexpr (STAGED) {
+    cp_async_wait<D - 1>();  // this row's group has landed
+    const int s = rr % (D + 1);
 #pragma unroll
-  for (int k = 0; k < 6; ++k) vv[k][4] = VV[((size_t)k * d.nplanes + (iy + 3)) * d.nmodes + m];
-  v1[4] = cvt2<LV>(V[vidx(d, 0, iy + 2, m)]);
-  v2[4] = cvt2<LV>(V[vidx(d, 1, iy + 2, m)]);
-  v3[4] = cvt2<LV>(V[vidx(d, 2, iy + 2, m)]);
+    for (int k = 0; k < 6; ++k) vv[k][4] = *s_vv(s, k);
+    v1[4] = cvt2<LV>(*s_v(s, 0));
+    v2[4] = cvt2<LV>(*s_v(s, 1));
+    v3[4] = cvt2<LV>(*s_v(s, 2));
+    o_eta = *s_old(s, 0);
+    o_d2v = *s_old(s, 1);
+    stage(rr + D);  // into the slot of row rr-1, already read
+  } else {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) vv[k][4] = VV[((size_t)k * d.nplanes + (iy + 3)) * d.nmodes + m];
+    v1[4] = cvt2<LV>(V[vidx(d, 0, iy + 2, m)]);
+    v2[4] = cvt2<LV>(V[vidx(d, 1, iy + 2, m)]);
+    v3[4] = cvt2<LV>(V[vidx(d, 2, iy + 2, m)]);
+    o_eta = old[((size_t)0 * (d.ny - 1) + (iy - 1)) * d.nmodes + m];
+    o_d2v = old[((size_t)1 * (d.ny - 1) + (iy - 1)) * d.nmodes + m];
+  }
   // stencil coefficients of this row in T
   const T* drT = derT + (size_t)iy * 20;
   T e0[5], e1[5], e2[5];
@@ -228,7 +278,7 @@ __global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2*
     LV r = lmul(cfr[0] + k2 * (cfr[5] + k2 * cfr[10]), v2[0]);
 #pragma unroll
     for (int j = 1; j < 5; ++j) r = r + lmul(cfr[j] + k2 * (cfr[5 + j] + k2 * cfr[10 + j]), v2[j]);
-    const O2 o = old[r1];
+    const O2 o = o_d2v;
     LV e = mk<LV>(conv<L>(explv.x), conv<L>(explv.y));
     if (F) e = e + fv;
     r = r + lmul(lode2, e);
@@ -247,7 +297,7 @@ __global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2*
       sw = sw + cfr[15 + j] * v3[j].x;
     }
     LV r = mk<LV>(su, sw);
-    const O2 o = old[r0];
+    const O2 o = o_eta;
     r = r + lmul(lode2, e);
     r = r - lmul(lode3, mk<LV>(conv<L>(o.x), conv<L>(o.y)));
     old[r0] = mk<O2>(store_as<OT>(e.x), store_as<OT>(e.y));
@@ -263,7 +313,7 @@ __global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2*
       s3 = s3 + lmul(nj, v3[j]);
     }
     LV r = mul_ia<LV>(b, s1) - mul_ia<LV>(a, s3);
-    const O2 o = old[r0];
+    const O2 o = o_eta;
     LV e = mk<LV>(conv<L>(ee.x), conv<L>(ee.y));
     if (F) e = e + fe;
     r = r + lmul(lode2, e);
@@ -554,7 +604,12 @@ __device__ __forceinline__ void deriv_uw(double2* __restrict__ V, const double* 
 // the u, w recovery.
 // registers capped for 8 resident 64-thread blocks per SM: at 147 456 pairs
 // (383x384x383) the extra warps hide the recurrences' latency (-19% per
-// launch); at 16 384 pairs the grid, not the registers, limits residency
+// launch); at 16 384 pairs the grid, not the registers, limits residency.
+// FACTORED: the factorisation ran before (k_factor, kFacPerRow values per
+// row and pair, the mean mode's wall terms in sc->wallrhs); pass A loads each
+// row's 1/d, u1, u2 and pass B its l2, l1 instead of assembling and
+// factoring.
+template <bool FACTORED>
 __global__ void __launch_bounds__(64, 8) k_linsolve(double2* __restrict__ V, const double2* rhs, size_t rcs, int roff,
                                                  double* __restrict__ fac, const double* __restrict__ der,
                                                  const double* __restrict__ d0lu, const double* __restrict__ yint,
@@ -594,55 +649,86 @@ __global__ void __launch_bounds__(64, 8) k_linsolve(double2* __restrict__ V, con
   const bool ucor = role == 1 && is00;
   const AsmCoef ac = asm_coef(lambda, k2, ni);
 
+  // fac layout: kFacPerRow values per row (l2, l1, 1/d, u1, u2 of each
+  // system) when factored ahead, else the fused kernel's own l2, l1
+  constexpr int FS = FACTORED ? kFacPerRow : kFacPerRowFused, RS = FACTORED ? 5 : 2;
   if (active) {
     // ---- pass A: bottom-up assembly + BC fold + factor + Step1 ----
     double L1[2] = {0, 0}, L2[2] = {0, 0};
     double2 x1[2] = {cz(), cz()}, x2[2] = {cz(), cz()};
     double2 xc1 = cz(), xc2 = cz();
     const double2* rsrc = rhs + (role == 0 ? rcs : 0);
-    // right-hand sides one row ahead of the recurrence (global-load latency)
+    // right-hand sides (and factors) one row ahead of the recurrence
+    // (global-load latency)
     double2 bnext[2] = {cz(), cz()};
 #pragma unroll
     for (int t = 0; t < 2; ++t)
       if (t < nm) bnext[t] = rsrc[(size_t)(ny - 1 + roff) * d.nmodes + mm[t]];
+    double fnext[3] = {0, 0, 0};
+    if constexpr (FACTORED) {
+      const double* f = fac + ((size_t)(ny - 2) * FS + RS * role + 2) * P + q;
+      fnext[0] = f[0];
+      fnext[1] = f[P];
+      fnext[2] = f[2 * P];
+    }
     for (int iy = ny - 1; iy >= 1; --iy) {
       const double* dr = der + (size_t)iy * 20;
       double2 b[2] = {bnext[0], bnext[1]};
+      double A[5];
+      if constexpr (FACTORED) {
+        A[2] = fnext[0];
+        A[3] = fnext[1];
+        A[4] = fnext[2];
+      }
       if (iy > 1) {
 #pragma unroll
         for (int t = 0; t < 2; ++t)
           if (t < nm) bnext[t] = rsrc[(size_t)(iy - 1 + roff) * d.nmodes + mm[t]];
+        if constexpr (FACTORED) {
+          const double* f = fac + ((size_t)(iy - 2) * FS + RS * role + 2) * P + q;
+          fnext[0] = f[0];
+          fnext[1] = f[P];
+          fnext[2] = f[2 * P];
+        }
       }
-      // warp-uniform: each warp assembles only its own matrix; the products
-      // -ni d4 and -ni d2, the same for every mode, come from the per-row
-      // table nud when there is one
-      double A[5];
-      if (role) {
-#pragma unroll
-        for (int j = 0; j < 5; ++j) {
-          const double p2 = nud ? __ldg(nud + (size_t)iy * 10 + 5 + j) : ac.ce2 * __ldg(dr + 10 + j);
-          A[j] = fma(ac.ce0, __ldg(dr + j), p2);
+      if constexpr (FACTORED) {
+        if (role == 1 && is00) {  // the wall terms k_factor stored (linsolve_blocking.inc:26-27,40-41)
+          if (iy == 1) b[0] = b[0] - make_double2(sc->wallrhs[0], sc->wallrhs[1]);
+          if (iy == 2) b[0] = b[0] - make_double2(sc->wallrhs[2], sc->wallrhs[3]);
+          if (iy == ny - 2) b[0] = b[0] - make_double2(sc->wallrhs[4], sc->wallrhs[5]);
+          if (iy == ny - 1) b[0] = b[0] - make_double2(sc->wallrhs[6], sc->wallrhs[7]);
         }
       } else {
+        // warp-uniform: each warp assembles only its own matrix; the products
+        // -ni d4 and -ni d2, the same for every mode, come from the per-row
+        // table nud when there is one
+        if (role) {
 #pragma unroll
-        for (int j = 0; j < 5; ++j) {
-          const double p4 = nud ? __ldg(nud + (size_t)iy * 10 + j) : ac.cv4 * __ldg(dr + 15 + j);
-          A[j] = fma(ac.cv0, __ldg(dr + j), fma(ac.cv2, __ldg(dr + 10 + j), p4));
+          for (int j = 0; j < 5; ++j) {
+            const double p2 = nud ? __ldg(nud + (size_t)iy * 10 + 5 + j) : ac.ce2 * __ldg(dr + 10 + j);
+            A[j] = fma(ac.ce0, __ldg(dr + j), p2);
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 5; ++j) {
+            const double p4 = nud ? __ldg(nud + (size_t)iy * 10 + j) : ac.cv4 * __ldg(dr + 15 + j);
+            A[j] = fma(ac.cv0, __ldg(dr + j), fma(ac.cv2, __ldg(dr + 10 + j), p4));
+          }
         }
+        if (iy == ny - 1) bc_top1(A, top, topp1);
+        if (iy == ny - 2) bc_top2(A, top);
+        if (iy == 1) bc_bot1(A, bot, botm1);
+        if (iy == 2) bc_bot2(A, bot);
+        if (role == 1 && is00) {  // the packed wall velocity enters rows 1, 2, ny-2, ny-1 (linsolve_blocking.inc:26-27,40-41)
+          if (iy == 1) b[0] = b[0] - make_double2(A[1] * bval0 / bot[1], A[1] * 0.0 / bot[1]);
+          if (iy == 2) b[0] = b[0] - make_double2(A[0] * bval0 / bot[1], A[0] * 0.0 / bot[1]);
+          if (iy == ny - 1) b[0] = b[0] - make_double2(A[3] * bvaln / top[3], A[3] * 0.0 / top[3]);
+          if (iy == ny - 2) b[0] = b[0] - make_double2(A[4] * bvaln / top[3], A[4] * 0.0 / top[3]);
+        }
+        if (iy == ny - 1) { A[3] = 0; A[4] = 0; }  // rbparmat_blocking.f90:29
+        if (iy == ny - 2) A[4] = 0;
+        lu_row(A, L1, L2);
       }
-      if (iy == ny - 1) bc_top1(A, top, topp1);
-      if (iy == ny - 2) bc_top2(A, top);
-      if (iy == 1) bc_bot1(A, bot, botm1);
-      if (iy == 2) bc_bot2(A, bot);
-      if (role == 1 && is00) {  // the packed wall velocity enters rows 1, 2, ny-2, ny-1 (linsolve_blocking.inc:26-27,40-41)
-        if (iy == 1) b[0] = b[0] - make_double2(A[1] * bval0 / bot[1], A[1] * 0.0 / bot[1]);
-        if (iy == 2) b[0] = b[0] - make_double2(A[0] * bval0 / bot[1], A[0] * 0.0 / bot[1]);
-        if (iy == ny - 1) b[0] = b[0] - make_double2(A[3] * bvaln / top[3], A[3] * 0.0 / top[3]);
-        if (iy == ny - 2) b[0] = b[0] - make_double2(A[4] * bvaln / top[3], A[4] * 0.0 / top[3]);
-      }
-      if (iy == ny - 1) { A[3] = 0; A[4] = 0; }  // rbparmat_blocking.f90:29
-      if (iy == ny - 2) A[4] = 0;
-      lu_row(A, L1, L2);
 #pragma unroll
       for (int t = 0; t < 2; ++t) {
         if (t < nm) {
@@ -658,20 +744,22 @@ __global__ void __launch_bounds__(64, 8) k_linsolve(double2* __restrict__ V, con
         xc1 = nc;
         V[vidx(d, 2, iy, mm[0])] = nc;
       }
-      L2[0] = L1[0]; L2[1] = L1[1];
-      L1[0] = A[0]; L1[1] = A[1];
-      if (iy == 1) { A[0] = 0; A[1] = 0; }  // rbparmat_blocking.f90:45
-      if (iy == 2) A[0] = 0;
-      double* f = fac + ((size_t)(iy - 1) * 4 + 2 * role) * P + q;
-      f[0] = A[0];
-      f[P] = A[1];
+      if constexpr (!FACTORED) {
+        L2[0] = L1[0]; L2[1] = L1[1];
+        L1[0] = A[0]; L1[1] = A[1];
+        if (iy == 1) { A[0] = 0; A[1] = 0; }  // rbparmat_blocking.f90:45
+        if (iy == 2) A[0] = 0;
+        double* f = fac + ((size_t)(iy - 1) * FS + RS * role) * P + q;
+        f[0] = A[0];
+        f[P] = A[1];
+      }
     }
     // ---- pass B: top-down Step2; rows 1..3 and ny-3..ny-1 kept for the walls ----
     double2 lo[2][3], hi[2][3], clo[3], chi[3];
     {
       double2 m2[2] = {cz(), cz()}, m1[2] = {cz(), cz()}, c2 = cz(), c1 = cz();
       // factors and Step1 results one row ahead
-      const double* f1 = fac + ((size_t)0 * 4 + 2 * role) * P + q;
+      const double* f1 = fac + ((size_t)0 * FS + RS * role) * P + q;
       double l2n = f1[0], l1n = f1[P];
       double2 vn[2] = {cz(), cz()};
 #pragma unroll
@@ -681,7 +769,7 @@ __global__ void __launch_bounds__(64, 8) k_linsolve(double2* __restrict__ V, con
         const double l2 = l2n, l1 = l1n;
         const double2 vcur[2] = {vn[0], vn[1]};
         if (iy < ny - 1) {
-          const double* f = fac + ((size_t)iy * 4 + 2 * role) * P + q;
+          const double* f = fac + ((size_t)iy * FS + RS * role) * P + q;
           l2n = f[0];
           l1n = f[P];
 #pragma unroll
@@ -1049,12 +1137,18 @@ void launch_linsolve(const SolveLaunch& L, cudaStream_t s) {
   if (L.q_hi <= L.q_lo) return;
   const unsigned grid = (unsigned)((L.q_hi - L.q_lo + 31) / 32);
   if (!L.split_solve) {
-    k_linsolve<<<grid, 64, 0, s>>>(L.V, L.rhs_src, L.rhs_cstride, L.rhs_plane_off, L.fac, L.der, L.d0lu, L.yint, L.bc,
-                                   L.d, L.lambda, L.ode[0], L.lambda_from_dt, L.sc, (const dd*)L.lindd, L.nud, L.q_lo,
-                                   L.q_hi);
+    k_linsolve<false><<<grid, 64, 0, s>>>(L.V, L.rhs_src, L.rhs_cstride, L.rhs_plane_off, L.fac, L.der, L.d0lu, L.yint,
+                                          L.bc, L.d, L.lambda, L.ode[0], L.lambda_from_dt, L.sc, (const dd*)L.lindd,
+                                          L.nud, L.q_lo, L.q_hi);
     return;
   }
   if (!L.factored) launch_factor(L, s);
+  if (L.split_solve == 2) {
+    k_linsolve<true><<<grid, 64, 0, s>>>(L.V, L.rhs_src, L.rhs_cstride, L.rhs_plane_off, L.fac, L.der, L.d0lu, L.yint,
+                                         L.bc, L.d, L.lambda, L.ode[0], L.lambda_from_dt, L.sc, (const dd*)L.lindd,
+                                         L.nud, L.q_lo, L.q_hi);
+    return;
+  }
   k_solve<<<grid, 128, 0, s>>>(L.V, L.rhs_src, L.rhs_cstride, L.rhs_plane_off, L.fac, L.der, L.d0lu, L.yint, L.bc,
                                L.d, L.sc, (const dd*)L.lindd, L.q_lo, L.q_hi);
 }

@@ -147,19 +147,23 @@ const char* chgpu_ensemble_last_error(const chgpu_ensemble* e);
  * kernels run, the register cap of the register-blocked x-row kernel where
  * it runs; then the banded solves as one fused kernel (two threads per
  * (kx, +-kz) pair), as factorisation + substitution kernels (four threads
- * per pair), or as those two with each substep's factorisation on a side
- * stream, overlapping the substep's transforms (it needs only dt); and the
- * step on one stream or in two kx halves, timed as whole steps.  Keeps the fastest; the field, the RK history and the module
+ * per pair), as those two with each substep's factorisation on a side
+ * stream, overlapping the substep's transforms (it needs only dt), or with
+ * the factorisation ahead and the fused kernel's two threads per pair
+ * substituting; and the step on one stream or in two kx halves, timed as
+ * whole steps.  Keeps the fastest; the field, the RK history and the module
  * scalars are saved and put back, and the results of a step do not depend on
  * the tiles.  Optional: without it the handle uses tiles sized from the
- * shared-memory budget, the split solve below 65 536 pairs and two halves
- * from there on.  No counterpart in the reference. */
+ * shared-memory budget, the split solve with the factorisation ahead below
+ * 65 536 pairs and the fused solve in two halves from there on.  No
+ * counterpart in the reference. */
 #define CHGPU_NTILES 7
 int chgpu_autotune(chgpu_handle* h);
 /* tiles = {z columns per block, x rows per block, x-row variant, z threads
  *          per block, x threads per block, solve form (1: fused, 2: split,
- *          3: split with the factorisation ahead on a side stream), step
- *          halves (1 or 2)}.  z columns 0: the
+ *          3: split with the factorisation ahead on a side stream, 4: the
+ *          factorisation ahead, fused-kernel substitutions), step halves (1
+ *          or 2)}.  z columns 0: the
  * register-blocked z kernels (compile-time plans for nzd = 32, 48, 64, 96,
  * 192, 384, 768, 1536); x-row variant 1-3: the generic kernel with its
  * registers capped for that many 256-thread blocks per SM, 4 and 5: the
