@@ -229,11 +229,13 @@ def timed_run(p, V0, prec, K, W, ws, clocks_gpu=None):
     sampler = ClockSampler(clocks_gpu) if clocks_gpu is not None else None
     if sampler:
         sampler.__enter__()
+    torch.cuda.nvtx.range_push("timed")  # the timed steps, for profiler range filters
     e0.record(stream)
     for _ in range(K):
         g.step(sync=False)
     e1.record(stream)
     e1.synchronize()
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     if sampler:
         sampler.__exit__()
@@ -315,11 +317,13 @@ def ensemble_run(K=10, W=3, n=64):
     ens.synchronize()
     s = torch.cuda.ExternalStream(ens.stream)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("timed")
     e0.record(s)
     for _ in range(K):
         ens.step(sync=False)
     e1.record(s)
     e1.synchronize()
+    torch.cuda.nvtx.range_pop()
     lines = ens.step()
     ms = e0.elapsed_time(e1) / K
     ens.close()
@@ -449,6 +453,12 @@ def run_ours(args):
         gpu_id = "GPU-" + str(torch.cuda.get_device_properties(local).uuid)
     except Exception:
         pass
+    if args.mode == "timed" and args.only:  # one precision's timed steps alone (profiler captures)
+        r = timed_run(p, V0, args.only, K, W, ws)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "precision": args.only, "ms_per_step": r["ms"] / K,
+                              "tiles": r["tiles"], "mode": "timed"}), flush=True)
+        return
     r64 = timed_run(p, V0, "fp64", K, W, ws, clocks_gpu=gpu_id)
     rdd = timed_run(p, V0, "fp64dd", K, W, ws)
     rmx = timed_run(p, V0, "mixed", K, W, ws)
@@ -707,8 +717,11 @@ def main():
                     help="fixed tiles instead of autotuning, e.g. fp64:0,4,2,256,256,2,1/mixed:0,2,4,256,256,1,2 "
                          "(z columns, x rows, x-row variant, z threads, x threads; for reproducible profiler "
                          "captures)")
-    ap.add_argument("--mode", default="full", choices=["full", "timed", "long", "closure"],
-                    help="timed: only the three timed runs (for profiler captures); long: --steps steps of FP64, "
+    ap.add_argument("--only", default="", choices=["", "fp64", "fp64dd", "mixed"],
+                    help="timed mode: time this precision alone")
+    ap.add_argument("--mode", default="full", choices=["full", "timed", "long", "closure", "ensemble"],
+                    help="timed: only the three timed runs (for profiler captures); ensemble: only the batched "
+                         "ensemble of uneven runs (--steps, --warmup); long: --steps steps of FP64, "
                          "FP64DD and mixed from one field, Runtimedata and profile errors against FP64 over the run; "
                          "closure: the learned closure trained and evaluated against the FP64 DNS")
     args = ap.parse_args()
@@ -721,7 +734,9 @@ def main():
 
     if args.impl == "ours":
         b.build()
-        if args.mode == "long":
+        if args.mode == "ensemble":
+            print(json.dumps(ensemble_run(K=args.steps, W=args.warmup)), flush=True)
+        elif args.mode == "long":
             run_long(args)
         elif args.mode == "closure":
             run_closure(args)
