@@ -244,6 +244,31 @@ void set_twiddle_offsets(RadixDev& r) {
   }
 }
 
+// FP64 twiddle of the fused multiply-add butterflies (lf_butterfly, cplx.cuh):
+// w = exp(-2 pi i phi) as (c, t) with w = c (1 + i t), or w = i c (1 + i t)
+// marked by c's lowest significand bit, whichever gives |t| <= 1
+double2 lf_entry(long double phi) {
+  const long double ang = 2.0L * 3.14159265358979323846264338327950288L * phi;
+  const long double wx = cosl(ang), wy = -sinl(ang);
+  const bool q = fabsl(wy) > fabsl(wx);
+  const long double c = q ? wy : wx, t = q ? -wx / wy : wy / wx;
+  double cd = (double)c;
+  unsigned long long bits;
+  std::memcpy(&bits, &cd, sizeof bits);
+  bits = (bits & ~1ull) | (q ? 1ull : 0ull);
+  std::memcpy(&cd, &bits, sizeof bits);
+  return make_double2(cd, (double)t);
+}
+// the R-1 entries of one k of a power-of-two radix-R stage, in lf_dft's
+// order: level l = 1..log2 R, m' < 2^(l-1): W_{2^l Ns}^{k + Ns m'}
+void lf_stage_entries(double2* out, int Ns, int R, int k) {
+  int i = 0;
+  for (int half = 1; half < R; half *= 2)  // half = 2^(l-1)
+    for (int mp = 0; mp < half; ++mp)
+      out[i++] = lf_entry((long double)(k + Ns * mp) / (long double)(2 * half * Ns));
+}
+template <typename V2> constexpr bool lf_format(int R) { return std::is_same<V2, double2>::value && is_pow2c(R); }
+
 template <typename V2>
 int upload_stage_twiddles(chgpu_handle* h, void** dst, const RadixDev& rad) {
   using T = decltype(V2::x);
@@ -251,6 +276,13 @@ int upload_stage_twiddles(chgpu_handle* h, void** dst, const RadixDev& rad) {
   int Ns = 1;
   for (int st = 0; st < rad.nst; ++st) {
     const int R = rad.r[st];
+    if constexpr (std::is_same<V2, double2>::value) {
+      if (lf_format<V2>(R)) {
+        for (int k = 0; k < Ns; ++k) lf_stage_entries(&w[rad.twoff[st] + k * (R - 1)], Ns, R, k);
+        Ns *= R;
+        continue;
+      }
+    }
     for (int k = 0; k < Ns; ++k)
       for (int r = 1; r < R; ++r) {
         const long double ang = 2.0L * 3.14159265358979323846264338327950288L * (long double)(r * k) /
@@ -295,6 +327,10 @@ int upload_rplan_twiddles(chgpu_handle* h, void** dst, int n, bool xplan = false
   std::vector<V2> w(std::max(1, rplan_twsize(E, TPR)));
   for (int p = 1; p < np; ++p) {
     const int R = rplan_radix(E, TPR, p), Ns = rplan_ns(E, TPR, p), off = rplan_twoff(E, TPR, p);
+    if constexpr (std::is_same<V2, double2>::value) {  // every pass after the first has a power-of-two radix
+      for (int k = 0; k < Ns; ++k) lf_stage_entries(&w[off + k * (R - 1)], Ns, R, k);
+      continue;
+    }
     for (int k = 0; k < Ns; ++k)
       for (int r = 1; r < R; ++r) {
         const long double ang = 2.0L * 3.14159265358979323846264338327950288L * (long double)(r * k) /

@@ -262,6 +262,66 @@ template <> __device__ __forceinline__ cdd ldg_v<cdd>(const cdd* p) {
   return cdd{dd(f.x, f.y), dd(f.z, f.w)};
 }
 
+// ---------------------------------------------------------------------------
+// FP64 twiddled DFTs with fused multiply-adds (Linzer and Feig, "Modified
+// FFTs for fused multiply-add architectures", Math. Comp. 60, 1993).  A
+// twiddle w is held as (c, t) with w = c (1 + i t) or w = i c (1 + i t)
+// (whichever gives |t| <= 1; the choice q is the lowest significand bit of
+// c, a perturbation of at most one ulp), so that a butterfly a +- w b is
+//   P + i Q = (1 + i t) b          two FMAs
+//   a +- c (P + i Q)  or  a +- i c (P + i Q)   four FMAs
+// -- six FP64 operations where a complex product and two complex additions
+// take eight.  The rotation by i only swaps P and Q and flips a sign of c,
+// which are integer selects, off the FP64 pipe.  SIGN > 0 uses conj(w).
+// ---------------------------------------------------------------------------
+template <int SIGN> __device__ __forceinline__ void lf_butterfly(double2& a, double2& b, double2 w) {
+  const int lo = __double2loint(w.x);
+  const bool q = (lo & 1) != 0;
+  const double t = w.y;
+  const double P = SIGN < 0 ? fma(-t, b.y, b.x) : fma(t, b.y, b.x);
+  const double Q = SIGN < 0 ? fma(t, b.x, b.y) : fma(-t, b.x, b.y);
+  const double X = q ? Q : P, Y = q ? P : Q;
+  const double cneg = __hiloint2double(__double2hiint(w.x) ^ (int)0x80000000, lo);
+  const double cx = (SIGN < 0 && q) ? cneg : w.x;
+  const double cy = (SIGN > 0 && q) ? cneg : w.x;
+  const double2 o1 = make_double2(fma(cx, X, a.x), fma(cy, Y, a.y));
+  b = make_double2(fma(-cx, X, a.x), fma(-cy, Y, a.y));
+  a = o1;
+}
+__host__ __device__ constexpr int ilog2c(int r) { return r <= 1 ? 0 : 1 + ilog2c(r / 2); }
+__host__ __device__ constexpr bool is_pow2c(int r) { return r >= 2 && (r & (r - 1)) == 0; }
+// position of partial transform m (l bits) in the in-place radix-2 cascade
+// of an R-point DFT: bit i of m at R / 2^(i+1)
+__host__ __device__ constexpr int lf_pos(int m, int l, int R) {
+  int o = 0;
+  for (int i = 0; i < l; ++i)
+    if ((m >> i) & 1) o += R >> (i + 1);
+  return o;
+}
+// X_m = sum_r a_r W_{Ns R}^{r k} W_R^{r m} for R = 2^L, natural order in and
+// out, as L levels of radix-2 decimation in time: level l combines pairs at
+// distance R / 2^l with the twiddles W_{2^l Ns}^{k + Ns m'} (m' < 2^(l-1)),
+// which are w[2^(l-1) - 1 + m'] (R - 1 values per k, in that order).
+template <int R, int SIGN> __device__ __forceinline__ void lf_dft(double2* a, const double2* __restrict__ w) {
+  constexpr int L = ilog2c(R);
+#pragma unroll
+  for (int l = 1; l <= L; ++l) {
+    const int h = R >> l;
+#pragma unroll
+    for (int mp = 0; mp < (1 << (l - 1)); ++mp) {
+      const double2 tw = __ldg(w + (1 << (l - 1)) - 1 + mp);
+      const int off = lf_pos(mp, l - 1, R);
+#pragma unroll
+      for (int r = 0; r < h; ++r) lf_butterfly<SIGN>(a[off + r], a[off + r + h], tw);
+    }
+  }
+  double2 y[R];
+#pragma unroll
+  for (int m = 0; m < R; ++m) y[m] = a[lf_pos(m, L, R)];
+#pragma unroll
+  for (int m = 0; m < R; ++m) a[m] = y[m];
+}
+
 // One Stockham stage (Govindaraju et al. 2008 formulation) with radix R over
 // B transforms of length n held in padded shared memory (pad32): item j of
 // a transform reads R points at stride n/R, twiddles them by
@@ -283,12 +343,18 @@ __device__ __forceinline__ void stockham_stage(const V* __restrict__ src, V* __r
     V a[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) a[r] = src[pad32(sbase + r * nb)];
-    if (Ns > 1) {
-      const V* w = twst + k * (R - 1);
+    if constexpr (std::is_same<V, double2>::value && is_pow2c(R)) {
+      // FP64: the twiddles in the fused multiply-add form (lf_dft)
+      if (Ns > 1) lf_dft<R, SIGN>(a, twst + k * (R - 1));
+      else Dft<R, V>::template run<SIGN>(a);
+    } else {
+      if (Ns > 1) {
+        const V* w = twst + k * (R - 1);
 #pragma unroll
-      for (int r = 1; r < R; ++r) a[r] = cmul_s_inner<SIGN>(a[r], ldg_v(w + r - 1));
+        for (int r = 1; r < R; ++r) a[r] = cmul_s_inner<SIGN>(a[r], ldg_v(w + r - 1));
+      }
+      Dft<R, V>::template run<SIGN>(a);
     }
-    Dft<R, V>::template run<SIGN>(a);
     const int dbase = t * n + (j - k) * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) dst[pad32(dbase + r * Ns)] = a[r];

@@ -117,6 +117,22 @@ template <int R, typename V> __device__ __forceinline__ void load_twiddles(const
   }
 }
 
+// One butterfly of a pass p >= 1: the R-1 twiddles of its run of the table,
+// then the R-point DFT; FP64 in the fused multiply-add form (lf_dft, whose
+// tables hold (c, t) pairs in its order)
+template <int R, int SIGN, typename V> __device__ __forceinline__ void twiddled_dft(V (&b)[R], const V* w) {
+  static_assert(is_pow2c(R), "passes after the first have power-of-two radices");
+  if constexpr (std::is_same<V, double2>::value) {
+    lf_dft<R, SIGN>(b, w);
+  } else {
+    V tw_[R];
+    load_twiddles<R>(w, tw_);
+#pragma unroll
+    for (int r = 1; r < R; ++r) b[r] = cmul_s_inner<SIGN>(b[r], tw_[r]);
+    Dft<R, V>::template run<SIGN>(b);
+  }
+}
+
 // Writes the outputs of a pass whose inputs are in a[] (pass p >= 1) or the
 // outputs of pass 1 (p == 0, a[] already transformed) to buf.
 template <int E, int TPR, int P, int SIGN, bool PADDED, typename V>
@@ -140,11 +156,7 @@ __device__ __forceinline__ void rpass_store(V (&a)[E], V* buf, int t, const V* _
       V b[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) b[r] = a[i + r * B];
-      V tw_[R];
-      load_twiddles<R>(twp + k * (R - 1), tw_);
-#pragma unroll
-      for (int r = 1; r < R; ++r) b[r] = cmul_s_inner<SIGN>(b[r], tw_[r]);
-      Dft<R, V>::template run<SIGN>(b);
+      twiddled_dft<R, SIGN>(b, twp + k * (R - 1));
       const int base = (j - k) * R + k;
 #pragma unroll
       for (int r = 0; r < R; ++r) {
@@ -186,11 +198,7 @@ __device__ __forceinline__ void rpass_last_any(V (&a)[E], int t, const V* __rest
       V b[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) b[r] = a[i + r * B];
-      V tw_[R];
-      load_twiddles<R>(twp + j * (R - 1), tw_);
-#pragma unroll
-      for (int r = 1; r < R; ++r) b[r] = cmul_s_inner<SIGN>(b[r], tw_[r]);
-      Dft<R, V>::template run<SIGN>(b);
+      twiddled_dft<R, SIGN>(b, twp + j * (R - 1));
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         if constexpr (TO_REGS) a[i + r * B] = b[r];

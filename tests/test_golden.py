@@ -5,7 +5,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from helpers import rel_l2
+from helpers import line_close, rel_l2
 
 GOLD = Path(__file__).resolve().parent / "golden" / "small_seed0.npz"
 
@@ -15,9 +15,11 @@ def load():
 
 
 def lines_close(a, b, rtol):
-    a, b = np.asarray(a), np.asarray(b)
-    scale = np.maximum(np.abs(b), 1e-3 * np.abs(b).max(axis=-1, keepdims=True))
-    return float((np.abs(a - b) / scale).max()) <= rtol
+    """Every Runtimedata line within rtol, each column group in its own norm
+    (helpers.LINE_GROUPS: the pressure gradient at constant flow rate with
+    its conditioning allowance, which also covers the same code compiled for
+    another host architecture)."""
+    return all(line_close(x, y, rtol)[0] for x, y in zip(np.asarray(a), np.asarray(b)))
 
 
 def run(engine, nsteps):
