@@ -28,6 +28,18 @@
 
 namespace chgpu {
 
+// c2r packing term (X_k + conj X_{M-k}) + i (X_k - conj X_{M-k}) conj(w_k):
+// the product and the sum as four fused multiply-adds (FP64 and FP32);
+// double-float through its complex operations
+template <typename V2> __device__ __forceinline__ V2 c2r_pack(V2 xk, V2 xm, V2 w) {
+  const V2 e = xk + xm, d = xk - xm;
+  if constexpr (std::is_same<V2, cdd>::value) {
+    return e + mul_is<+1>(cmul_s<+1>(d, w));
+  } else {
+    return mk<V2>(fma(d.x, w.y, fma(-d.y, w.x, e.x)), fma(d.y, w.y, fma(d.x, w.x, e.y)));
+  }
+}
+
 __device__ __forceinline__ void block_max_atomic(double v, double* target) {
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
   __shared__ double wmax[32];
@@ -88,8 +100,7 @@ __global__ void __launch_bounds__(256, MINB) k_xrow(const typename C2<T>::t* __r
     V2 xm = czero<V2>();
     if (k == 0) xk.y = T();  // the c2r reads only Re of the kx=0 entry
     else xm = conjg(Cb[pad32(cr * M + M - k)]);
-    V2 e = xk + xm, o = cmul_s<+1>(xk - xm, twh[k]);
-    A[pad32(idx)] = e + mul_is<+1>(o);
+    A[pad32(idx)] = c2r_pack(xk, xm, twh[k]);
   }
   __syncthreads();
   V2* U = fft_block<+1, V2, true>(A, B, 3 * nrows, rx, twx);
@@ -219,8 +230,7 @@ __global__ void __launch_bounds__(256) k_xphys(const typename C2<T>::t* __restri
     V2 xm = czero<V2>();
     if (k == 0) xk.y = T();
     else xm = conjg(Cb[pad32(cr * M + M - k)]);
-    V2 e = xk + xm, o = cmul_s<+1>(xk - xm, twh[k]);
-    A[pad32(idx)] = e + mul_is<+1>(o);
+    A[pad32(idx)] = c2r_pack(xk, xm, twh[k]);
   }
   __syncthreads();
   V2* U = fft_block<+1, V2, true>(A, B, 3 * nrows, rx, twx);
