@@ -324,7 +324,12 @@ int upload_rplan_twiddles(chgpu_handle* h, void** dst, int n, bool xplan = false
   int E = 0, TPR = 0;
   if (!(xplan ? xlen_plan(n, &E, &TPR) : rlen_plan(n, &E, &TPR))) return 0;
   const int np = rplan_passes(E, TPR);
-  std::vector<V2> w(std::max(1, rplan_twsize(E, TPR)));
+  const int tail = std::is_same<V2, double2>::value ? rplan_tailsize(E) : 0;
+  std::vector<V2> w(std::max(1, rplan_twsize(E, TPR) + tail));
+  if constexpr (std::is_same<V2, double2>::value) {  // the composite first pass's twiddled DFTs (rpass_first)
+    for (int k1 = 1; k1 <= 2 && tail > 0; ++k1)
+      lf_stage_entries(&w[rplan_twsize(E, TPR) + (k1 - 1) * (E / 3 - 1)], 3, E / 3, k1);
+  }
   for (int p = 1; p < np; ++p) {
     const int R = rplan_radix(E, TPR, p), Ns = rplan_ns(E, TPR, p), off = rplan_twoff(E, TPR, p);
     if constexpr (std::is_same<V2, double2>::value) {  // every pass after the first has a power-of-two radix

@@ -86,9 +86,43 @@ template <int TPR> __device__ __forceinline__ void group_sync() {
   }
 }
 
-// pass 1: one radix-E register DFT per thread
-template <int E, int SIGN, typename V> __device__ __forceinline__ void rpass_first(V (&a)[E]) {
-  Dft<E, V>::template run<SIGN>(a);
+// pass 1: one radix-E register DFT per thread.  FP64 with E = 3P: the
+// composite DFT's two twiddled P-point DFTs (twiddles W_{3P}^{r k1}, k1 = 1,
+// 2) in the fused multiply-add form, from the 2 (P-1) pairs at the end of
+// the plan's table
+template <int E, int TPR, int SIGN, typename V>
+__device__ __forceinline__ void rpass_first(V (&a)[E], const V* __restrict__ tw) {
+  if constexpr (std::is_same<V, double2>::value && E % 3 == 0 && is_pow2c(E / 3)) {
+    constexpr int P = E / 3;
+    const V* tail = tw + rplan_twsize(E, TPR);
+#pragma unroll
+    for (int r2 = 0; r2 < P; ++r2) {
+      V b[3] = {a[r2], a[P + r2], a[2 * P + r2]};
+      Dft<3, V>::template run<SIGN>(b);
+      a[r2] = b[0];
+      a[P + r2] = b[1];
+      a[2 * P + r2] = b[2];
+    }
+    V y[E];
+#pragma unroll
+    for (int k1 = 0; k1 < 3; ++k1) {
+      V c[P];
+#pragma unroll
+      for (int r2 = 0; r2 < P; ++r2) c[r2] = a[k1 * P + r2];
+      if (k1 == 0) Dft<P, V>::template run<SIGN>(c);
+      else lf_dft<P, SIGN>(c, tail + (k1 - 1) * (P - 1));
+#pragma unroll
+      for (int k2 = 0; k2 < P; ++k2) y[k1 + 3 * k2] = c[k2];
+    }
+#pragma unroll
+    for (int k = 0; k < E; ++k) a[k] = y[k];
+  } else {
+    Dft<E, V>::template run<SIGN>(a);
+  }
+}
+// entries after the per-pass twiddles: FP64 composite first passes only
+__host__ __device__ constexpr int rplan_tailsize(int E) {
+  return (E % 3 == 0 && E / 3 >= 2 && ((E / 3) & (E / 3 - 1)) == 0) ? 2 * (E / 3 - 1) : 0;
 }
 
 // The R-1 twiddles w^1..w^(R-1) of one butterfly from its run of the
@@ -214,7 +248,7 @@ __device__ __forceinline__ void rpass_last_any(V (&a)[E], int t, const V* __rest
 template <int E, int TPR, int SIGN, typename V>
 __device__ __forceinline__ void rfft_head(V (&a)[E], V* buf, int t, const V* __restrict__ tw) {
   constexpr int NP = rplan_passes(E, TPR);
-  rpass_first<E, SIGN>(a);
+  rpass_first<E, TPR, SIGN>(a, tw);
   if constexpr (NP >= 2) {
     rpass_store<E, TPR, 0, SIGN, true>(a, buf, t, tw);
     group_sync<TPR>();
