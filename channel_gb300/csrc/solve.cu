@@ -44,6 +44,10 @@ __device__ __forceinline__ double2 cdivr(double2 a, double s) { return make_doub
 // (0 + i a) * z, the product with ialfa/ibeta of the reference (the zero real
 // part contributes exact zeros)
 template <typename V> __device__ __forceinline__ V mul_ia(decltype(V::x) a, V z) { return mk<V>(-(a * z.y), a * z.x); }
+// a * b + c in the arithmetic type: one FMA for FP64 and FP32, the
+// double-float product and sum for double-float
+template <typename T> __device__ __forceinline__ T fmaT(T a, T b, T c) { return fma(a, b, c); }
+template <> __device__ __forceinline__ dd fmaT<dd>(dd a, dd b, dd c) { return a * b + c; }
 
 __device__ __forceinline__ size_t vidx(const Dims& d, int c, int iy, int m) {
   return ((size_t)c * d.nplanes + (iy + 1)) * d.nmodes + m;
@@ -243,12 +247,22 @@ __global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2*
     return s;
   };
   const V2 DD0_6 = DD(e0, 5), DD1_6 = DD(e1, 5);
-  const V2 rhsu = czero<V2>() - mul_ia<V2>(ta, DD(e0, 0)) - DD(e1, 3) - mul_ia<V2>(tb, DD0_6);
-  const V2 rhsv = czero<V2>() - mul_ia<V2>(ta, DD(e0, 3)) - DD(e1, 1) - mul_ia<V2>(tb, DD(e0, 4));
-  const V2 rhsw = czero<V2>() - mul_ia<V2>(ta, DD0_6) - DD(e1, 4) - mul_ia<V2>(tb, DD(e0, 2));
-  V2 explv = mul_ia<V2>(ta, mul_ia<V2>(ta, DD(e1, 0)) + DD(e2, 3) + mul_ia<V2>(tb, DD1_6)) +
-             mul_ia<V2>(tb, mul_ia<V2>(ta, DD1_6) + DD(e2, 4) + mul_ia<V2>(tb, DD(e1, 2)));
-  explv = explv - mk<V2>(tk2 * rhsv.x, tk2 * rhsv.y);
+  // rhsu = -i ta DD0(uu) - DD1(uv) - i tb DD0(uw) (dnsdata.f90:636-638), and
+  // rhsv, rhsw alike: with i a z = (-a z.y, a z.x), each component two
+  // fused multiply-adds (a leading 0 - ... would block the fusion)
+  auto rhs3 = [&](V2 X, V2 Y, V2 Z) {
+    return mk<V2>(fmaT(tb, Z.y, fmaT(ta, X.y, -Y.x)), fmaT(-tb, Z.x, fmaT(-ta, X.x, -Y.y)));
+  };
+  const V2 rhsu = rhs3(DD(e0, 0), DD(e1, 3), DD0_6);
+  const V2 rhsv = rhs3(DD(e0, 3), DD(e1, 1), DD(e0, 4));
+  const V2 rhsw = rhs3(DD0_6, DD(e1, 4), DD(e0, 2));
+  // expl_v = i ta (i ta D1uu + D2uv + i tb D1uw) + i tb (i ta D1uw + D2vw + i tb D1ww) - k2 rhsv (:639-640)
+  auto ia_sum = [&](V2 X, V2 Y, V2 Z) {  // i ta X + Y + i tb Z
+    return mk<V2>(fmaT(-tb, Z.y, fmaT(-ta, X.y, Y.x)), fmaT(tb, Z.x, fmaT(ta, X.x, Y.y)));
+  };
+  const V2 in1 = ia_sum(DD(e1, 0), DD(e2, 3), DD1_6), in2 = ia_sum(DD1_6, DD(e2, 4), DD(e1, 2));
+  const V2 explv = mk<V2>(fmaT(-tk2, rhsv.x, fmaT(-ta, in1.y, -(tb * in2.y))),
+                          fmaT(-tk2, rhsv.y, fmaT(ta, in1.x, tb * in2.x)));
   // body-force terms (dnsdata.f90:644, 651, 658): fv for the v equation,
   // fe for eta (or the mean mode's D0 of Re F1, Re F3)
   LV fv = czero<LV>(), fe = czero<LV>();
@@ -303,7 +317,8 @@ __global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2*
     old[r0] = mk<O2>(store_as<OT>(e.x), store_as<OT>(e.y));
     rhs[r0] = make_double2(Num<L>::to_double(r.x), Num<L>::to_double(r.y));
   } else {  // eta (:656-661): with w = i kz V1 - i kx V3, unkn = D0(w), impl = ni (D2(w) - k2 D0(w))
-    const V2 ee = mul_ia<V2>(tb, rhsu) - mul_ia<V2>(ta, rhsw);
+    // i tb rhsu - i ta rhsw (:654)
+    const V2 ee = mk<V2>(fmaT(ta, rhsw.y, -(tb * rhsu.y)), fmaT(-ta, rhsw.x, tb * rhsu.x));
     L nj = cfr[15] + k2 * cfr[20];
     LV s1 = lmul(nj, v1[0]), s3 = lmul(nj, v3[0]);
 #pragma unroll
@@ -312,7 +327,7 @@ __global__ void __launch_bounds__(128, RhsBlocks<T>::value) k_rhs(const double2*
       s1 = s1 + lmul(nj, v1[j]);
       s3 = s3 + lmul(nj, v3[j]);
     }
-    LV r = mul_ia<LV>(b, s1) - mul_ia<LV>(a, s3);
+    LV r = mk<LV>(fmaT(a, s3.y, -(b * s1.y)), fmaT(-a, s3.x, b * s1.x));  // i kz s1 - i kx s3
     const O2 o = o_eta;
     LV e = mk<LV>(conv<L>(ee.x), conv<L>(ee.y));
     if (F) e = e + fe;
@@ -556,8 +571,13 @@ __device__ __forceinline__ void deriv_uw(double2* __restrict__ V, const double* 
       if (iy == 1) f = f - (O::rm(O::d0(der, lindd, iy, 1), f0) + O::rm(O::d0(der, lindd, iy, 0), fm1));
       if (iy == 2) f = f - O::rm(O::d0(der, lindd, iy, 0), f0);
       // Step1 of D0mat: x = A2 (f - A3 x1 - A4 x2)
-      const C s = O::rm(O::lu(d0lu, lindd, iy, 3), x1) + O::rm(O::lu(d0lu, lindd, iy, 4), x2);
-      const C x = O::rm(O::lu(d0lu, lindd, iy, 2), f - s);
+      C x;
+      if constexpr (std::is_same<R, double>::value) {
+        x = step1u(f, O::lu(d0lu, lindd, iy, 2), O::lu(d0lu, lindd, iy, 3), O::lu(d0lu, lindd, iy, 4), x1, x2);
+      } else {
+        const C s = O::rm(O::lu(d0lu, lindd, iy, 3), x1) + O::rm(O::lu(d0lu, lindd, iy, 4), x2);
+        x = O::rm(O::lu(d0lu, lindd, iy, 2), f - s);
+      }
       x2 = x1;
       x1 = x;
       O::park(&V[vidx(d, 2, iy, m)], x);
@@ -579,7 +599,9 @@ __device__ __forceinline__ void deriv_uw(double2* __restrict__ V, const double* 
       else if (iy == 0) vp = f0;
       else if (iy == ny) vp = fn;
       else if (iy == ny + 1) vp = fn1;
-      else  // Step2 of D0mat: vp = x - (l2 bm2 + l1 bm1)
+      else if constexpr (std::is_same<R, double>::value)  // Step2 of D0mat: vp = x - (l2 bm2 + l1 bm1)
+        vp = step2(O::unpark(&xs), O::lu(d0lu, lindd, iy, 0), O::lu(d0lu, lindd, iy, 1), bm2, bm1);
+      else
         vp = O::unpark(&xs) - (O::rm(O::lu(d0lu, lindd, iy, 0), bm2) + O::rm(O::lu(d0lu, lindd, iy, 1), bm1));
       if (iy >= 0 && iy <= ny - 1) {
         bm2 = bm1;
