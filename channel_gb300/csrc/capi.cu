@@ -278,7 +278,11 @@ int upload_stage_twiddles(chgpu_handle* h, void** dst, const RadixDev& rad) {
     const int R = rad.r[st];
     if constexpr (std::is_same<V2, double2>::value) {
       if (lf_format<V2>(R)) {
-        for (int k = 0; k < Ns; ++k) lf_stage_entries(&w[rad.twoff[st] + k * (R - 1)], Ns, R, k);
+        if (Ns == 1 && R == 16) {  // the first stage's inner twiddled DFT4s (lf_dft16_first)
+          for (int k1 = 1; k1 <= 3; ++k1) lf_stage_entries(&w[rad.twoff[st] + 3 * (k1 - 1)], 4, 4, k1);
+        } else {
+          for (int k = 0; k < Ns; ++k) lf_stage_entries(&w[rad.twoff[st] + k * (R - 1)], Ns, R, k);
+        }
         Ns *= R;
         continue;
       }

@@ -152,11 +152,21 @@ template <typename V> struct Dft<3, V> {
   template <int SIGN> __device__ static void run(V* a) {
     using T = decltype(V::x);
     const V t1 = a[1] + a[2];
-    const V t2 = a[0] - scale(t1, T(0.5f));
-    const V t3 = mul_is<SIGN>(scale(a[1] - a[2], Num<T>::sqrt3_2()));
-    a[0] = a[0] + t1;
-    a[1] = t2 + t3;
-    a[2] = t2 - t3;
+    if constexpr (std::is_same<V, cdd>::value) {
+      const V t2 = a[0] - scale(t1, T(0.5f));
+      const V t3 = mul_is<SIGN>(scale(a[1] - a[2], Num<T>::sqrt3_2()));
+      a[0] = a[0] + t1;
+      a[1] = t2 + t3;
+      a[2] = t2 - t3;
+    } else {
+      // m +- SIGN i (sqrt3/2) d as four fused multiply-adds onto m = a0 - t1/2
+      const V d = a[1] - a[2];
+      const T s = SIGN > 0 ? Num<T>::sqrt3_2() : -Num<T>::sqrt3_2();
+      const V m = mk<V>(fma(T(-0.5f), t1.x, a[0].x), fma(T(-0.5f), t1.y, a[0].y));
+      a[0] = a[0] + t1;
+      a[1] = mk<V>(fma(-s, d.y, m.x), fma(s, d.x, m.y));
+      a[2] = mk<V>(fma(s, d.y, m.x), fma(-s, d.x, m.y));
+    }
   }
 };
 template <typename V> struct Dft<4, V> {
@@ -322,6 +332,26 @@ template <int R, int SIGN> __device__ __forceinline__ void lf_dft(double2* a, co
   for (int m = 0; m < R; ++m) a[m] = y[m];
 }
 
+// A 16-point DFT without external twiddles as Dft<16> splits it (DFT4 over
+// r1, twiddles w16^(r2 k1), DFT4 over r2), with the twiddled DFT4s of k1 =
+// 1..3 as lf_dft<4> (their twiddles are those of a radix-4 pass with Ns = 4
+// at k = k1): w holds their 3 x 3 pairs
+template <int SIGN> __device__ __forceinline__ void lf_dft16_first(double2* a, const double2* __restrict__ w) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) dft4_inner<SIGN>(a[q], a[q + 4], a[q + 8], a[q + 12]);
+  double2 y[16];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    double2 c[4] = {a[4 * k1], a[4 * k1 + 1], a[4 * k1 + 2], a[4 * k1 + 3]};
+    if (k1 == 0) dft4<SIGN>(c[0], c[1], c[2], c[3]);
+    else lf_dft<4, SIGN>(c, w + 3 * (k1 - 1));
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) y[k1 + 4 * k2] = c[k2];
+  }
+#pragma unroll
+  for (int k = 0; k < 16; ++k) a[k] = y[k];
+}
+
 // One Stockham stage (Govindaraju et al. 2008 formulation) with radix R over
 // B transforms of length n held in padded shared memory (pad32): item j of
 // a transform reads R points at stride n/R, twiddles them by
@@ -344,8 +374,10 @@ __device__ __forceinline__ void stockham_stage(const V* __restrict__ src, V* __r
 #pragma unroll
     for (int r = 0; r < R; ++r) a[r] = src[pad32(sbase + r * nb)];
     if constexpr (std::is_same<V, double2>::value && is_pow2c(R)) {
-      // FP64: the twiddles in the fused multiply-add form (lf_dft)
+      // FP64: the twiddles in the fused multiply-add form (lf_dft); a
+      // first radix-16 stage twiddles only inside its DFT (lf_dft16_first)
       if (Ns > 1) lf_dft<R, SIGN>(a, twst + k * (R - 1));
+      else if constexpr (R == 16) lf_dft16_first<SIGN>(a, twst);
       else Dft<R, V>::template run<SIGN>(a);
     } else {
       if (Ns > 1) {
