@@ -36,7 +36,7 @@ def test_pivot_reciprocal_outside_the_iteration_range(gpu_lib):
     from channel_gb300.lib import pivot_reciprocal
 
     x = np.array([0.0, -0.0, 5e-324, -2.2e-308, 2.0**1022, -1.5 * 2.0**1022, 1.7e308, np.inf, -np.inf, np.nan])
-    with np.errstate(divide="ignore"):
+    with np.errstate(divide="ignore", over="ignore"):
         ref = 1.0 / x
     y = pivot_reciprocal(x)
     assert np.array_equal(np.isnan(y), np.isnan(ref))
