@@ -67,7 +67,9 @@ struct chgpu_handle {
   // needs only dt and the RK coefficient), so that the FP64-pipe bound
   // k_factor runs beside the FP32 / memory-bound transforms and k_rhs; 4: the
   // factorisation ahead as in 3, the substitutions by the fused kernel's two
-  // threads per pair reading the factors
+  // threads per pair reading the factors; 5: the factorisation ahead, the
+  // substitutions with eight threads per pair (k_solve_ri: one per system,
+  // mode and real / imaginary component)
   int solve_form = 1;
   cudaStream_t stream2 = nullptr, stream3 = nullptr;
   cudaEvent_t ev_vv = nullptr, ev_solved = nullptr, ev_fac_fork = nullptr, ev_factored = nullptr;
@@ -527,7 +529,7 @@ void run_linsolve(chgpu_handle* h, double ode1, double lambda, int from_dt, bool
     L.rhs_plane_off = -1;
   }
   if (!s) s = h->stream;
-  L.split_solve = h->solve_form == 1 ? 0 : (h->solve_form == 4 ? 2 : 1);
+  L.split_solve = h->solve_form == 1 ? 0 : (h->solve_form == 4 ? 2 : (h->solve_form == 5 ? 3 : 1));
   L.factored = factored && h->solve_form >= 2 ? 1 : 0;
   if (L.factored) cudaStreamWaitEvent(s, h->ev_factored, 0);
   timed(h, 4, [&] { launch_linsolve(L, s); });
@@ -1223,10 +1225,11 @@ namespace {
 // with four threads per pair (one per system and mode), as those two with
 // the factorisation on a third stream beside the substep's transforms, or
 // with the factorisation ahead and the fused kernel's two threads per pair
-// substituting; and the step on one stream or in two kx halves on two
-// streams: the eight combinations timed as whole steps on this handle's
-// sizes, the fastest kept.  All eight perform the same operations in the same
-// order (the results are bit-identical).  The field, the RK history and the
+// substituting, or with the factorisation ahead and eight threads per pair
+// substituting (one per system, mode and component); and the step on one
+// stream or in two kx halves on two streams: the ten combinations timed as
+// whole steps on this handle's sizes, the fastest kept.  All ten perform the
+// same operations in the same order (the results are bit-identical).  The field, the RK history and the
 // module scalars are saved first and put back.
 int tune_solve_and_halves(chgpu_handle* h) {
   const Dims& d = h->d;
@@ -1250,9 +1253,9 @@ int tune_solve_and_halves(chgpu_handle* h) {
   int best_form = h->solve_form, best_halves = h->halves;
   cudaEvent_t a = take_event(h), b = take_event(h);
   int rc = 0;
-  for (int c = 0; c < 8 && rc == 0; ++c) {
-    h->solve_form = 1 + c % 4;
-    h->halves = c >= 4 ? 2 : 1;
+  for (int c = 0; c < 10 && rc == 0; ++c) {
+    h->solve_form = 1 + c % 5;
+    h->halves = c >= 5 ? 2 : 1;
     enqueue_step(h);  // warm-up
     cudaEventRecord(a, h->stream);
     enqueue_step(h);
@@ -1403,7 +1406,7 @@ int chgpu_set_tiles(chgpu_handle* h, const int tiles[CHGPU_NTILES]) {
   const bool zplan = rlen_plan(h->d.nzd, &e_, &tpr_), xplan = xlen_plan(h->d.nxd, &e_, &tpr_);
   if ((zc == 0 && !zplan) || (zc != 0 && (zc < 1 || zc > 8 || conv_zinv_smem(zc, h->d.nzd, h->d.nzt, ts) > lim)) ||
       (xr != 1 && xr != 2 && xr != 4) || h->d.nzd % xr != 0 || conv_x_smem(xr, h->d.nxd, ts) > lim ||
-      (xb >= 4 && !xplan) || xb < 1 || xb > 5 || !threads_ok(zt) || !threads_ok(xt) || sf < 1 || sf > 4 ||
+      (xb >= 4 && !xplan) || xb < 1 || xb > 5 || !threads_ok(zt) || !threads_ok(xt) || sf < 1 || sf > 5 ||
       (hv != 1 && hv != 2))
     return fail(h, CHGPU_E_PARAM, "chgpu_set_tiles: tiles outside what this handle's sizes allow");
   h->zfast = zc == 0;

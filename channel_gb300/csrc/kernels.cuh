@@ -111,7 +111,8 @@ struct SolveLaunch {
   int m_lo, m_hi;     // modes of k_rhs (all: 0, nmodes); a range of whole kx columns
   int q_lo, q_hi;     // (kx, +-kz) pairs of k_linsolve (all: 0, npairs)
   int split_solve;    // 0: the fused k_linsolve; 1: k_factor then k_solve (fac holds kFacPerRow per row);
-                      // 2: k_factor then k_linsolve reading the factors (two threads per pair)
+                      // 2: k_factor then k_linsolve reading the factors (two threads per pair);
+                      // 3: k_factor then k_solve_ri (eight threads per pair)
   int factored;       // split form: fac already holds this substep's factors (k_factor ran ahead), k_solve only
 };
 

@@ -607,12 +607,21 @@ __device__ __forceinline__ void deriv_uw(double2* __restrict__ V, const double* 
         bm2 = bm1;
         bm1 = vp;
       }
-      // u = (i kx v' - i kz eta)/k2, w = (i kz v' + i kx eta)/k2
+      // u = (i kx v' - i kz eta)/k2, w = (i kz v' + i kx eta)/k2; in FP64 with
+      // explicit fused multiply-adds, so that the per-component kernel
+      // (deriv_uw_c) rounds exactly alike
       C u, w;
-      u.x = bu * et.y - au * vp.y;
-      u.y = au * vp.x - bu * et.x;
-      w.x = R() - bu * vp.y - au * et.y;
-      w.y = bu * vp.x + au * et.x;
+      if constexpr (std::is_same<R, double>::value) {
+        u.x = fma(bu, et.y, -(au * vp.y));
+        u.y = fma(au, vp.x, -(bu * et.x));
+        w.x = fma(-au, et.y, -(bu * vp.y));
+        w.y = fma(bu, vp.x, au * et.x);
+      } else {
+        u.x = bu * et.y - au * vp.y;
+        u.y = au * vp.x - bu * et.x;
+        w.x = R() - bu * vp.y - au * et.y;
+        w.y = bu * vp.x + au * et.x;
+      }
       V[vidx(d, 0, iy, m)] = O::out(u);
       V[vidx(d, 2, iy, m)] = O::out(w);
     }
@@ -1148,6 +1157,326 @@ __global__ void __launch_bounds__(128, 4) k_solve(double2* __restrict__ V, const
   else deriv_uw<double>(V, der, d0lu, lindd, bc, d, mm[t], ka, (t == 0 ? 1.0 : -1.0) * kb, k2);
 }
 
+// ---------------------------------------------------------------------------
+// The substitutions with eight threads per (kx, +-kz) pair: the systems'
+// coefficients are real, so the real and imaginary parts of every
+// recurrence are independent and each (system, mode) thread of k_solve
+// splits into two, one per component, with the same operations on each (the
+// results are bit-identical to k_solve's).  Twice the warps for a kernel
+// whose y recurrences are latency-bound.  Only the u, w recovery mixes the
+// components (i kx v', i kz eta): each thread takes its partner's values by
+// a shuffle, so no thread reads the half of a slot its partner writes.
+// ---------------------------------------------------------------------------
+namespace {
+// component c of a complex128 in memory
+__device__ __forceinline__ const double* cptr(const double2* p, int c) { return reinterpret_cast<const double*>(p) + c; }
+__device__ __forceinline__ double* cptr(double2* p, int c) { return reinterpret_cast<double*>(p) + c; }
+
+// one component of DerivOps' arithmetic
+template <typename R> struct DerivC;
+template <> struct DerivC<double> {
+  using S = double;
+  __device__ static S in(double v) { return v; }
+  __device__ static double scal(double v) { return v; }
+  __device__ static S rm(double c, S x) { return c * x; }
+  __device__ static void park(double2* p, int c, S x) { *cptr(p, c) = x; }
+  __device__ static S unpark(const double2* p, int c) { return *cptr(p, c); }
+  __device__ static double out(S x) { return x; }
+  __device__ static S partner(S x, unsigned mask) { return __shfl_xor_sync(mask, x, 1); }
+};
+template <> struct DerivC<dd> {
+  using S = dd;
+  __device__ static S in(double v) { return dd_from_double(v); }
+  __device__ static dd scal(double v) { return dd_from_double(v); }
+  __device__ static S rm(dd c, S x) { return c * x; }
+  __device__ static void park(double2* p, int c, S x) { reinterpret_cast<float2*>(p)[c] = make_float2(x.hi, x.lo); }
+  __device__ static S unpark(const double2* p, int c) {
+    const float2 f = reinterpret_cast<const float2*>(p)[c];
+    return dd(f.x, f.y);
+  }
+  __device__ static double out(S x) { return dd_to_double_int(x); }
+  __device__ static S partner(S x, unsigned mask) {
+    return dd(__shfl_xor_sync(mask, x.hi, 1), __shfl_xor_sync(mask, x.lo, 1));
+  }
+};
+
+// deriv_uw for component c of mode m (the partner lane, lane ^ 1, holds the
+// other component of the same mode; mask: the lanes taking part)
+template <typename R>
+__device__ __forceinline__ void deriv_uw_c(double2* __restrict__ V, const double* __restrict__ der,
+                                           const double* __restrict__ d0lu, const dd* __restrict__ lindd,
+                                           const BcRows& bc, const Dims& d, int m, double ka, double kz, double k2,
+                                           int c, unsigned mask) {
+  using O = DerivOps<R>;
+  using Q = DerivC<R>;
+  using S = typename Q::S;
+  const int ny = d.ny;
+  const double rk2 = 1.0 / k2;
+  const R au = O::scal(ka * rk2), bu = O::scal(kz * rk2);
+  S vlo[5], vhi[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    vlo[j] = Q::in(*cptr(&V[vidx(d, 1, -1 + j, m)], c));
+    vhi[j] = Q::in(*cptr(&V[vidx(d, 1, ny - 3 + j, m)], c));
+  }
+  auto dot5r = [&](const S* v, const double* cf) {
+    S acc = Q::rm(Q::scal(cf[0]), v[0]);
+#pragma unroll
+    for (int j = 1; j < 5; ++j) acc = acc + Q::rm(Q::scal(cf[j]), v[j]);
+    return acc;
+  };
+  const S f0 = dot5r(vlo, bc.d140), fm1 = dot5r(vlo, bc.d14m1);
+  const S fn = dot5r(vhi, bc.d14n), fn1 = dot5r(vhi, bc.d14np1);
+  {
+    S win[5];
+    win[1] = vhi[1];
+    win[2] = vhi[2];
+    win[3] = vhi[3];
+    win[4] = vhi[4];
+    S x1 = S(), x2 = S();
+    double wnext = *cptr(&V[vidx(d, 1, ny - 3, m)], c);
+    for (int iy = ny - 1; iy >= 1; --iy) {
+      win[0] = Q::in(wnext);
+      if (iy > 1) wnext = *cptr(&V[vidx(d, 1, iy - 3, m)], c);
+      S f = Q::rm(O::d1(der, lindd, iy, 0), win[0]);
+#pragma unroll
+      for (int j = 1; j < 5; ++j) f = f + Q::rm(O::d1(der, lindd, iy, j), win[j]);
+      if (iy == ny - 1) f = f - (Q::rm(O::d0(der, lindd, iy, 3), fn) + Q::rm(O::d0(der, lindd, iy, 4), fn1));
+      if (iy == ny - 2) f = f - Q::rm(O::d0(der, lindd, iy, 4), fn);
+      if (iy == 1) f = f - (Q::rm(O::d0(der, lindd, iy, 1), f0) + Q::rm(O::d0(der, lindd, iy, 0), fm1));
+      if (iy == 2) f = f - Q::rm(O::d0(der, lindd, iy, 0), f0);
+      S x;
+      if constexpr (std::is_same<R, double>::value) {
+        x = O::lu(d0lu, lindd, iy, 2) * fma(-O::lu(d0lu, lindd, iy, 4), x2, fma(-O::lu(d0lu, lindd, iy, 3), x1, f));
+      } else {
+        const S s = Q::rm(O::lu(d0lu, lindd, iy, 3), x1) + Q::rm(O::lu(d0lu, lindd, iy, 4), x2);
+        x = Q::rm(O::lu(d0lu, lindd, iy, 2), f - s);
+      }
+      x2 = x1;
+      x1 = x;
+      Q::park(&V[vidx(d, 2, iy, m)], c, x);
+#pragma unroll
+      for (int j = 4; j > 0; --j) win[j] = win[j - 1];
+    }
+  }
+  {
+    S bm2 = S(), bm1 = fm1;
+    double etn = *cptr(&V[vidx(d, 0, -1, m)], c);
+    S xn = S();
+    for (int iy = -1; iy <= ny + 1; ++iy) {
+      const S et = Q::in(etn);
+      const S xs = xn;
+      if (iy < ny + 1) etn = *cptr(&V[vidx(d, 0, iy + 1, m)], c);
+      if (iy + 1 >= 1 && iy + 1 <= ny - 1) xn = Q::unpark(&V[vidx(d, 2, iy + 1, m)], c);
+      S vp;
+      if (iy == -1) vp = fm1;
+      else if (iy == 0) vp = f0;
+      else if (iy == ny) vp = fn;
+      else if (iy == ny + 1) vp = fn1;
+      else if constexpr (std::is_same<R, double>::value)
+        vp = fma(-O::lu(d0lu, lindd, iy, 1), bm1, fma(-O::lu(d0lu, lindd, iy, 0), bm2, xs));
+      else
+        vp = xs - (Q::rm(O::lu(d0lu, lindd, iy, 0), bm2) + Q::rm(O::lu(d0lu, lindd, iy, 1), bm1));
+      if (iy >= 0 && iy <= ny - 1) {
+        bm2 = bm1;
+        bm1 = vp;
+      }
+      // u = (i kx v' - i kz eta)/k2, w = (i kz v' + i kx eta)/k2: each
+      // component takes the other component of v' and eta
+      const S vo = Q::partner(vp, mask), eo = Q::partner(et, mask);
+      S u, w;
+      if constexpr (std::is_same<R, double>::value) {  // deriv_uw's fused forms
+        if (c == 0) {
+          u = fma(bu, eo, -(au * vo));
+          w = fma(-au, eo, -(bu * vo));
+        } else {
+          u = fma(au, vo, -(bu * eo));
+          w = fma(bu, vo, au * eo);
+        }
+      } else if (c == 0) {
+        u = bu * eo - au * vo;
+        w = R() - bu * vo - au * eo;
+      } else {
+        u = au * vo - bu * eo;
+        w = bu * vo + au * eo;
+      }
+      *cptr(&V[vidx(d, 0, iy, m)], c) = Q::out(u);
+      *cptr(&V[vidx(d, 2, iy, m)], c) = Q::out(w);
+    }
+  }
+}
+}  // namespace
+
+// Eight threads per pair: warp w is the role of k_solve's warp w (system w/2,
+// mode w%2); lane l takes pair l/2 of the block's 16 and component l%2.
+__global__ void __launch_bounds__(128, 4) k_solve_ri(double2* __restrict__ V, const double2* rhs, size_t rcs,
+                                                     int roff, const double* __restrict__ fac,
+                                                     const double* __restrict__ der, const double* __restrict__ d0lu,
+                                                     const double* __restrict__ yint, BcRows bc, Dims d,
+                                                     DevScalars* __restrict__ sc, const dd* __restrict__ lindd,
+                                                     int q_lo, int q_hi) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int sys = w >> 1, t = w & 1, c = lane & 1;
+  const int q = q_lo + blockIdx.x * 16 + (lane >> 1);
+  const bool active = q < q_hi;
+  const int ny = d.ny, nz = d.nz;
+  const int ix = active ? q / (nz + 1) : 0;
+  const int a = active ? q - ix * (nz + 1) : 0;
+  const int nm = (a == 0) ? 1 : 2;
+  int mm[2];
+  mm[0] = ix * d.nzt + nz + a;
+  mm[1] = ix * d.nzt + nz - a;
+  const bool is00 = (ix == 0 && a == 0);
+  const double ka = ix * d.alfa0, kb = a * d.beta0;
+  const double k2 = ka * ka + kb * kb;
+  const double ni = d.ni;
+  const size_t P = d.npairs;
+  const bool ucor = active && is00 && sys == 1 && t == 1;  // unit-forcing response (linsolve_blocking.inc:62-68)
+  const bool mine = active && t < nm;
+  const int m = mm[ucor ? 0 : t];
+  const int vc = ucor ? 2 : (sys == 0 ? 1 : 0);  // field slot written
+  const bool wallrhs = mine && sys == 1 && is00;
+  double bot[5], botm1[5], top[5], topp1[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    bot[j] = sys ? bc.eta0bc[j] : bc.v0bc[j];
+    botm1[j] = sys ? bc.eta0m1bc[j] : bc.v0m1bc[j];
+    top[j] = sys ? bc.etanbc[j] : bc.vnbc[j];
+    topp1[j] = sys ? bc.etanp1bc[j] : bc.vnp1bc[j];
+  }
+  // the wall velocity enters the real component only
+  const double bval0 = (wallrhs && c == 0) ? sc->u0 : 0.0, bvaln = (wallrhs && c == 0) ? sc->uN : 0.0;
+  if (mine || ucor) {
+    const double* fs = fac + (size_t)5 * sys * P + q;
+    const size_t frow = (size_t)kFacPerRow * P;
+    // ---- Step1 bottom-up: x = (b - u1 x(+1) - u2 x(+2)) / d ----
+    const double2* rsrc = rhs + (sys == 0 ? rcs : 0);
+    double x1 = 0.0, x2 = 0.0;
+    double bn = ucor ? (c == 0 ? 1.0 : 0.0) : *cptr(&rsrc[(size_t)(ny - 1 + roff) * d.nmodes + m], c);
+    const double* f = fs + (size_t)(ny - 2) * frow;
+    double dn = f[2 * P], u1n = f[3 * P], u2n = f[4 * P];
+    for (int iy = ny - 1; iy >= 1; --iy) {
+      double b = bn;
+      const double dv = dn, u1 = u1n, u2 = u2n;
+      if (iy > 1) {  // one row ahead (global-load latency)
+        if (!ucor) bn = *cptr(&rsrc[(size_t)(iy - 1 + roff) * d.nmodes + m], c);
+        f -= frow;
+        dn = f[2 * P];
+        u1n = f[3 * P];
+        u2n = f[4 * P];
+      }
+      if (iy - kSolvePrefetch >= 1) {  // and the lines of a row further down
+        const double* fp = f - (size_t)(kSolvePrefetch - 1) * frow;
+        prefetch_l1(fp + 2 * P);
+        prefetch_l1(fp + 3 * P);
+        prefetch_l1(fp + 4 * P);
+        if (!ucor) prefetch_l1(rsrc + (size_t)(iy - kSolvePrefetch + roff) * d.nmodes + m);
+      }
+      if (wallrhs) {
+        if (iy == 1) b = b - sc->wallrhs[0 + c];
+        if (iy == 2) b = b - sc->wallrhs[2 + c];
+        if (iy == ny - 2) b = b - sc->wallrhs[4 + c];
+        if (iy == ny - 1) b = b - sc->wallrhs[6 + c];
+      }
+      const double x = dv * fma(-u2, x2, fma(-u1, x1, b));
+      x2 = x1;
+      x1 = x;
+      *cptr(&V[vidx(d, vc, iy, m)], c) = x;
+    }
+    // ---- Step2 top-down: v = x - l2 v(-2) - l1 v(-1); rows 1..3 and ny-3..ny-1 kept ----
+    double lo[3], hi[3];
+    double m2 = 0.0, m1 = 0.0;
+    f = fs;
+    double l2n = f[0], l1n = f[P];
+    double vn = *cptr(&V[vidx(d, vc, 1, m)], c);
+    for (int iy = 1; iy <= ny - 1; ++iy) {
+      const double l2 = l2n, l1 = l1n;
+      const double vcur = vn;
+      if (iy < ny - 1) {
+        f += frow;
+        l2n = f[0];
+        l1n = f[P];
+        vn = *cptr(&V[vidx(d, vc, iy + 1, m)], c);
+      }
+      if (iy + kSolvePrefetch <= ny - 1) {
+        const double* fp = f + (size_t)(kSolvePrefetch - 1) * frow;
+        prefetch_l1(fp);
+        prefetch_l1(fp + P);
+        prefetch_l1(&V[vidx(d, vc, iy + kSolvePrefetch, m)]);
+      }
+      const double nv = fma(-l1, m1, fma(-l2, m2, vcur));
+      *cptr(&V[vidx(d, vc, iy, m)], c) = nv;
+      m2 = m1;
+      m1 = nv;
+      if (iy == 1) lo[0] = nv;
+      if (iy == 2) lo[1] = nv;
+      if (iy == 3) lo[2] = nv;
+      if (iy == ny - 3) hi[0] = nv;
+      if (iy == ny - 2) hi[1] = nv;
+      if (iy == ny - 1) hi[2] = nv;
+    }
+    // wall and ghost values (linsolve_blocking.inc:50-61), per component as dot3/dot4/cdivr
+    auto d3 = [](const double* v, const double* cf) {
+      double s = cf[0] * v[0];
+      s = s + cf[1] * v[1];
+      return s + cf[2] * v[2];
+    };
+    auto d4 = [](const double* v, const double* cf) {
+      double s = cf[0] * v[0];
+      s = s + cf[1] * v[1];
+      s = s + cf[2] * v[2];
+      return s + cf[3] * v[3];
+    };
+    const double w0 = (bval0 - d3(lo, bot + 2)) / bot[1];
+    const double rb[4] = {w0, lo[0], lo[1], lo[2]};
+    const double wm1 = (0.0 - d4(rb, botm1 + 1)) / botm1[0];
+    const double wn = (bvaln - d3(hi, top)) / top[3];
+    const double rt[4] = {hi[0], hi[1], hi[2], wn};
+    const double wn1 = (0.0 - d4(rt, topp1)) / topp1[4];
+    *cptr(&V[vidx(d, vc, -1, m)], c) = wm1;
+    *cptr(&V[vidx(d, vc, 0, m)], c) = w0;
+    *cptr(&V[vidx(d, vc, ny, m)], c) = wn;
+    *cptr(&V[vidx(d, vc, ny + 1, m)], c) = wn1;
+  }
+  __syncthreads();  // v, eta (and the unit response) of this block's pairs are in V
+  if (wallrhs && c == 0) {  // mean flow (linsolve_blocking.inc:62-97), both components
+    double fu = 0.0, fw = 0.0, fc = 0.0;
+    for (int iy = 1, k = 0; iy <= ny - 1; iy += 2, ++k) {
+      const double a1 = yint[3 * k], a2 = yint[3 * k + 1], a3 = yint[3 * k + 2];
+      const double2 e0 = V[vidx(d, 0, iy - 1, m)], e1 = V[vidx(d, 0, iy, m)], e2 = V[vidx(d, 0, iy + 1, m)];
+      const double2 u0 = V[vidx(d, 2, iy - 1, m)], u1 = V[vidx(d, 2, iy, m)], u2 = V[vidx(d, 2, iy + 1, m)];
+      fu = fu + a1 * e0.x + a2 * e1.x + a3 * e2.x;
+      fw = fw + a1 * e0.y + a2 * e1.y + a3 * e2.y;
+      fc = fc + a1 * u0.x + a2 * u1.x + a3 * u2.x;
+    }
+    double corrpx = sc->corrpx, corrpz = sc->corrpz;
+    const bool cx = fabs(d.meanflowx) > 1.0e-7 && !d.cpi;
+    const bool cz_ = fabs(d.meanflowz) > 1.0e-7 && !d.cpi;
+    if (cx) corrpx = (d.meanflowx - fu) / fc;
+    if (cz_) corrpz = (d.meanflowz - fw) / fc;
+    for (int iy = -1; iy <= ny + 1; ++iy) {
+      const double2 et = V[vidx(d, 0, iy, m)];
+      const double uc = V[vidx(d, 2, iy, m)].x;
+      double U = et.x, W = et.y;
+      if (cx) U = U + corrpx * uc;
+      if (cz_) W = W + corrpz * uc;
+      V[vidx(d, 0, iy, m)] = make_double2(U, 0.0);
+      V[vidx(d, 2, iy, m)] = make_double2(W, 0.0);
+    }
+    sc->fr[0] = fu; sc->fr[1] = fw; sc->fr[2] = fc;
+    sc->corrpx = corrpx; sc->corrpz = corrpz;
+    if (d.cpi) {
+      if (d.cpi_type == 0) sc->meanpx = (1 - d.gamma) * 6 * ni / fu;
+      else sc->meanpx = (1.5 / d.gamma) * fu * ni;
+    }
+  }
+  const bool takes = active && !is00 && sys == 0 && t < nm;  // the same for both lanes of a pair
+  const unsigned mask = __ballot_sync(0xffffffffu, takes);
+  if (!takes) return;
+  if (lindd) deriv_uw_c<dd>(V, der, d0lu, lindd, bc, d, mm[t], ka, (t == 0 ? 1.0 : -1.0) * kb, k2, c, mask);
+  else deriv_uw_c<double>(V, der, d0lu, lindd, bc, d, mm[t], ka, (t == 0 ? 1.0 : -1.0) * kb, k2, c, mask);
+}
+
 void launch_factor(const SolveLaunch& L, cudaStream_t s) {
   if (L.q_hi <= L.q_lo) return;
   const unsigned grid = (unsigned)((L.q_hi - L.q_lo + 31) / 32);
@@ -1165,6 +1494,12 @@ void launch_linsolve(const SolveLaunch& L, cudaStream_t s) {
     return;
   }
   if (!L.factored) launch_factor(L, s);
+  if (L.split_solve == 3) {
+    k_solve_ri<<<(unsigned)((L.q_hi - L.q_lo + 15) / 16), 128, 0, s>>>(
+        L.V, L.rhs_src, L.rhs_cstride, L.rhs_plane_off, L.fac, L.der, L.d0lu, L.yint, L.bc, L.d, L.sc,
+        (const dd*)L.lindd, L.q_lo, L.q_hi);
+    return;
+  }
   if (L.split_solve == 2) {
     k_linsolve<true><<<grid, 64, 0, s>>>(L.V, L.rhs_src, L.rhs_cstride, L.rhs_plane_off, L.fac, L.der, L.d0lu, L.yint,
                                          L.bc, L.d, L.lambda, L.ode[0], L.lambda_from_dt, L.sc, (const dd*)L.lindd,

@@ -150,8 +150,9 @@ const char* chgpu_ensemble_last_error(const chgpu_ensemble* e);
  * per pair), as those two with each substep's factorisation on a side
  * stream, overlapping the substep's transforms (it needs only dt), or with
  * the factorisation ahead and the fused kernel's two threads per pair
- * substituting; and the step on one stream or in two kx halves, timed as
- * whole steps.  Keeps the fastest; the field, the RK history and the module
+ * substituting, or with the factorisation ahead and eight threads per pair
+ * substituting (one per system, mode and real / imaginary component); and
+ * the step on one stream or in two kx halves, timed as whole steps.  Keeps the fastest; the field, the RK history and the module
  * scalars are saved and put back, and the results of a step do not depend on
  * the tiles.  Optional: without it the handle uses tiles sized from the
  * shared-memory budget, the split solve with the factorisation ahead below
@@ -162,8 +163,9 @@ int chgpu_autotune(chgpu_handle* h);
 /* tiles = {z columns per block, x rows per block, x-row variant, z threads
  *          per block, x threads per block, solve form (1: fused, 2: split,
  *          3: split with the factorisation ahead on a side stream, 4: the
- *          factorisation ahead, fused-kernel substitutions), step halves (1
- *          or 2)}.  z columns 0: the
+ *          factorisation ahead, fused-kernel substitutions, 5: the
+ *          factorisation ahead, eight threads per pair), step halves (1 or
+ *          2)}.  z columns 0: the
  * register-blocked z kernels (compile-time plans for nzd = 32, 48, 64, 96,
  * 192, 384, 768, 1536); x-row variant 1-3: the generic kernel with its
  * registers capped for that many 256-thread blocks per SM, 4 and 5: the

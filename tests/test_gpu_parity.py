@@ -183,7 +183,7 @@ def test_autotuned_tiles_give_identical_steps(gpu_lib, prec):
     with pytest.raises(ChannelError):
         u.set_tiles((9, 3, 1, 256, 256, 1, 1))
     with pytest.raises(ChannelError):
-        u.set_tiles(tiles[:5] + (5, 1))
+        u.set_tiles(tiles[:5] + (6, 1))
     for h in (g, t, u):
         h.close()
 
@@ -217,16 +217,17 @@ def test_stepped_field_is_divergence_free(gpu_lib, prec, tol):
 def test_solve_forms_are_identical(gpu_lib, prec):
     """The fused solve (two threads per pair), the factorisation +
     substitution kernels (four threads per pair), those with the
-    factorisation ahead on a side stream, and the factorisation ahead with the
-    fused kernel's two threads per pair substituting, each on one stream and
-    in two halves, give the same field and Runtimedata bit for bit: the
+    factorisation ahead on a side stream, the factorisation ahead with the
+    fused kernel's two threads per pair substituting, and the factorisation
+    ahead with eight threads per pair (one per component), each on one stream
+    and in two halves, give the same field and Runtimedata bit for bit: the
     autotuner's choice among them changes nothing but the time."""
     p, V0, _, g = make("small", 0.02, 6, prec)
     from channel_gb300 import Channel
 
     base = g.tiles()
     out = []
-    for form, halves in ((1, 1), (2, 1), (3, 1), (4, 1), (1, 2), (2, 2), (3, 2), (4, 2)):
+    for form, halves in ((1, 1), (2, 1), (3, 1), (4, 1), (5, 1), (1, 2), (2, 2), (3, 2), (4, 2), (5, 2)):
         with Channel(p, prec) as h:
             h.set_tiles(base[:5] + (form, halves))
             h.upload(V0)
