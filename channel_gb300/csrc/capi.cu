@@ -73,6 +73,7 @@ struct chgpu_handle {
   int solve_form = 1;
   cudaStream_t stream2 = nullptr, stream3 = nullptr;
   cudaEvent_t ev_vv = nullptr, ev_solved = nullptr, ev_fac_fork = nullptr, ev_factored = nullptr;
+  cudaEvent_t ev_copy_fork = nullptr, ev_copy_join = nullptr;  // the two-stream field upload
   // device buffers
   double2* V = nullptr;
   void* old = nullptr;
@@ -640,6 +641,8 @@ void release(chgpu_handle* h) {
   if (h->ev_vv) cudaEventDestroy(h->ev_vv);
   if (h->ev_solved) cudaEventDestroy(h->ev_solved);
   if (h->ev_fac_fork) cudaEventDestroy(h->ev_fac_fork);
+  if (h->ev_copy_fork) cudaEventDestroy(h->ev_copy_fork);
+  if (h->ev_copy_join) cudaEventDestroy(h->ev_copy_join);
   if (h->ev_factored) cudaEventDestroy(h->ev_factored);
   if (h->stream2) cudaStreamDestroy(h->stream2);
   if (h->stream3) cudaStreamDestroy(h->stream3);
@@ -745,6 +748,8 @@ int chgpu_create(const chgpu_params* p, chgpu_handle** out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream3, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fac_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_factored, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_copy_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_copy_join, cudaEventDisableTiming);
     if (e != cudaSuccess) { rc = cuda_fail(h, e, "cudaStreamCreate"); break; }
     e = conv_set_smem_limits();
     if (e != cudaSuccess) { rc = cuda_fail(h, e, "cudaFuncSetAttribute"); break; }
@@ -866,7 +871,18 @@ int chgpu_upload_field(chgpu_handle* h, const double* V) {
   if (!h || !V) return fail(h, CHGPU_E_PARAM, "chgpu_upload_field: null argument");
   const size_t n = (size_t)3 * h->d.nplanes * h->d.nmodes;
   double2* stage = reinterpret_cast<double2*>(h->Pb);
-  CK(h, cudaMemcpyAsync(stage, V, sizeof(double2) * n, cudaMemcpyHostToDevice, h->stream));
+  // the two halves on two streams: one host-to-device copy of pinned memory
+  // measured ~110 GB/s on GB300, two concurrent ones ~210 GB/s; both start
+  // after the work already on the handle's stream (the staging buffer is
+  // step scratch) and the transposes wait for both
+  const size_t half = n / 2;
+  CK(h, cudaEventRecord(h->ev_copy_fork, h->stream));
+  CK(h, cudaStreamWaitEvent(h->stream2, h->ev_copy_fork, 0));
+  CK(h, cudaMemcpyAsync(stage, V, sizeof(double2) * half, cudaMemcpyHostToDevice, h->stream));
+  CK(h, cudaMemcpyAsync(stage + half, V + 2 * half, sizeof(double2) * (n - half), cudaMemcpyHostToDevice,
+                        h->stream2));
+  CK(h, cudaEventRecord(h->ev_copy_join, h->stream2));
+  CK(h, cudaStreamWaitEvent(h->stream, h->ev_copy_join, 0));
   // restart order per component: [mode][iy] -> device [iy][mode]
   launch_transpose(stage, h->V, h->d.nmodes, h->d.nplanes, 3, h->stream);
   h->launches += 1;
