@@ -324,7 +324,8 @@ int upload_pack_roots(chgpu_handle* h, void** dst, int n, long double scale) {
 }
 
 // per-pass twiddles of a register-blocked plan (rfft.cuh): pass p >= 1 at
-// rplan_twoff(p), R-1 forward roots w_{Ns R}^{r k} (r = 1..R-1) per k < Ns
+// rplan_twoff(p), R-1 forward roots w_{Ns R}^{r k} (r = 1..R-1) per k < Ns,
+// padded to R per k in FP32 tables
 template <typename V2>
 int upload_rplan_twiddles(chgpu_handle* h, void** dst, int n, bool xplan = false) {
   using T = decltype(V2::x);
@@ -332,13 +333,13 @@ int upload_rplan_twiddles(chgpu_handle* h, void** dst, int n, bool xplan = false
   if (!(xplan ? xlen_plan(n, &E, &TPR) : rlen_plan(n, &E, &TPR))) return 0;
   const int np = rplan_passes(E, TPR);
   const int tail = std::is_same<V2, double2>::value ? rplan_tailsize(E) : 0;
-  std::vector<V2> w(std::max(1, rplan_twsize(E, TPR) + tail));
+  std::vector<V2> w(std::max(1, rplan_twsize<V2>(E, TPR) + tail));
   if constexpr (std::is_same<V2, double2>::value) {  // the composite first pass's twiddled DFTs (rpass_first)
     for (int k1 = 1; k1 <= 2 && tail > 0; ++k1)
-      lf_stage_entries(&w[rplan_twsize(E, TPR) + (k1 - 1) * (E / 3 - 1)], 3, E / 3, k1);
+      lf_stage_entries(&w[rplan_twsize<V2>(E, TPR) + (k1 - 1) * (E / 3 - 1)], 3, E / 3, k1);
   }
   for (int p = 1; p < np; ++p) {
-    const int R = rplan_radix(E, TPR, p), Ns = rplan_ns(E, TPR, p), off = rplan_twoff(E, TPR, p);
+    const int R = rplan_radix(E, TPR, p), Ns = rplan_ns(E, TPR, p), off = rplan_twoff<V2>(E, TPR, p);
     if constexpr (std::is_same<V2, double2>::value) {  // every pass after the first has a power-of-two radix
       for (int k = 0; k < Ns; ++k) lf_stage_entries(&w[off + k * (R - 1)], Ns, R, k);
       continue;
@@ -347,7 +348,7 @@ int upload_rplan_twiddles(chgpu_handle* h, void** dst, int n, bool xplan = false
       for (int r = 1; r < R; ++r) {
         const long double ang = 2.0L * 3.14159265358979323846264338327950288L * (long double)(r * k) /
                                 (long double)(Ns * R);
-        V2& e = w[off + k * (R - 1) + r - 1];
+        V2& e = w[off + k * tw_per_k<V2>(R) + r - 1];
         e.x = from_ld<T>(cosl(ang));
         e.y = from_ld<T>(-sinl(ang));
       }

@@ -62,14 +62,20 @@ __host__ __device__ constexpr int rplan_ns(int E, int TPR, int p) {
   for (int q = 1; q < p; ++q) ns *= rplan_radix(E, TPR, q);
   return p == 0 ? 1 : ns;
 }
-// offset of pass p's twiddles in the plan's table: R-1 values per k < Ns
-__host__ __device__ constexpr int rplan_twoff(int E, int TPR, int p) {
+// table entries per butterfly position k of a radix-R pass: the R-1
+// twiddles, padded to R in FP32 tables so that twiddle pairs are 16-byte
+// loads (load_twiddles)
+template <typename V> __host__ __device__ constexpr int tw_per_k(int R) {
+  return std::is_same<V, float2>::value ? R : R - 1;
+}
+// offset of pass p's twiddles in the plan's table: tw_per_k values per k < Ns
+template <typename V> __host__ __device__ constexpr int rplan_twoff(int E, int TPR, int p) {
   int off = 0;
-  for (int q = 1; q < p; ++q) off += rplan_ns(E, TPR, q) * (rplan_radix(E, TPR, q) - 1);
+  for (int q = 1; q < p; ++q) off += rplan_ns(E, TPR, q) * tw_per_k<V>(rplan_radix(E, TPR, q));
   return off;
 }
-__host__ __device__ constexpr int rplan_twsize(int E, int TPR) {
-  return rplan_twoff(E, TPR, rplan_passes(E, TPR));
+template <typename V> __host__ __device__ constexpr int rplan_twsize(int E, int TPR) {
+  return rplan_twoff<V>(E, TPR, rplan_passes(E, TPR));
 }
 
 // padded index of an exchange buffer
@@ -94,7 +100,7 @@ template <int E, int TPR, int SIGN, typename V>
 __device__ __forceinline__ void rpass_first(V (&a)[E], const V* __restrict__ tw) {
   if constexpr (std::is_same<V, double2>::value && E % 3 == 0 && is_pow2c(E / 3)) {
     constexpr int P = E / 3;
-    const V* tail = tw + rplan_twsize(E, TPR);
+    const V* tail = tw + rplan_twsize<V>(E, TPR);
 #pragma unroll
     for (int r2 = 0; r2 < P; ++r2) {
       V b[3] = {a[r2], a[P + r2], a[2 * P + r2]};
@@ -126,24 +132,30 @@ __host__ __device__ constexpr int rplan_tailsize(int E) {
 }
 
 // The R-1 twiddles w^1..w^(R-1) of one butterfly from its run of the
-// table.  TW_PRODUCTS (FP32 only): only w^1, w^2, w^4 are loaded and the
-// others formed as products (w^3 = w w^2, w^5 = w w^4, w^6 = w^2 w^4,
-// w^7 = w^3 w^4: at most two more roundings, ~1e-7), which cuts the loads
-// that bound these latency-limited kernels (measured 3-4% faster on GB300);
-// FP64 and double-float load every value (their multiplications bound them).
+// table.  TW_PRODUCTS (FP32 only, whose runs are padded to R entries): a
+// radix-8 butterfly loads w^1..w^4 as two 16-byte loads and forms w^5, w^6,
+// w^7 as products with w^4 (one more rounding, ~1e-7), a radix-4 one loads
+// w^1, w^2 as one and forms w^3; fewer loads for these latency-limited
+// kernels (products in place of loads measured 3-4% faster on GB300; the
+// paired loads measured even).  FP64 and double-float load every value
+// (their multiplications bound them).
 constexpr bool TW_PRODUCTS = true;
 template <int R, typename V> __device__ __forceinline__ void load_twiddles(const V* w, V (&tw)[R]) {
   if constexpr (TW_PRODUCTS && std::is_same<V, float2>::value && R == 8) {
-    tw[1] = ldg_v(w);
-    tw[2] = ldg_v(w + 1);
-    tw[4] = ldg_v(w + 3);
-    tw[3] = cmul(tw[1], tw[2]);
+    // w^1..w^4 as two 16-byte loads (the run is padded to 8 entries)
+    const float4 a = __ldg(reinterpret_cast<const float4*>(w));
+    const float4 b = __ldg(reinterpret_cast<const float4*>(w + 2));
+    tw[1] = make_float2(a.x, a.y);
+    tw[2] = make_float2(a.z, a.w);
+    tw[3] = make_float2(b.x, b.y);
+    tw[4] = make_float2(b.z, b.w);
     tw[5] = cmul(tw[1], tw[4]);
     tw[6] = cmul(tw[2], tw[4]);
     tw[7] = cmul(tw[3], tw[4]);
   } else if constexpr (TW_PRODUCTS && std::is_same<V, float2>::value && R == 4) {
-    tw[1] = ldg_v(w);
-    tw[2] = ldg_v(w + 1);
+    const float4 a = __ldg(reinterpret_cast<const float4*>(w));
+    tw[1] = make_float2(a.x, a.y);
+    tw[2] = make_float2(a.z, a.w);
     tw[3] = cmul(tw[1], tw[2]);
   } else {
 #pragma unroll
@@ -182,7 +194,7 @@ __device__ __forceinline__ void rpass_store(V (&a)[E], V* buf, int t, const V* _
     constexpr int R = rplan_radix(E, TPR, P);
     constexpr int Ns = rplan_ns(E, TPR, P);
     constexpr int B = E / R;
-    const V* twp = tw + rplan_twoff(E, TPR, P);
+    const V* twp = tw + rplan_twoff<V>(E, TPR, P);
 #pragma unroll
     for (int i = 0; i < B; ++i) {
       const int j = t + TPR * i;
@@ -190,7 +202,7 @@ __device__ __forceinline__ void rpass_store(V (&a)[E], V* buf, int t, const V* _
       V b[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) b[r] = a[i + r * B];
-      twiddled_dft<R, SIGN>(b, twp + k * (R - 1));
+      twiddled_dft<R, SIGN>(b, twp + k * tw_per_k<V>(R));
       const int base = (j - k) * R + k;
 #pragma unroll
       for (int r = 0; r < R; ++r) {
@@ -225,14 +237,14 @@ __device__ __forceinline__ void rpass_last_any(V (&a)[E], int t, const V* __rest
     constexpr int Ns = rplan_ns(E, TPR, P);
     constexpr int B = E / R;
     static_assert(Ns * R == E * TPR, "last pass");
-    const V* twp = tw + rplan_twoff(E, TPR, P);
+    const V* twp = tw + rplan_twoff<V>(E, TPR, P);
 #pragma unroll
     for (int i = 0; i < B; ++i) {
       const int j = t + TPR * i;  // < Ns, so k = j
       V b[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) b[r] = a[i + r * B];
-      twiddled_dft<R, SIGN>(b, twp + j * (R - 1));
+      twiddled_dft<R, SIGN>(b, twp + j * tw_per_k<V>(R));
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         if constexpr (TO_REGS) a[i + r * B] = b[r];
